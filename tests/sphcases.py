@@ -1,0 +1,77 @@
+"""Shared helpers for the parity tests: golden-case loading, oracle drivers,
+error norms."""
+import os
+
+import numpy as np
+
+HERE = os.path.dirname(os.path.abspath(__file__))
+GOLDEN = os.path.join(HERE, "golden")
+
+STATE_FIELDS = ("m", "rho", "p", "c", "drho", "h", "x", "y", "vx", "vy", "ax", "ay",
+                "xsphx", "xsphy", "x0", "y0", "vx0", "vy0", "rho0")
+
+SOLVER_CASES = ["solver_tank_cubic", "solver_tank_gauss", "solver_tank_xsph", "solver_tank_sumdens",
+                "solver_tank_dynh", "solver_tank_euler", "solver_lattice_cubic", "solver_lattice_gauss",
+                "solver_alias"]
+
+
+def load(name):
+    return np.load(os.path.join(GOLDEN, name if name.endswith(".npz") else name + ".npz"))
+
+
+def load_case(name):
+    z = load(name)
+    meta = {k[5:]: z[k].item() for k in z.files if k.startswith("meta_")}
+    init = {k: z["init_" + k] for k in STATE_FIELDS + ("label",)}
+    ev = {k: z["eval_" + k] for k in STATE_FIELDS + ("label",)}
+    steps = []
+    for s in range(int(meta["steps"])):
+        steps.append({k: z["step%d_%s" % (s + 1, k)] for k in STATE_FIELDS + ("label",)})
+    return meta, init, ev, steps, z["dts"]
+
+
+def rel_err(a, b):
+    """Norm-wise relative error ||a - b|| / ||b|| (absolute when ||b|| == 0)."""
+    a = np.asarray(a, dtype=np.float64)
+    b = np.asarray(b, dtype=np.float64)
+    d = np.linalg.norm(a - b)
+    n = np.linalg.norm(b)
+    return d / n if n > 0 else d
+
+
+def oracle_params(meta):
+    import oracle
+    return oracle.wcsph_params(meta["height"], meta["r0"], 1000.0, use_xsph=bool(meta["useXSPH"]),
+                               use_summation_density=bool(meta["sumdens"]), kernel=int(meta["kernel"]))
+
+
+def oracle_eval(meta, init, nthreads=1):
+    import oracle
+    P = oracle.Particles(arrays=init)
+    nn = oracle.NN(2.0)
+    h_fixed = meta["h"] if meta["h"] > 0 else 0.0
+    st = oracle.compute(oracle_params(meta), nn, P, h_fixed, nthreads)
+    return P, st
+
+
+def oracle_steps(meta, init, nsteps, nthreads=1):
+    import oracle
+    P = oracle.Particles(arrays=init)
+    nn = oracle.NN(2.0)
+    h_fixed = meta["h"] if meta["h"] > 0 else 0.0
+    dts = oracle.run(oracle_params(meta), nn, P, nsteps, h_fixed=h_fixed,
+                     dt_fixed=meta["fixed_dt"] if meta["fixed_dt"] > 0 else 0.0,
+                     gamma_c=meta["gamma_c"], gamma_f=0.25, damping=0.0, integrator=int(meta["integrator"]),
+                     pec_use_xsph=bool(meta["useXSPH"]), pec_strict=bool(meta["strict"]), nthreads=nthreads)
+    return P, dts
+
+
+def compare_state(got, want, fields, tol):
+    """Return {field: rel_err} for fields whose error exceeds tol."""
+    bad = {}
+    for k in fields:
+        g = got[k] if isinstance(got, dict) else getattr(got, k)
+        e = rel_err(g, want[k])
+        if not (e <= tol):
+            bad[k] = e
+    return bad
