@@ -1,0 +1,372 @@
+#!/usr/bin/env python
+"""WCSPH throughput benchmark (particle-steps/s) on one or more GB300s.
+
+Workload (default ``lattice1m``): the 1M-particle lattice of the single
+derivative evaluation configuration -- 1000 x 1000 fluid particles at
+dx = 0.01, jitter U(+-0.05 dx), v ~ N(0, 0.1), rho = 1000 (1 + U(+-0.01)),
+h = 1.3 dx, cubic spline, no boundaries -- advanced by full PEC time steps.
+One step = TimeStep (Courant/force dt) -> PEC predict -> neighbour build ->
+h reset + Tait EOS + continuity + momentum (one fused pair kernel) -> PEC
+correct, all on the device.  ``dambreak2m`` is the 2M-fluid dam break.
+
+Metric: particle-steps/s = fluid particles x steps / device time of the
+timed steps (whole job: summed over ranks; N > 1 runs independent replicas).
+
+Lines printed: one JSON object (rank 0).  ``--impl reference`` times the CPU
+reference implementation of the step (the C restatement in oracle/, OpenMP
+over all host cores) on a bounded sample of the same workload.
+"""
+import argparse
+import json
+import os
+import subprocess
+import sys
+import threading
+import time
+
+REPO = os.path.dirname(os.path.abspath(__file__))
+for _p in (REPO, os.path.join(REPO, "offshore-sph_gb300")):
+    if _p not in sys.path:
+        sys.path.insert(0, _p)
+
+import numpy as np  # noqa: E402
+
+METRIC = "WCSPH particle-steps/s"
+UNIT = "particle-steps/s"
+PAIR_BYTES = 81     # algorithmic bytes of the pair evaluation per particle (x,y,vx,vy,rho,m,h,label in; drho,ax,ay out)
+STEP_BYTES = 385    # algorithmic bytes of one PEC step per particle (dt 32 + predict 144 + build 24 + pair 81 + correct 104)
+
+
+def workload(name):
+    from sph import scenarios as S
+    if name == "lattice1m":
+        pa = S.jittered_lattice(1000, 1000, 0.01, seed=0)
+        return dict(pa=pa, height=10.0, r0=0.01, h=0.013, kernel=0, gamma_c=0.25, setup=False,
+                    desc="1000x1000 jittered lattice, dx=0.01, h=1.3dx, cubic, no boundaries, PEC step")
+    if name == "lattice1m_gauss":
+        pa = S.jittered_lattice(1000, 1000, 0.01, seed=0)
+        return dict(pa=pa, height=10.0, r0=0.01, h=0.013, kernel=1, gamma_c=0.25, setup=False,
+                    desc="1000x1000 jittered lattice, dx=0.01, h=1.3dx, Gaussian (q<=3), PEC step")
+    if name == "dambreak2m":
+        pa = S.cfg_dam_break_large()
+        return dict(pa=pa, height=20.0, r0=0.01, h=0.013, kernel=0, gamma_c=0.3, setup=True,
+                    desc="10x20 m column at dx=0.01 (2M fluid) in a 40x30 m tank, 2 wall layers at dx/2, "
+                         "cubic, PEC, Courant 0.3")
+    if name == "dambreak3200":
+        pa = S.cfg_dam_break_small()
+        return dict(pa=pa, height=2.0, r0=0.025, h=0.0325, kernel=0, gamma_c=0.3, setup=True,
+                    desc="1x2 m column at dx=0.025 (3200 fluid) in a 4x3 m tank, cubic, PEC, Courant 0.3")
+    raise SystemExit("unknown workload " + name)
+
+
+def lattice_sample(n_side, seed=0):
+    """The same lattice recipe at n_side x n_side (CPU baseline sample)."""
+    from sph import scenarios as S
+    return S.jittered_lattice(n_side, n_side, 0.01, seed=seed)
+
+
+# ---------------------------------------------------------------------------
+class ClockSampler:
+    """nvidia-smi clocks / throttle reasons sampled during the timed region."""
+    Q = ("index,clocks.sm,clocks.max.sm,power.draw,clocks_event_reasons.active,"
+         "clocks_event_reasons.hw_slowdown,clocks_event_reasons.hw_thermal_slowdown,"
+         "clocks_event_reasons.sw_thermal_slowdown,clocks_event_reasons.sw_power_cap")
+
+    def __init__(self, gpu_index):
+        self.gpu = gpu_index
+        self.proc = None
+        self.lines = []
+
+    def start(self):
+        try:
+            self.proc = subprocess.Popen(["nvidia-smi", "-i", str(self.gpu), "--query-gpu=" + self.Q,
+                                          "--format=csv,noheader,nounits", "-lms", "100"],
+                                         stdout=subprocess.PIPE, stderr=subprocess.DEVNULL, text=True)
+            self.t = threading.Thread(target=self._read, daemon=True)
+            self.t.start()
+        except (OSError, FileNotFoundError):
+            self.proc = None
+
+    def _read(self):
+        for line in self.proc.stdout:
+            self.lines.append(line.strip())
+
+    def stop(self):
+        if not self.proc:
+            return {"sm_mhz": None, "sm_max_mhz": None, "reasons": ["nvidia-smi unavailable"], "samples": 0}
+        self.proc.terminate()
+        try:
+            self.proc.wait(timeout=5)
+        except subprocess.TimeoutExpired:
+            self.proc.kill()
+        sm, smax, reasons, power = [], [], set(), []
+        names = ["hw_slowdown", "hw_thermal_slowdown", "sw_thermal_slowdown", "sw_power_cap"]
+        for ln in self.lines:
+            f = [x.strip() for x in ln.split(",")]
+            if len(f) < 9:
+                continue
+            try:
+                sm.append(float(f[1]))
+                smax.append(float(f[2]))
+                power.append(float(f[3]))
+            except ValueError:
+                continue
+            for nm, v in zip(names, f[5:9]):
+                if v.lower().startswith("active"):
+                    reasons.add(nm)
+        return {"sm_mhz": float(np.median(sm)) if sm else None, "sm_max_mhz": max(smax) if smax else None,
+                "power_w_max": max(power) if power else None, "reasons": sorted(reasons), "samples": len(sm)}
+
+
+# ---------------------------------------------------------------------------
+def peaks():
+    p = os.path.join(REPO, "MEASURED_PEAKS.json")
+    if os.path.exists(p):
+        with open(p) as f:
+            d = json.load(f)
+        return float(d["hbm_gbs"]), "measured"
+    return 6800.0, "fallback"
+
+
+def prepare(wl, precision):
+    import torch
+    from sph import core, state
+    pa = wl["pa"]
+    dp = state.DeviceParticles.from_array(pa)
+    wc = core.wcsph_struct(wl["height"], wl["r0"], 1000.0)
+    cfg = core.config_struct(kernel=wl["kernel"], precision=precision, h_fixed=wl["h"], cfl_c=wl["gamma_c"],
+                             cfl_f=0.25)
+    if wl["setup"]:
+        core.initialize(dp, wc, cfg)
+    else:
+        # Solver.setup without the hydrostatic initialise: h, p, c of fluid
+        f = dp.label == 0
+        dp.h[f] = wl["h"]
+        core.eos(dp, wc)
+    ws = state.DeviceWorkspace(dp.n)
+    torch.cuda.synchronize()
+    return dp, wc, cfg, ws
+
+
+def time_steps(core, dp, wc, cfg, ws, k):
+    import torch
+    s, e = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
+    torch.cuda.synchronize()
+    s.record()
+    core.run(dp, wc, cfg, ws, k)
+    e.record()
+    torch.cuda.synchronize()
+    return s.elapsed_time(e) / 1e3
+
+
+def e2e_steps(core, dp, wc, cfg, ws, k, pa):
+    """Steps through the C ABI with the particle state on the HOST: each step
+    copies its inputs host -> device (pinned) and its results back."""
+    import torch
+    fin = ("x", "y", "vx", "vy", "rho", "ax", "ay", "drho", "m", "h", "c")
+    fout = ("x", "y", "vx", "vy", "rho", "p", "drho", "ax", "ay")
+    host = {f: torch.from_numpy(np.ascontiguousarray(dp.fields[f].cpu().numpy())).pin_memory() for f in fin}
+    host["p"] = torch.empty(dp.n, dtype=torch.float64).pin_memory()
+    host_label = torch.from_numpy(dp.label.cpu().numpy()).pin_memory()
+    h2d = sum(host[f].numel() * 8 for f in fin) + host_label.numel()
+    d2h = dp.n * 8 * len(fout)
+    s, e = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
+    torch.cuda.synchronize()
+    s.record()
+    for _ in range(k):
+        for f in fin:
+            dp.fields[f].copy_(host[f], non_blocking=True)
+        dp.label.copy_(host_label, non_blocking=True)
+        core.run(dp, wc, cfg, ws, 1)
+        for f in fout:
+            host[f].copy_(dp.fields[f], non_blocking=True)
+    e.record()
+    torch.cuda.synchronize()
+    return s.elapsed_time(e) / 1e3, h2d, d2h
+
+
+def cpu_baseline(wl, budget_s=10.0):
+    """The oracle (C restatement of the reference's step) on a bounded sample:
+    a 200 x 200 lattice of the same recipe, PEC steps, all host threads."""
+    import oracle
+    threads = oracle.max_threads()
+    side = 200
+    pa = lattice_sample(side)
+    d = {k: pa[k] for k in pa.dtype.names if k != "deleted"}
+    d["h"][:] = wl["h"]
+    par = oracle.wcsph_params(wl["height"], wl["r0"], 1000.0, kernel=wl["kernel"])
+    d["p"] = oracle.eos(d["label"], d["rho"], par)
+    d["c"][:] = par.co
+    P = oracle.Particles(arrays=d)
+    nn = oracle.NN(2.0)
+    oracle.run(par, nn, P, 1, h_fixed=wl["h"], gamma_c=wl["gamma_c"], nthreads=threads)
+    steps, t0 = 0, time.perf_counter()
+    while True:
+        oracle.run(par, nn, P, 1, h_fixed=wl["h"], gamma_c=wl["gamma_c"], nthreads=threads)
+        steps += 1
+        el = time.perf_counter() - t0
+        if el >= budget_s or steps >= 200:
+            break
+    nf = int(np.sum(P.label == 0))
+    return {"value": nf * steps / el, "unit": UNIT, "cores": threads, "kind": "port",
+            "sample": "%dx%d lattice of the same recipe (%d fluid), %d PEC steps, OpenMP over particles"
+                      % (side, side, nf, steps)}
+
+
+def run_reference(args, wl_name):
+    """--impl reference: the CPU reference implementation of the step (the C
+    restatement in oracle/, all host threads) on a bounded sample."""
+    import oracle
+    rank = int(os.environ.get("RANK", "0"))
+    if rank != 0:
+        return
+    oracle.build()
+    wl = workload(wl_name)
+    threads = oracle.max_threads()
+    # size the per-step sample so that warmup + steps take about a minute
+    side = 1000 if wl_name.startswith("lattice") else None
+    par = oracle.wcsph_params(wl["height"], wl["r0"], 1000.0, kernel=wl["kernel"])
+
+    def make(side_):
+        if side_ is None:
+            pa = wl["pa"]
+        else:
+            pa = lattice_sample(side_)
+        d = {k: pa[k] for k in pa.dtype.names if k != "deleted"}
+        P = oracle.Particles(arrays=d)
+        if wl["setup"]:
+            oracle.setup(P, par, wl["height"], wl["h"])
+        else:
+            P.h[P.label == 0] = wl["h"]
+            P.p[:] = oracle.eos(P.label, P.rho, par)
+            P.c[:] = par.co
+        return P
+
+    P = make(side)
+    nn = oracle.NN(2.0)
+    t0 = time.perf_counter()
+    oracle.run(par, nn, P, 1, h_fixed=wl["h"], gamma_c=wl["gamma_c"], nthreads=threads)
+    per_step = time.perf_counter() - t0
+    total = args.steps + args.warmup
+    if side is not None and per_step * total > 60.0:
+        side = max(100, int(side * (60.0 / (per_step * total)) ** 0.5))
+        P = make(side)
+    for _ in range(args.warmup):
+        oracle.run(par, nn, P, 1, h_fixed=wl["h"], gamma_c=wl["gamma_c"], nthreads=threads)
+    t0 = time.perf_counter()
+    oracle.run(par, nn, P, args.steps, h_fixed=wl["h"], gamma_c=wl["gamma_c"], nthreads=threads)
+    el = time.perf_counter() - t0
+    nf = int(np.sum(P.label == 0))
+    v = nf * args.steps / el
+    sample = ("%s: %s" % (wl_name, "%dx%d lattice sample (%d fluid)" % (side, side, nf) if side else
+                          "full workload (%d fluid)" % nf)) + ", PEC steps, OpenMP over particles"
+    out = {"impl": "reference", "metric": METRIC, "value": v, "unit": UNIT, "n_gpus": args.gpus,
+           "steps": args.steps, "warmup": args.warmup, "ms_per_step": el / args.steps * 1e3,
+           "higher_is_better": True, "scaling": "weak", "vs_baseline": None, "dtype": "f64", "data": "synthetic",
+           "config": {"workload": wl["desc"], "sample": sample},
+           "cpu_baseline": {"value": v, "unit": UNIT, "cores": threads, "kind": "port", "sample": sample},
+           "e2e": {"value": v, "unit": UNIT, "h2d_bytes_per_step": 0, "d2h_bytes_per_step": 0}}
+    print(json.dumps(out))
+
+
+def main():
+    ap = argparse.ArgumentParser()
+    ap.add_argument("--gpus", type=int, default=1)
+    ap.add_argument("--steps", type=int, default=2000)
+    ap.add_argument("--warmup", type=int, default=10)
+    ap.add_argument("--impl", default="ours", choices=["ours", "reference"])
+    ap.add_argument("--workload", default="lattice1m")
+    ap.add_argument("--precision", default="mixed", choices=["mixed", "fp64"])
+    ap.add_argument("--no-extras", action="store_true", help="skip the FP64 / e2e / CPU / profile passes")
+    args = ap.parse_args()
+    if args.warmup < 3:
+        raise SystemExit("--warmup must be >= 3")
+    if args.impl == "reference":
+        run_reference(args, args.workload)
+        return
+
+    import torch
+    import torch.distributed as dist
+    rank = int(os.environ.get("RANK", "0"))
+    world = int(os.environ.get("WORLD_SIZE", "1"))
+    local = int(os.environ.get("LOCAL_RANK", "0"))
+    torch.cuda.set_device(local)
+    if world > 1:
+        dist.init_process_group("nccl", device_id=torch.device("cuda", local))
+    from sph import build as sph_build
+    sph_build.build()
+    from sph import core
+
+    wl = workload(args.workload)
+    nfluid = int(np.sum(wl["pa"]["label"] == 0))
+    dp, wc, cfg, ws = prepare(wl, args.precision)
+    core.run(dp, wc, cfg, ws, args.warmup)
+    ws.check()
+
+    def barrier():
+        if world > 1:
+            dist.barrier()
+
+    clocks = ClockSampler(local)
+    clocks.start()
+    time.sleep(0.3)
+    barrier()
+    el = time_steps(core, dp, wc, cfg, ws, args.steps)
+    barrier()
+    clk = clocks.stop()
+    ws.check()
+    t = torch.tensor([el], dtype=torch.float64, device="cuda")
+    if world > 1:
+        dist.all_reduce(t, op=dist.ReduceOp.MAX)
+    el = float(t.item())
+    value = world * nfluid * args.steps / el
+    launches_per_step = 11
+    out = {"metric": METRIC, "value": value, "unit": UNIT, "n_gpus": world, "steps": args.steps,
+           "warmup": args.warmup, "ms_per_step": el / args.steps * 1e3, "higher_is_better": True,
+           "scaling": "weak", "vs_baseline": None,
+           "dtype": "f32 pair / f64 state" if args.precision == "mixed" else "f64",
+           "data": "synthetic",
+           "config": {"workload": args.workload + ": " + wl["desc"], "n_particles": int(dp.n), "n_fluid": nfluid,
+                      "precision": args.precision, "integrator": "PEC",
+                      "l2": "inputs larger than L2 (state + records ~%.0f MB per step)"
+                            % ((dp.n * (19 * 8 + 1) + ws.buf.numel()) / 1e6),
+                      "parallelism": "replicas" if world > 1 else "single GPU"},
+           "clocks": clk, "gpu_launches": launches_per_step * args.steps + 1}
+    if not args.no_extras and rank == 0:
+        hbm, peak_kind = peaks()
+        kprof = min(args.steps, 50)
+        stages = core.run_profiled(dp, wc, cfg, ws, kprof)
+        pair_s = stages["pair"] / 1e3 / kprof
+        step_s = sum(stages.values()) / 1e3 / kprof
+        ach = dp.n * PAIR_BYTES / pair_s / 1e9
+        out["stages_ms_per_step"] = {k: v / kprof for k, v in stages.items()}
+        out["roofline"] = {"bound": "hbm", "kernel": "k_pair32" if args.precision == "mixed" else "k_pair64",
+                           "achieved": ach, "peak": hbm, "unit": "GB/s", "frac": ach / hbm,
+                           "peak_kind": peak_kind, "traffic": None,
+                           "algorithmic_bytes_per_launch": dp.n * PAIR_BYTES,
+                           "step_achieved_gbs": dp.n * STEP_BYTES / step_s / 1e9}
+        # the GPU's own FP64 path on the same workload
+        if args.precision == "mixed":
+            dp64, wc64, cfg64, ws64 = prepare(wl, "fp64")
+            core.run(dp64, wc64, cfg64, ws64, 3)
+            k64 = max(3, min(args.steps // 10, 200))
+            el64 = time_steps(core, dp64, wc64, cfg64, ws64, k64)
+            ws64.check()
+            v64 = nfluid * k64 / el64
+            out["fp64"] = {"value": v64, "steps": k64, "ms_per_step": el64 / k64 * 1e3,
+                           "mixed_over_fp64": value / world / v64}
+            del dp64, ws64
+        # end to end through host buffers
+        ke = max(3, min(args.steps, 100))
+        el_e, h2d, d2h = e2e_steps(core, dp, wc, cfg, ws, ke, wl["pa"])
+        out["e2e"] = {"value": nfluid * ke / el_e, "unit": UNIT, "h2d_bytes_per_step": h2d,
+                      "d2h_bytes_per_step": d2h, "steps": ke}
+        out["cpu_baseline"] = cpu_baseline(wl)
+    if rank == 0:
+        print(json.dumps(out))
+    if world > 1:
+        dist.destroy_process_group()
+
+
+if __name__ == "__main__":
+    main()

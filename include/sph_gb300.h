@@ -1,0 +1,241 @@
+/*
+ * sph_gb300.h -- C ABI of the GB300-native WCSPH step.
+ *
+ * A drop-in for the hot path of Offshore-SPH's Solver: the cell linked-list
+ * neighbour search, the Tait EOS, continuity, momentum with artificial
+ * viscosity, the Lennard-Jones boundary force, optional XSPH and summation
+ * density, the Courant/force time step and the PEC / Euler integrators.
+ * Every entry point names the reference routine it replaces (paths relative
+ * to the Offshore-SPH repository root).
+ *
+ * Conventions
+ *  - All particle arrays are DEVICE pointers, structure-of-arrays, one entry
+ *    per active particle, in the caller's order (the order of
+ *    particleArray[indexes] in the reference).  Results are written back in
+ *    that order.
+ *  - Nothing here allocates or frees caller memory.  Scratch lives in a
+ *    caller-allocated device workspace sized by sph_workspace_size() and
+ *    prepared once by sph_workspace_init().
+ *  - Every call is asynchronous on the given stream (a cudaStream_t; NULL is
+ *    the legacy default stream) and does no host synchronisation, so a
+ *    sequence of calls may be captured into a CUDA graph.  The exceptions are
+ *    sph_get_status() and sph_workspace_init(), which synchronise.
+ *  - Return value: SPH_OK or an SPH_ERR_* code for errors detected on the host
+ *    (bad arguments, launch failures).  Conditions detected on the device set
+ *    bits in a sticky status word in the workspace, read and cleared with
+ *    sph_get_status().
+ *  - Not re-entrant per workspace: calls that share a workspace must be
+ *    ordered on one stream.  Distinct workspaces are independent.
+ */
+#ifndef SPH_GB300_H
+#define SPH_GB300_H
+
+#include <stddef.h>
+#include <stdint.h>
+
+#ifdef __cplusplus
+extern "C" {
+#endif
+
+#define SPH_ABI_VERSION 1
+
+typedef struct CUstream_st *sph_stream_t; /* identical to cudaStream_t */
+
+/* particle labels (src/Common.py:8-12 ParticleType) */
+enum { SPH_FLUID = 0, SPH_BOUNDARY = 1, SPH_TEMP_BOUNDARY = 2, SPH_COUPLED = 3 };
+
+/* smoothing kernels (src/Kernels/CubicSpline.py, src/Kernels/Gaussian.py) */
+enum { SPH_KERNEL_CUBIC = 0, SPH_KERNEL_GAUSSIAN = 1 };
+
+/* arithmetic of the pair interaction: FP64 throughout, or FP32 pair
+ * arithmetic over FP64 state (positions, velocities, densities, dt and the
+ * integrator stay FP64) */
+enum { SPH_PREC_FP64 = 0, SPH_PREC_MIXED = 1 };
+
+/* integrators (src/Integrators/PEC.py, src/Integrators/Euler.py) */
+enum { SPH_INTEGRATOR_PEC = 0, SPH_INTEGRATOR_EULER = 1 };
+
+/* host-side return codes */
+enum {
+  SPH_OK = 0,
+  SPH_ERR_INVALID_ARGUMENT = 1,
+  SPH_ERR_WORKSPACE_TOO_SMALL = 2,
+  SPH_ERR_CUDA = 3,
+  SPH_ERR_NOT_INITIALISED = 4
+};
+
+/* device status bits (sticky, see sph_get_status) */
+enum {
+  /* a particle's flat cell id is >= n_cells of the reference grid: the
+   * reference writes past heads[] there (src/Tools/NNLinkedList.py:129-141).
+   * Such particles are left out of every neighbour list. */
+  SPH_STATUS_CELL_OVERFLOW = 1u << 0,
+  /* the traversal grid was coarsened to fit the workspace's cell capacity
+   * (results stay exact, the search does more work) */
+  SPH_STATUS_GRID_COARSENED = 1u << 1,
+  /* a position, h or reduction input was not finite */
+  SPH_STATUS_NONFINITE = 1u << 2,
+  /* the reference grid has more than 2^30 cells per axis */
+  SPH_STATUS_GRID_TOO_LARGE = 1u << 3,
+  /* no fluid particle to take the time step from */
+  SPH_STATUS_NO_FLUID = 1u << 4,
+  /* TimeStep's dt fell below 1e-6 (the reference records it, src/Solver.py:219-224) */
+  SPH_STATUS_SMALL_DT = 1u << 5
+};
+
+/* WCSPH method constants, the attributes of src/Methods/WCSPH.py:33-79.
+ * Fill them from the reference's formulas (co = 10 sqrt(2 g H),
+ * B = co^2 rho0 / gamma, D = 5 g H) or set them directly, as the reference
+ * allows (its jitclass attributes are mutable). */
+typedef struct sph_wcsph {
+  double rho0, gamma, co, B, Pb; /* Tait EOS (src/Equations/TaitEOS.py) */
+  double alpha, beta;            /* artificial viscosity (src/Equations/Momentum.py) */
+  double epsilon;                /* XSPH (src/Equations/XSPH.py) */
+  double r0, D, p1, p2;          /* Lennard-Jones boundary (src/Equations/BoundaryForce.py) */
+  double height;                 /* water column height H (TaitEOS_height) */
+  int32_t use_xsph;              /* WCSPH.useXSPH */
+  int32_t use_summation_density; /* WCSPH.useSummationDensity */
+} sph_wcsph_t;
+
+/* Solver / integrator / kernel / neighbour-finder settings */
+typedef struct sph_config {
+  int32_t kernel;       /* SPH_KERNEL_* (the Solver's kernel object) */
+  int32_t precision;    /* SPH_PREC_* */
+  int32_t integrator;   /* SPH_INTEGRATOR_* */
+  int32_t pec_use_xsph; /* PEC(useXSPH=...) (src/Integrators/PEC.py:13) */
+  int32_t pec_strict;   /* PEC(strict=...) */
+  int32_t pad0;
+  double nn_scale;      /* NNLinkedList(scale) -- the Solver uses 2.0 (src/Solver.py:109) */
+  double h_fixed;       /* Solver(h=...): > 0 fixed h for fluid; <= 0: computeH(1.3, m, rho) */
+  double cfl_c, cfl_f;  /* TimeStep.compute gamma_c, gamma_f (src/Solver.py:215 uses 0.25, 0.25) */
+  double damping;       /* Solver damping factor passed to predict/correct */
+  double dt_fixed;      /* Solver(timeStep=...): > 0 fixed dt, else TimeStep */
+} sph_config_t;
+
+/* The active particles as device structure-of-arrays: the fields of
+ * particle_dtype (src/Common.py:26-57), 'deleted' excluded. */
+typedef struct sph_particles {
+  int64_t n;
+  int8_t *label;
+  double *m, *rho, *p, *c, *drho, *h, *x, *y, *vx, *vy, *ax, *ay, *xsphx, *xsphy;
+  double *x0, *y0, *vx0, *vy0, *rho0;
+} sph_particles_t;
+
+/* A caller-allocated device workspace: ptr/bytes is device memory of at least
+ * sph_workspace_size(n_cap, max_cells) bytes; n_cap bounds the particle count
+ * of every call that uses it, max_cells the number of search cells.  The
+ * workspace holds the cell table, the sort permutation, the sorted pair
+ * records and the reduction and status words. */
+typedef struct sph_workspace {
+  void *ptr;
+  size_t bytes;
+  int64_t n_cap;
+  int64_t max_cells;
+} sph_workspace_t;
+
+/* Library ABI version (SPH_ABI_VERSION of the build). */
+int sph_abi_version(void);
+
+/* Bytes of device workspace for up to n particles and max_cells search cells
+ * (max_cells <= 0 picks the default, sph_default_max_cells(n)). */
+int sph_workspace_size(int64_t n, int64_t max_cells, size_t *bytes);
+int64_t sph_default_max_cells(int64_t n);
+
+/* Prepare a workspace (fills in ws->max_cells when it is <= 0): clears the
+ * counters and the status word.  Synchronises the stream. */
+int sph_workspace_init(sph_workspace_t *ws, sph_stream_t stream);
+
+/* Read and clear the sticky device status word (SPH_STATUS_* bits).
+ * Synchronises the stream. */
+int sph_get_status(const sph_workspace_t *ws, uint32_t *status, sph_stream_t stream);
+
+/* Human-readable name of a return code or a single status bit. */
+const char *sph_status_string(int code);
+
+/* WCSPH.initialize + the fluid part of Solver.setup
+ * (src/Methods/WCSPH.py:82-108, src/Solver.py:184-196): for fluid particles
+ * set h (fixed or computeH), rho = TaitEOS_height(y), p = TaitEOS(rho) + Pb,
+ * c = co. */
+int sph_initialize(sph_particles_t *pa, const sph_wcsph_t *w, const sph_config_t *cfg, sph_stream_t stream);
+
+/* WCSPH.compute_pressure and compute_speed_of_sound for every particle
+ * (src/Methods/WCSPH.py:110-149, src/Equations/TaitEOS.py:6-31). */
+int sph_eos(sph_particles_t *pa, const sph_wcsph_t *w, sph_stream_t stream);
+
+/* Kernel.evaluate / Kernel.gradient as elementwise device maps over n values
+ * (src/Kernels/CubicSpline.py:10-70, src/Kernels/Gaussian.py:16-59):
+ * out[j] = W(r[j], h[j]), or the gradient component x[j] dW/dr / r for the
+ * coordinate difference x[j]; sph_gauss_deriv is Gaussian.derivative
+ * (dW/dq).  Arrays are device doubles. */
+int sph_kernel_eval(int kernel, int64_t n, const double *r, const double *h, double *out, sph_stream_t stream);
+int sph_kernel_grad(int kernel, int64_t n, const double *x, const double *r, const double *h, double *out,
+                    sph_stream_t stream);
+int sph_gauss_deriv(int64_t n, const double *r, const double *h, double *out, sph_stream_t stream);
+
+/* NNLinkedList.update (src/Tools/NNLinkedList.py:37-39, 86-141): bins the
+ * particles into the reference's cell grid (origin = min x, y; cell size =
+ * scale * min h, or 1.0 below 1e-6) and builds the sorted cell table in the
+ * workspace. */
+int sph_nn_update(const sph_particles_t *pa, const sph_config_t *cfg, const sph_workspace_t *ws, sph_stream_t stream);
+
+/* NNLinkedList.near(i) for every particle i (src/Tools/NNLinkedList.py:41-84)
+ * on the table of the last sph_nn_update: counts[i] = number of neighbours
+ * (device int64[n]).  Then, with offsets = exclusive prefix sum of counts
+ * (device int64[n+1]), sph_nn_export writes the neighbour indices of i into
+ * idx[offsets[i] .. offsets[i+1]) in ascending index order.  The neighbour
+ * SETS are those of the reference, bit for bit, including its truncated
+ * 3x3-cell stencil and its aliasing of x-overflow cells. */
+int sph_nn_count(const sph_particles_t *pa, const sph_config_t *cfg, const sph_workspace_t *ws, int64_t *counts,
+                 sph_stream_t stream);
+int sph_nn_export(const sph_particles_t *pa, const sph_config_t *cfg, const sph_workspace_t *ws, const int64_t *offsets,
+                  int64_t *idx, sph_stream_t stream);
+
+/* Solver._compute (src/Solver.py:232-256) = NNLinkedList.update, the h reset
+ * (fixed or computeH, src/Tools/SolverTools.py:106-118) and the derivative
+ * loop _loop (src/Tools/SolverTools.py:120-175) as one fused pair kernel:
+ * writes p, c (all particles), h (fluid) and, for fluid particles with at
+ * least one neighbour, drho, ax, ay, xsphx, xsphy.  Also leaves in the
+ * workspace the reductions the next sph_timestep would compute. */
+int sph_compute(sph_particles_t *pa, const sph_wcsph_t *w, const sph_config_t *cfg, const sph_workspace_t *ws,
+                sph_stream_t stream);
+
+/* TimeStep.compute over the fluid particles (src/Equations/TimeStep.py:7-91,
+ * gamma_c = cfg->cfl_c, gamma_f = cfg->cfl_f): dt3[0..2] = {dt, dt_courant,
+ * dt_force} (device doubles).  Sets SPH_STATUS_SMALL_DT when dt < 1e-6. */
+int sph_timestep(const sph_particles_t *pa, const sph_wcsph_t *w, const sph_config_t *cfg, const sph_workspace_t *ws,
+                 double *dt3, sph_stream_t stream);
+
+/* Integrator.predict / correct on the fluid particles (src/Integrators/PEC.py:32-89,
+ * src/Integrators/Euler.py:13-27), dt read from the device double *dt. */
+int sph_predict(sph_particles_t *pa, const sph_config_t *cfg, const double *dt, sph_stream_t stream);
+int sph_correct(sph_particles_t *pa, const sph_config_t *cfg, const double *dt, sph_stream_t stream);
+
+/* nsteps bare time steps of Solver.run's loop body (src/Solver.py:366-410)
+ * with settling and storage left out: dt (TimeStep or cfg->dt_fixed) ->
+ * predict -> _compute -> correct, all on the device.  dt_hist, if not NULL,
+ * receives 3 doubles per step {dt, dt_courant, dt_force} (device memory). */
+int sph_run(sph_particles_t *pa, const sph_wcsph_t *w, const sph_config_t *cfg, const sph_workspace_t *ws, int64_t nsteps,
+            double *dt_hist, sph_stream_t stream);
+
+/* sph_run with a CUDA-event lap after every stage, for measurement: the
+ * time of each stage summed over the steps, in ms, into
+ * stage_ms[SPH_NSTAGES] (host memory).  Synchronises after every stage, so
+ * it is slower than sph_run and cannot be captured in a graph.  The stages
+ * are the parts of Solver.run's step body (src/Solver.py:366-410). */
+enum {
+  SPH_STAGE_TIMESTEP = 0, /* initial TimeStep.compute */
+  SPH_STAGE_PREDICT = 1,  /* integrator.predict fused with the bounds of nn.update */
+  SPH_STAGE_BUILD = 2,    /* rest of nn.update: grid, keys, counting sort */
+  SPH_STAGE_RECORDS = 3,  /* h reset + Tait EOS + sorted pair records */
+  SPH_STAGE_PAIR = 4,     /* the fused pair interaction (+ next TimeStep) */
+  SPH_STAGE_CORRECT = 5,  /* integrator.correct */
+  SPH_NSTAGES = 6
+};
+int sph_run_profiled(sph_particles_t *pa, const sph_wcsph_t *w, const sph_config_t *cfg, const sph_workspace_t *ws,
+                     int64_t nsteps, double *stage_ms, sph_stream_t stream);
+
+#ifdef __cplusplus
+}
+#endif
+
+#endif /* SPH_GB300_H */

@@ -1,0 +1,381 @@
+// capi.cu -- extern "C" entry points of libsph_gb300 (see include/sph_gb300.h).
+#include <string.h>
+
+#include "sph_internal.cuh"
+
+namespace sph {
+
+static size_t align256(size_t v) { return (v + 255) & ~(size_t)255; }
+
+WsLayout make_layout(long long n_cap, long long max_cells) {
+  WsLayout L;
+  size_t off = 0;
+  auto take = [&](size_t bytes) {
+    size_t o = off;
+    off = align256(off + bytes);
+    return o;
+  };
+  size_t n = (size_t)(n_cap > 0 ? n_cap : 1);
+  size_t mc = (size_t)max_cells;
+  L.n_cap = n_cap;
+  L.max_cells = max_cells;
+  L.n_parts = (long long)((mc + 1 + kScanTile - 1) / kScanTile);
+  L.ctrl = take(sizeof(DevCtrl));
+  L.grid = take(sizeof(DevGrid));
+  L.keys = take(n * 4);
+  L.refcell = take(n * 8);
+  L.perm_tmp = take(n * 4);
+  L.keys_sorted = take(n * 4);
+  L.perm = take(n * 4);
+  L.meta = take(n * 8);
+  L.counts = take((mc + 1) * 4);
+  L.cstart = take((mc + 2) * 4);
+  L.scan_part = take((size_t)L.n_parts * 4);
+  L.recA = take(n * 32);
+  L.recB = take(n * 32);
+  L.recC = take(n * 16);
+  L.rho_sd = take(8);
+  L.total = off;
+  return L;
+}
+
+WsPtrs ws_ptrs(const sph_workspace_t *ws) {
+  WsLayout L = make_layout(ws->n_cap, ws->max_cells);
+  char *b = (char *)ws->ptr;
+  WsPtrs p;
+  p.ctrl = (DevCtrl *)(b + L.ctrl);
+  p.grid = (DevGrid *)(b + L.grid);
+  p.keys = (int *)(b + L.keys);
+  p.refcell = (int2 *)(b + L.refcell);
+  p.perm_tmp = (int *)(b + L.perm_tmp);
+  p.keys_sorted = (int *)(b + L.keys_sorted);
+  p.perm = (int *)(b + L.perm);
+  p.meta = (int2 *)(b + L.meta);
+  p.counts = (unsigned int *)(b + L.counts);
+  p.cstart = (unsigned int *)(b + L.cstart);
+  p.scan_part = (unsigned int *)(b + L.scan_part);
+  p.recA = b + L.recA;
+  p.recB = b + L.recB;
+  p.recC = b + L.recC;
+  p.rho_sd = (double *)(b + L.rho_sd);
+  p.n_cap = L.n_cap;
+  p.max_cells = L.max_cells;
+  p.n_parts = L.n_parts;
+  return p;
+}
+
+__global__ void k_ctrl_init(DevCtrl *c) {
+  if (threadIdx.x != 0) return;
+  memset(c, 0, sizeof(DevCtrl));
+  c->xmin = c->ymin = c->hmin_all = c->ts_hmin = kEncMinId;
+  c->xmax = c->ymax = c->hmax_new = c->ts_cmax = c->ts_a2max = kEncMaxId;
+  c->initialised = 0x53504821u;
+}
+
+__global__ void k_fill_dt(double *dt_hist, long long nsteps, double dt) {
+  long long s = (long long)blockIdx.x * blockDim.x + threadIdx.x;
+  if (s >= nsteps) return;
+  dt_hist[3 * s] = dt;
+  dt_hist[3 * s + 1] = 0.0;
+  dt_hist[3 * s + 2] = 0.0;
+}
+
+}  // namespace sph
+
+using namespace sph;
+
+static int check_launch() { return cudaGetLastError() == cudaSuccess ? SPH_OK : SPH_ERR_CUDA; }
+
+static bool particles_ok(const sph_particles_t *pa) {
+  if (!pa || pa->n < 0) return false;
+  if (pa->n == 0) return true;
+  const void *ptrs[] = {pa->label, pa->m, pa->rho, pa->p, pa->c, pa->drho, pa->h, pa->x, pa->y, pa->vx,
+                        pa->vy, pa->ax, pa->ay, pa->xsphx, pa->xsphy, pa->x0, pa->y0, pa->vx0, pa->vy0,
+                        pa->rho0};
+  for (const void *p : ptrs)
+    if (!p) return false;
+  return true;
+}
+
+static int ws_ok(const sph_workspace_t *ws, int64_t n) {
+  if (!ws || !ws->ptr || ws->max_cells <= 0 || ws->n_cap < 0) return SPH_ERR_INVALID_ARGUMENT;
+  if (n > ws->n_cap) return SPH_ERR_WORKSPACE_TOO_SMALL;
+  if (n > 0x7fffffffll || ws->max_cells > 0x3fffffffll) return SPH_ERR_INVALID_ARGUMENT;
+  if (ws->bytes < make_layout(ws->n_cap, ws->max_cells).total) return SPH_ERR_WORKSPACE_TOO_SMALL;
+  return SPH_OK;
+}
+
+static bool config_ok(const sph_config_t *c) {
+  return c && (c->kernel == SPH_KERNEL_CUBIC || c->kernel == SPH_KERNEL_GAUSSIAN) &&
+         (c->precision == SPH_PREC_FP64 || c->precision == SPH_PREC_MIXED) &&
+         (c->integrator == SPH_INTEGRATOR_PEC || c->integrator == SPH_INTEGRATOR_EULER) && c->nn_scale > 0.0;
+}
+
+extern "C" {
+
+int sph_abi_version(void) { return SPH_ABI_VERSION; }
+
+int64_t sph_default_max_cells(int64_t n) {
+  int64_t m = 4 * (n > 0 ? n : 1);
+  return m < 65536 ? 65536 : m;
+}
+
+int sph_workspace_size(int64_t n, int64_t max_cells, size_t *bytes) {
+  if (!bytes || n < 0) return SPH_ERR_INVALID_ARGUMENT;
+  if (max_cells <= 0) max_cells = sph_default_max_cells(n);
+  if (max_cells > 0x3fffffffll) return SPH_ERR_INVALID_ARGUMENT;
+  *bytes = make_layout(n, max_cells).total;
+  return SPH_OK;
+}
+
+int sph_workspace_init(sph_workspace_t *ws, sph_stream_t stream) {
+  if (!ws) return SPH_ERR_INVALID_ARGUMENT;
+  if (ws->max_cells <= 0) ws->max_cells = sph_default_max_cells(ws->n_cap);
+  int e = ws_ok(ws, 0);
+  if (e) return e;
+  cudaStream_t st = (cudaStream_t)stream;
+  WsLayout L = make_layout(ws->n_cap, ws->max_cells);
+  WsPtrs p = ws_ptrs(ws);
+  if (cudaMemsetAsync(p.counts, 0, (size_t)(L.max_cells + 1) * 4, st) != cudaSuccess) return SPH_ERR_CUDA;
+  if (cudaMemsetAsync(p.grid, 0, sizeof(DevGrid), st) != cudaSuccess) return SPH_ERR_CUDA;
+  k_ctrl_init<<<1, 32, 0, st>>>(p.ctrl);
+  if (check_launch()) return SPH_ERR_CUDA;
+  return cudaStreamSynchronize(st) == cudaSuccess ? SPH_OK : SPH_ERR_CUDA;
+}
+
+int sph_get_status(const sph_workspace_t *ws, uint32_t *status, sph_stream_t stream) {
+  int e = ws_ok(ws, 0);
+  if (e) return e;
+  if (!status) return SPH_ERR_INVALID_ARGUMENT;
+  cudaStream_t st = (cudaStream_t)stream;
+  WsPtrs p = ws_ptrs(ws);
+  unsigned int v = 0;
+  if (cudaMemcpyAsync(&v, &p.ctrl->status, 4, cudaMemcpyDeviceToHost, st) != cudaSuccess) return SPH_ERR_CUDA;
+  if (cudaMemsetAsync(&p.ctrl->status, 0, 4, st) != cudaSuccess) return SPH_ERR_CUDA;
+  if (cudaStreamSynchronize(st) != cudaSuccess) return SPH_ERR_CUDA;
+  *status = v;
+  return SPH_OK;
+}
+
+const char *sph_status_string(int code) {
+  switch (code) {
+    case SPH_OK: return "ok";
+    case SPH_ERR_INVALID_ARGUMENT: return "invalid argument";
+    case SPH_ERR_WORKSPACE_TOO_SMALL: return "workspace too small";
+    case SPH_ERR_CUDA: return "CUDA error";
+    case SPH_ERR_NOT_INITIALISED: return "workspace not initialised";
+    default: break;
+  }
+  switch ((unsigned)code) {
+    case SPH_STATUS_CELL_OVERFLOW: return "cell id past the reference grid (reference writes out of bounds)";
+    case SPH_STATUS_GRID_COARSENED: return "search grid coarsened to fit the cell capacity";
+    case SPH_STATUS_NONFINITE: return "non-finite position or h";
+    case SPH_STATUS_GRID_TOO_LARGE: return "reference grid exceeds 2^30 cells per axis";
+    case SPH_STATUS_NO_FLUID: return "no fluid particle";
+    case SPH_STATUS_SMALL_DT: return "time step below 1e-6";
+    default: return "unknown";
+  }
+}
+
+int sph_initialize(sph_particles_t *pa, const sph_wcsph_t *w, const sph_config_t *cfg, sph_stream_t stream) {
+  if (!particles_ok(pa) || !w || !cfg) return SPH_ERR_INVALID_ARGUMENT;
+  if (pa->n == 0) return SPH_OK;
+  launch_initialize(step_args(pa), *w, *cfg, (cudaStream_t)stream);
+  return check_launch();
+}
+
+int sph_eos(sph_particles_t *pa, const sph_wcsph_t *w, sph_stream_t stream) {
+  if (!particles_ok(pa) || !w) return SPH_ERR_INVALID_ARGUMENT;
+  if (pa->n == 0) return SPH_OK;
+  launch_eos(step_args(pa), *w, (cudaStream_t)stream);
+  return check_launch();
+}
+
+int sph_kernel_eval(int kernel, int64_t n, const double *r, const double *h, double *out, sph_stream_t stream) {
+  if ((kernel != SPH_KERNEL_CUBIC && kernel != SPH_KERNEL_GAUSSIAN) || n < 0 || (n && (!r || !h || !out)))
+    return SPH_ERR_INVALID_ARGUMENT;
+  if (n == 0) return SPH_OK;
+  launch_kernel_map(kernel, 0, n, nullptr, r, h, out, (cudaStream_t)stream);
+  return check_launch();
+}
+
+int sph_kernel_grad(int kernel, int64_t n, const double *x, const double *r, const double *h, double *out,
+                    sph_stream_t stream) {
+  if ((kernel != SPH_KERNEL_CUBIC && kernel != SPH_KERNEL_GAUSSIAN) || n < 0 || (n && (!x || !r || !h || !out)))
+    return SPH_ERR_INVALID_ARGUMENT;
+  if (n == 0) return SPH_OK;
+  launch_kernel_map(kernel, 1, n, x, r, h, out, (cudaStream_t)stream);
+  return check_launch();
+}
+
+int sph_gauss_deriv(int64_t n, const double *r, const double *h, double *out, sph_stream_t stream) {
+  if (n < 0 || (n && (!r || !h || !out))) return SPH_ERR_INVALID_ARGUMENT;
+  if (n == 0) return SPH_OK;
+  launch_kernel_map(SPH_KERNEL_GAUSSIAN, 2, n, nullptr, r, h, out, (cudaStream_t)stream);
+  return check_launch();
+}
+
+int sph_nn_update(const sph_particles_t *pa, const sph_config_t *cfg, const sph_workspace_t *ws,
+                  sph_stream_t stream) {
+  if (!particles_ok(pa) || !config_ok(cfg)) return SPH_ERR_INVALID_ARGUMENT;
+  int e = ws_ok(ws, pa->n);
+  if (e) return e;
+  if (pa->n == 0) return SPH_OK;
+  cudaStream_t st = (cudaStream_t)stream;
+  StepArgs a = step_args(pa);
+  WsPtrs w = ws_ptrs(ws);
+  sph_wcsph_t wc;
+  memset(&wc, 0, sizeof(wc));
+  launch_bounds(a, w, *cfg, kBoundsOnly, nullptr, 0.0, st);
+  launch_build(a, w, *cfg, wc, st);
+  return check_launch();
+}
+
+int sph_nn_count(const sph_particles_t *pa, const sph_config_t *cfg, const sph_workspace_t *ws, int64_t *counts,
+                 sph_stream_t stream) {
+  if (!particles_ok(pa) || !config_ok(cfg) || (!counts && pa->n)) return SPH_ERR_INVALID_ARGUMENT;
+  int e = ws_ok(ws, pa->n);
+  if (e) return e;
+  if (pa->n == 0) return SPH_OK;
+  launch_nn_count(step_args(pa), ws_ptrs(ws), counts, nullptr, nullptr, (cudaStream_t)stream);
+  return check_launch();
+}
+
+int sph_nn_export(const sph_particles_t *pa, const sph_config_t *cfg, const sph_workspace_t *ws,
+                  const int64_t *offsets, int64_t *idx, sph_stream_t stream) {
+  if (!particles_ok(pa) || !config_ok(cfg) || (pa->n && (!offsets || !idx))) return SPH_ERR_INVALID_ARGUMENT;
+  int e = ws_ok(ws, pa->n);
+  if (e) return e;
+  if (pa->n == 0) return SPH_OK;
+  launch_nn_count(step_args(pa), ws_ptrs(ws), nullptr, offsets, idx, (cudaStream_t)stream);
+  return check_launch();
+}
+
+static void compute_body(const StepArgs &a, const WsPtrs &w, const sph_wcsph_t &wc, const sph_config_t &cfg,
+                         double *dt_out, double *dt_hist, cudaStream_t st) {
+  launch_build(a, w, cfg, wc, st);
+  launch_records(a, w, cfg, wc, true, nullptr, st);
+  if (wc.use_summation_density) {
+    launch_sumdens(a, w, cfg, wc, st);
+    launch_records(a, w, cfg, wc, false, a.rho, st);
+  }
+  launch_pair(a, w, cfg, wc, dt_out, dt_hist, st);
+}
+
+int sph_compute(sph_particles_t *pa, const sph_wcsph_t *w, const sph_config_t *cfg, const sph_workspace_t *ws,
+                sph_stream_t stream) {
+  if (!particles_ok(pa) || !w || !config_ok(cfg)) return SPH_ERR_INVALID_ARGUMENT;
+  int e = ws_ok(ws, pa->n);
+  if (e) return e;
+  if (pa->n == 0) return SPH_OK;
+  cudaStream_t st = (cudaStream_t)stream;
+  StepArgs a = step_args(pa);
+  WsPtrs wp = ws_ptrs(ws);
+  launch_bounds(a, wp, *cfg, kBoundsReset, nullptr, 0.0, st);
+  compute_body(a, wp, *w, *cfg, nullptr, nullptr, st);
+  return check_launch();
+}
+
+int sph_timestep(const sph_particles_t *pa, const sph_wcsph_t *w, const sph_config_t *cfg,
+                 const sph_workspace_t *ws, double *dt3, sph_stream_t stream) {
+  if (!particles_ok(pa) || !w || !config_ok(cfg) || !dt3) return SPH_ERR_INVALID_ARGUMENT;
+  int e = ws_ok(ws, pa->n);
+  if (e) return e;
+  launch_timestep(step_args(pa), ws_ptrs(ws), *cfg, dt3, nullptr, (cudaStream_t)stream);
+  return check_launch();
+}
+
+int sph_predict(sph_particles_t *pa, const sph_config_t *cfg, const double *dt, sph_stream_t stream) {
+  if (!particles_ok(pa) || !config_ok(cfg) || !dt) return SPH_ERR_INVALID_ARGUMENT;
+  if (pa->n == 0) return SPH_OK;
+  launch_predict(step_args(pa), *cfg, dt, 0.0, (cudaStream_t)stream);
+  return check_launch();
+}
+
+int sph_correct(sph_particles_t *pa, const sph_config_t *cfg, const double *dt, sph_stream_t stream) {
+  if (!particles_ok(pa) || !config_ok(cfg) || !dt) return SPH_ERR_INVALID_ARGUMENT;
+  if (pa->n == 0) return SPH_OK;
+  launch_correct(step_args(pa), *cfg, dt, 0.0, (cudaStream_t)stream);
+  return check_launch();
+}
+
+int sph_run(sph_particles_t *pa, const sph_wcsph_t *w, const sph_config_t *cfg, const sph_workspace_t *ws,
+            int64_t nsteps, double *dt_hist, sph_stream_t stream) {
+  if (!particles_ok(pa) || !w || !config_ok(cfg) || nsteps < 0) return SPH_ERR_INVALID_ARGUMENT;
+  int e = ws_ok(ws, pa->n);
+  if (e) return e;
+  if (pa->n == 0 || nsteps == 0) return SPH_OK;
+  cudaStream_t st = (cudaStream_t)stream;
+  StepArgs a = step_args(pa);
+  WsPtrs wp = ws_ptrs(ws);
+  const bool fixed = cfg->dt_fixed > 0.0;
+  double *ring = &wp.ctrl->dt_ring[0][0];
+  if (fixed) {
+    if (dt_hist) k_fill_dt<<<nblocks(nsteps), kBlock, 0, st>>>(dt_hist, nsteps, cfg->dt_fixed);
+  } else {
+    launch_timestep(a, wp, *cfg, ring, dt_hist, st);
+  }
+  for (int64_t s = 0; s < nsteps; s++) {
+    double *cur = ring + 3 * (s & 1);
+    double *nxt = ring + 3 * ((s + 1) & 1);
+    int bmode = cfg->integrator == SPH_INTEGRATOR_PEC ? kBoundsPredictPEC : kBoundsReset;
+    launch_bounds(a, wp, *cfg, bmode, cur, cfg->dt_fixed, st);
+    double *hist_next = (dt_hist && !fixed && s + 1 < nsteps) ? dt_hist + 3 * (s + 1) : nullptr;
+    compute_body(a, wp, *w, *cfg, fixed ? nullptr : nxt, hist_next, st);
+    launch_correct(a, *cfg, cur, cfg->dt_fixed, st);
+  }
+  return check_launch();
+}
+
+int sph_run_profiled(sph_particles_t *pa, const sph_wcsph_t *w, const sph_config_t *cfg, const sph_workspace_t *ws,
+                     int64_t nsteps, double *stage_ms, sph_stream_t stream) {
+  if (!particles_ok(pa) || !w || !config_ok(cfg) || nsteps < 0 || !stage_ms) return SPH_ERR_INVALID_ARGUMENT;
+  int e = ws_ok(ws, pa->n);
+  if (e) return e;
+  for (int k = 0; k < SPH_NSTAGES; k++) stage_ms[k] = 0.0;
+  if (pa->n == 0 || nsteps == 0) return SPH_OK;
+  cudaStream_t st = (cudaStream_t)stream;
+  StepArgs a = step_args(pa);
+  WsPtrs wp = ws_ptrs(ws);
+  const bool fixed = cfg->dt_fixed > 0.0;
+  double *ring = &wp.ctrl->dt_ring[0][0];
+  cudaEvent_t ev[SPH_NSTAGES + 1];
+  for (int k = 0; k <= SPH_NSTAGES; k++)
+    if (cudaEventCreate(&ev[k]) != cudaSuccess) return SPH_ERR_CUDA;
+  int rc = SPH_OK;
+  auto lap = [&](int stage, int from) {
+    float ms = 0.f;
+    cudaEventRecord(ev[stage + 1], st);
+    cudaEventSynchronize(ev[stage + 1]);
+    cudaEventElapsedTime(&ms, ev[from], ev[stage + 1]);
+    stage_ms[stage] += ms;
+  };
+  cudaEventRecord(ev[0], st);
+  if (!fixed) launch_timestep(a, wp, *cfg, ring, nullptr, st);
+  lap(SPH_STAGE_TIMESTEP, 0);
+  for (int64_t s = 0; s < nsteps; s++) {
+    double *cur = ring + 3 * (s & 1);
+    double *nxt = ring + 3 * ((s + 1) & 1);
+    int bmode = cfg->integrator == SPH_INTEGRATOR_PEC ? kBoundsPredictPEC : kBoundsReset;
+    cudaEventRecord(ev[0], st);
+    launch_bounds(a, wp, *cfg, bmode, cur, cfg->dt_fixed, st);
+    lap(SPH_STAGE_PREDICT, 0);
+    launch_build(a, wp, *cfg, *w, st);
+    lap(SPH_STAGE_BUILD, SPH_STAGE_PREDICT + 1);
+    launch_records(a, wp, *cfg, *w, true, nullptr, st);
+    if (w->use_summation_density) {
+      launch_sumdens(a, wp, *cfg, *w, st);
+      launch_records(a, wp, *cfg, *w, false, a.rho, st);
+    }
+    lap(SPH_STAGE_RECORDS, SPH_STAGE_BUILD + 1);
+    launch_pair(a, wp, *cfg, *w, fixed ? nullptr : nxt, nullptr, st);
+    lap(SPH_STAGE_PAIR, SPH_STAGE_RECORDS + 1);
+    launch_correct(a, *cfg, cur, cfg->dt_fixed, st);
+    lap(SPH_STAGE_CORRECT, SPH_STAGE_PAIR + 1);
+  }
+  if (check_launch()) rc = SPH_ERR_CUDA;
+  for (int k = 0; k <= SPH_NSTAGES; k++) cudaEventDestroy(ev[k]);
+  return rc;
+}
+
+}  // extern "C"

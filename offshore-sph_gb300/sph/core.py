@@ -1,0 +1,138 @@
+"""Functional layer over the C ABI: parameter packing and the calls the
+drop-in classes (Solver, WCSPH, PEC, ...) are built from."""
+import ctypes as C
+import math
+
+import numpy as np
+import torch
+
+from . import _lib as L
+from .state import DeviceParticles, DeviceWorkspace, current_stream
+
+PRECISIONS = {"fp64": L.PREC_FP64, "mixed": L.PREC_MIXED}
+
+
+def wcsph_struct(height, r0, rho0, use_xsph=False, Pb=0.0, use_summation_density=False, alpha=0.01,
+                 beta=0.0, epsilon=0.5, gamma=7.0, co=None, B=None, D=None, p1=4.0, p2=2.0):
+    """sph_wcsph_t with WCSPH's derived constants (src/Methods/WCSPH.py:35-79,
+    src/Equations/TaitEOS.py:33-44) unless given explicitly."""
+    if co is None:
+        co = 10.0 * math.sqrt(2 * 9.81 * height)
+    if B is None:
+        B = co * co * rho0 / gamma
+    if D is None:
+        D = 5 * 9.81 * height
+    return L.Wcsph(rho0=rho0, gamma=gamma, co=co, B=B, Pb=Pb, alpha=alpha, beta=beta, epsilon=epsilon, r0=r0,
+                   D=D, p1=p1, p2=p2, height=height, use_xsph=int(bool(use_xsph)),
+                   use_summation_density=int(bool(use_summation_density)))
+
+
+def config_struct(kernel=L.KERNEL_CUBIC, precision="fp64", integrator=L.INTEGRATOR_PEC, pec_use_xsph=False,
+                  pec_strict=True, nn_scale=2.0, h_fixed=0.0, cfl_c=0.25, cfl_f=0.25, damping=0.0,
+                  dt_fixed=0.0):
+    if isinstance(precision, str):
+        precision = PRECISIONS[precision]
+    return L.Config(kernel=int(kernel), precision=int(precision), integrator=int(integrator),
+                    pec_use_xsph=int(bool(pec_use_xsph)), pec_strict=int(bool(pec_strict)), nn_scale=nn_scale,
+                    h_fixed=h_fixed if h_fixed else 0.0, cfl_c=cfl_c, cfl_f=cfl_f, damping=damping,
+                    dt_fixed=dt_fixed if dt_fixed else 0.0)
+
+
+def _P(dp):
+    return C.byref(dp.cstruct())
+
+
+def initialize(dp, wc, cfg):
+    L.check(L.load().sph_initialize(_P(dp), C.byref(wc), C.byref(cfg), current_stream()), "sph_initialize")
+
+
+def eos(dp, wc):
+    L.check(L.load().sph_eos(_P(dp), C.byref(wc), current_stream()), "sph_eos")
+
+
+def compute(dp, wc, cfg, ws):
+    """Solver._compute on the device."""
+    L.check(L.load().sph_compute(_P(dp), C.byref(wc), C.byref(cfg), C.byref(ws.ws), current_stream()),
+            "sph_compute")
+
+
+def run(dp, wc, cfg, ws, nsteps, dt_hist=None):
+    """nsteps bare steps; dt_hist: optional device float64 tensor (nsteps, 3)."""
+    ptr = None
+    if dt_hist is not None:
+        assert dt_hist.dtype == torch.float64 and dt_hist.is_cuda and dt_hist.numel() >= 3 * nsteps
+        ptr = dt_hist.data_ptr()
+    L.check(L.load().sph_run(_P(dp), C.byref(wc), C.byref(cfg), C.byref(ws.ws), int(nsteps), ptr,
+                             current_stream()), "sph_run")
+
+
+def run_profiled(dp, wc, cfg, ws, nsteps):
+    """sph_run with CUDA-event laps per stage; returns {stage: ms summed over steps}."""
+    ms = (C.c_double * len(L.STAGES))()
+    L.check(L.load().sph_run_profiled(_P(dp), C.byref(wc), C.byref(cfg), C.byref(ws.ws), int(nsteps), ms,
+                                      current_stream()), "sph_run_profiled")
+    return {k: ms[j] for j, k in enumerate(L.STAGES)}
+
+
+def timestep(dp, wc, cfg, ws, dt3=None):
+    if dt3 is None:
+        dt3 = torch.zeros(3, dtype=torch.float64, device=dp.device)
+    L.check(L.load().sph_timestep(_P(dp), C.byref(wc), C.byref(cfg), C.byref(ws.ws), dt3.data_ptr(),
+                                  current_stream()), "sph_timestep")
+    return dt3
+
+
+def predict(dp, cfg, dt_dev):
+    L.check(L.load().sph_predict(_P(dp), C.byref(cfg), dt_dev.data_ptr(), current_stream()), "sph_predict")
+
+
+def correct(dp, cfg, dt_dev):
+    L.check(L.load().sph_correct(_P(dp), C.byref(cfg), dt_dev.data_ptr(), current_stream()), "sph_correct")
+
+
+def nn_update(dp, cfg, ws):
+    L.check(L.load().sph_nn_update(_P(dp), C.byref(cfg), C.byref(ws.ws), current_stream()), "sph_nn_update")
+
+
+def nn_export(dp, cfg, ws):
+    """Neighbour lists of the last nn_update: (offsets[n+1], idx) as numpy
+    int64, each list ascending."""
+    lib = L.load()
+    counts = torch.zeros(dp.n, dtype=torch.int64, device=dp.device)
+    L.check(lib.sph_nn_count(_P(dp), C.byref(cfg), C.byref(ws.ws), counts.data_ptr(), current_stream()),
+            "sph_nn_count")
+    offsets = torch.zeros(dp.n + 1, dtype=torch.int64, device=dp.device)
+    offsets[1:] = torch.cumsum(counts, 0)
+    total = int(offsets[-1].item())
+    idx = torch.zeros(max(total, 1), dtype=torch.int64, device=dp.device)
+    L.check(lib.sph_nn_export(_P(dp), C.byref(cfg), C.byref(ws.ws), offsets.data_ptr(), idx.data_ptr(),
+                              current_stream()), "sph_nn_export")
+    return offsets.cpu().numpy(), idx[:total].cpu().numpy()
+
+
+def kernel_eval(kernel, r, h):
+    r = torch.as_tensor(r, dtype=torch.float64, device="cuda").contiguous()
+    h = torch.as_tensor(h, dtype=torch.float64, device="cuda").contiguous()
+    out = torch.empty_like(r)
+    L.check(L.load().sph_kernel_eval(int(kernel), r.numel(), r.data_ptr(), h.data_ptr(), out.data_ptr(),
+                                     current_stream()), "sph_kernel_eval")
+    return out
+
+
+def kernel_grad(kernel, x, r, h):
+    x = torch.as_tensor(x, dtype=torch.float64, device="cuda").contiguous()
+    r = torch.as_tensor(r, dtype=torch.float64, device="cuda").contiguous()
+    h = torch.as_tensor(h, dtype=torch.float64, device="cuda").contiguous()
+    out = torch.empty_like(r)
+    L.check(L.load().sph_kernel_grad(int(kernel), r.numel(), x.data_ptr(), r.data_ptr(), h.data_ptr(),
+                                     out.data_ptr(), current_stream()), "sph_kernel_grad")
+    return out
+
+
+def gauss_deriv(r, h):
+    r = torch.as_tensor(r, dtype=torch.float64, device="cuda").contiguous()
+    h = torch.as_tensor(h, dtype=torch.float64, device="cuda").contiguous()
+    out = torch.empty_like(r)
+    L.check(L.load().sph_gauss_deriv(r.numel(), r.data_ptr(), h.data_ptr(), out.data_ptr(), current_stream()),
+            "sph_gauss_deriv")
+    return out
