@@ -224,11 +224,12 @@ int sph_run(sph_particles_t *pa, const sph_wcsph_t *w, const sph_config_t *cfg, 
  * are the parts of Solver.run's step body (src/Solver.py:366-410). */
 enum {
   SPH_STAGE_TIMESTEP = 0, /* initial TimeStep.compute */
-  SPH_STAGE_PREDICT = 1,  /* integrator.predict fused with the bounds of nn.update */
+  SPH_STAGE_PREDICT = 1,  /* the previous step's integrator.correct, this step's
+                             integrator.predict and the bounds of nn.update, one pass */
   SPH_STAGE_BUILD = 2,    /* rest of nn.update: grid, keys, counting sort */
   SPH_STAGE_RECORDS = 3,  /* h reset + Tait EOS + sorted pair records */
   SPH_STAGE_PAIR = 4,     /* the fused pair interaction (+ next TimeStep) */
-  SPH_STAGE_CORRECT = 5,  /* integrator.correct */
+  SPH_STAGE_CORRECT = 5,  /* the last step's integrator.correct */
   SPH_NSTAGES = 6
 };
 int sph_run_profiled(sph_particles_t *pa, const sph_wcsph_t *w, const sph_config_t *cfg, const sph_workspace_t *ws,

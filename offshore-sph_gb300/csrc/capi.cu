@@ -31,10 +31,11 @@ WsLayout make_layout(long long n_cap, long long max_cells) {
   L.counts = take((mc + 1) * 4);
   L.cstart = take((mc + 2) * 4);
   L.scan_part = take((size_t)L.n_parts * 4);
-  L.recA = take(n * 32);
-  L.recB = take(n * 32);
-  L.recC = take(n * 16);
-  L.rho_sd = take(8);
+  L.rec0 = take(n * 16);
+  L.rec1 = take(n * 16);
+  L.rec2 = take(n * 16);
+  L.rec64a = take(n * 32);
+  L.rec64b = take(n * 32);
   L.total = off;
   return L;
 }
@@ -54,10 +55,11 @@ WsPtrs ws_ptrs(const sph_workspace_t *ws) {
   p.counts = (unsigned int *)(b + L.counts);
   p.cstart = (unsigned int *)(b + L.cstart);
   p.scan_part = (unsigned int *)(b + L.scan_part);
-  p.recA = b + L.recA;
-  p.recB = b + L.recB;
-  p.recC = b + L.recC;
-  p.rho_sd = (double *)(b + L.rho_sd);
+  p.rec0 = (float4 *)(b + L.rec0);
+  p.rec1 = (float4 *)(b + L.rec1);
+  p.rec2 = (float4 *)(b + L.rec2);
+  p.rec64a = (double4_32a *)(b + L.rec64a);
+  p.rec64b = (double4_32a *)(b + L.rec64b);
   p.n_cap = L.n_cap;
   p.max_cells = L.max_cells;
   p.n_parts = L.n_parts;
@@ -67,8 +69,8 @@ WsPtrs ws_ptrs(const sph_workspace_t *ws) {
 __global__ void k_ctrl_init(DevCtrl *c) {
   if (threadIdx.x != 0) return;
   memset(c, 0, sizeof(DevCtrl));
-  c->xmin = c->ymin = c->hmin_all = c->ts_hmin = kEncMinId;
-  c->xmax = c->ymax = c->hmax_new = c->ts_cmax = c->ts_a2max = kEncMaxId;
+  c->xmin = c->ymin = c->hmin_all = c->ts_hmin = c->pd_hmin = kEncMinId;
+  c->xmax = c->ymax = c->hmax_new = c->ts_cmax = c->ts_a2max = c->pd_a2max = kEncMaxId;
   c->initialised = 0x53504821u;
 }
 
@@ -226,7 +228,7 @@ int sph_nn_update(const sph_particles_t *pa, const sph_config_t *cfg, const sph_
   WsPtrs w = ws_ptrs(ws);
   sph_wcsph_t wc;
   memset(&wc, 0, sizeof(wc));
-  launch_bounds(a, w, *cfg, kBoundsOnly, nullptr, 0.0, st);
+  launch_bounds(a, w, *cfg, kStageNone, false, nullptr, nullptr, st);
   launch_build(a, w, *cfg, wc, st);
   return check_launch();
 }
@@ -253,11 +255,12 @@ int sph_nn_export(const sph_particles_t *pa, const sph_config_t *cfg, const sph_
 
 static void compute_body(const StepArgs &a, const WsPtrs &w, const sph_wcsph_t &wc, const sph_config_t &cfg,
                          double *dt_out, double *dt_hist, cudaStream_t st) {
+  const bool do_dt = dt_out != nullptr || dt_hist != nullptr;
   launch_build(a, w, cfg, wc, st);
-  launch_records(a, w, cfg, wc, true, nullptr, st);
+  launch_records(a, w, cfg, wc, true, false, do_dt, st);
   if (wc.use_summation_density) {
     launch_sumdens(a, w, cfg, wc, st);
-    launch_records(a, w, cfg, wc, false, a.rho, st);
+    launch_records(a, w, cfg, wc, false, true, false, st);
   }
   launch_pair(a, w, cfg, wc, dt_out, dt_hist, st);
 }
@@ -271,7 +274,7 @@ int sph_compute(sph_particles_t *pa, const sph_wcsph_t *w, const sph_config_t *c
   cudaStream_t st = (cudaStream_t)stream;
   StepArgs a = step_args(pa);
   WsPtrs wp = ws_ptrs(ws);
-  launch_bounds(a, wp, *cfg, kBoundsReset, nullptr, 0.0, st);
+  launch_bounds(a, wp, *cfg, kStageNone, true, nullptr, nullptr, st);
   compute_body(a, wp, *w, *cfg, nullptr, nullptr, st);
   return check_launch();
 }
@@ -315,15 +318,17 @@ int sph_run(sph_particles_t *pa, const sph_wcsph_t *w, const sph_config_t *cfg, 
   } else {
     launch_timestep(a, wp, *cfg, ring, dt_hist, st);
   }
+  // the corrector of step s-1 and the predictor of step s run as one pass
+  // in front of step s's neighbour build; the last corrector runs alone
   for (int64_t s = 0; s < nsteps; s++) {
+    double *prev = ring + 3 * ((s + 1) & 1);
     double *cur = ring + 3 * (s & 1);
     double *nxt = ring + 3 * ((s + 1) & 1);
-    int bmode = cfg->integrator == SPH_INTEGRATOR_PEC ? kBoundsPredictPEC : kBoundsReset;
-    launch_bounds(a, wp, *cfg, bmode, cur, cfg->dt_fixed, st);
+    launch_bounds(a, wp, *cfg, s == 0 ? kStagePredict : kStageCorrectPredict, true, prev, cur, st);
     double *hist_next = (dt_hist && !fixed && s + 1 < nsteps) ? dt_hist + 3 * (s + 1) : nullptr;
     compute_body(a, wp, *w, *cfg, fixed ? nullptr : nxt, hist_next, st);
-    launch_correct(a, *cfg, cur, cfg->dt_fixed, st);
   }
+  launch_correct(a, *cfg, ring + 3 * ((nsteps - 1) & 1), cfg->dt_fixed, st);
   return check_launch();
 }
 
@@ -354,25 +359,26 @@ int sph_run_profiled(sph_particles_t *pa, const sph_wcsph_t *w, const sph_config
   if (!fixed) launch_timestep(a, wp, *cfg, ring, nullptr, st);
   lap(SPH_STAGE_TIMESTEP, 0);
   for (int64_t s = 0; s < nsteps; s++) {
+    double *prev = ring + 3 * ((s + 1) & 1);
     double *cur = ring + 3 * (s & 1);
     double *nxt = ring + 3 * ((s + 1) & 1);
-    int bmode = cfg->integrator == SPH_INTEGRATOR_PEC ? kBoundsPredictPEC : kBoundsReset;
     cudaEventRecord(ev[0], st);
-    launch_bounds(a, wp, *cfg, bmode, cur, cfg->dt_fixed, st);
+    launch_bounds(a, wp, *cfg, s == 0 ? kStagePredict : kStageCorrectPredict, true, prev, cur, st);
     lap(SPH_STAGE_PREDICT, 0);
     launch_build(a, wp, *cfg, *w, st);
     lap(SPH_STAGE_BUILD, SPH_STAGE_PREDICT + 1);
-    launch_records(a, wp, *cfg, *w, true, nullptr, st);
+    launch_records(a, wp, *cfg, *w, true, false, !fixed, st);
     if (w->use_summation_density) {
       launch_sumdens(a, wp, *cfg, *w, st);
-      launch_records(a, wp, *cfg, *w, false, a.rho, st);
+      launch_records(a, wp, *cfg, *w, false, true, false, st);
     }
     lap(SPH_STAGE_RECORDS, SPH_STAGE_BUILD + 1);
     launch_pair(a, wp, *cfg, *w, fixed ? nullptr : nxt, nullptr, st);
     lap(SPH_STAGE_PAIR, SPH_STAGE_RECORDS + 1);
-    launch_correct(a, *cfg, cur, cfg->dt_fixed, st);
-    lap(SPH_STAGE_CORRECT, SPH_STAGE_PAIR + 1);
   }
+  cudaEventRecord(ev[SPH_STAGE_PAIR + 1], st);
+  launch_correct(a, *cfg, ring + 3 * ((nsteps - 1) & 1), cfg->dt_fixed, st);
+  lap(SPH_STAGE_CORRECT, SPH_STAGE_PAIR + 1);
   if (check_launch()) rc = SPH_ERR_CUDA;
   for (int k = 0; k <= SPH_NSTAGES; k++) cudaEventDestroy(ev[k]);
   return rc;

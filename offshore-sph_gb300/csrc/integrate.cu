@@ -10,6 +10,7 @@ struct IntParams {
   double dt_fixed;
   const double *dt;
   double inv_damp;
+  int damped;
   int use_xsph, strict, integrator;
 };
 
@@ -57,25 +58,29 @@ __global__ void __launch_bounds__(kBlock) k_correct(StepArgs a, IntParams ip) {
     a.rho[i] = a.rho[i] + dt * drho;
     return;
   }
+  // PEC's corrector x = 2 (x0 + dt/2 v) - x0 etc. in its reduced form
+  // x0 + dt v: the same value to one rounding, with half the FP64 operations
   const double x0 = a.x0[i], y0 = a.y0[i], vx0 = a.vx0[i], vy0 = a.vy0[i], rho0 = a.rho0[i];
-  double mid_x, mid_y;
   if (ip.use_xsph) {
-    mid_x = x0 + hdt * a.xsphx[i];
-    mid_y = y0 + hdt * a.xsphy[i];
+    a.x[i] = fma(dt, a.xsphx[i], x0);
+    a.y[i] = fma(dt, a.xsphy[i], y0);
   } else {
-    mid_x = x0 + hdt * a.vx[i];
-    mid_y = y0 + hdt * a.vy[i];
+    a.x[i] = fma(dt, a.vx[i], x0);
+    a.y[i] = fma(dt, a.vy[i], y0);
   }
-  const double mid_vx = (vx0 + hdt * ax) * ip.inv_damp;
-  const double mid_vy = (vy0 + hdt * ay) * ip.inv_damp;
-  a.x[i] = 2.0 * mid_x - x0;
-  a.y[i] = 2.0 * mid_y - y0;
-  a.vx[i] = 2.0 * mid_vx - vx0;
-  a.vy[i] = 2.0 * mid_vy - vy0;
-  const double mid_rho = rho0 + hdt * drho;
-  double rho = 2.0 * mid_rho - rho0;
+  if (ip.damped) {
+    // 2 (v0 + dt/2 a) / (1 + damping/2) - v0
+    const double c0 = 2.0 * ip.inv_damp - 1.0, c1 = dt * ip.inv_damp;
+    a.vx[i] = fma(c1, ax, c0 * vx0);
+    a.vy[i] = fma(c1, ay, c0 * vy0);
+  } else {
+    a.vx[i] = fma(dt, ax, vx0);
+    a.vy[i] = fma(dt, ay, vy0);
+  }
+  double rho = fma(dt, drho, rho0);
   if (ip.strict && rho < 0.0) rho = 0.0;
   a.rho[i] = rho;
+  (void)hdt;
 }
 
 static IntParams int_params(const sph_config_t &cfg, const double *dt, double dt_fixed) {
@@ -83,6 +88,7 @@ static IntParams int_params(const sph_config_t &cfg, const double *dt, double dt
   ip.dt_fixed = dt_fixed;
   ip.dt = dt;
   ip.inv_damp = 1.0 / (1.0 + 0.5 * cfg.damping);
+  ip.damped = cfg.damping != 0.0 ? 1 : 0;
   ip.use_xsph = cfg.pec_use_xsph;
   ip.strict = cfg.pec_strict;
   ip.integrator = cfg.integrator;
@@ -175,7 +181,7 @@ __global__ void __launch_bounds__(kBlock) k_initialize(StepArgs a, double h_fixe
   double frac = rho0 * 9.81 * (H - a.y[i]) / B;
   double rho = rho0 * pow(1.0 + frac, 1.0 / gamma);
   a.rho[i] = rho;
-  a.p[i] = tait_p(rho, SPH_FLUID, gamma, B, rho0, Pb);
+  a.p[i] = tait_p(rho, SPH_FLUID, gamma, B, 1.0 / rho0, Pb);
   a.c[i] = co;
 }
 
@@ -188,7 +194,7 @@ __global__ void __launch_bounds__(kBlock) k_eos(StepArgs a, double gamma, double
                                                 double co) {
   long long i = (long long)blockIdx.x * blockDim.x + threadIdx.x;
   if (i >= a.n) return;
-  a.p[i] = tait_p(a.rho[i], a.label[i], gamma, B, rho0, Pb);
+  a.p[i] = tait_p(a.rho[i], a.label[i], gamma, B, 1.0 / rho0, Pb);
   a.c[i] = co;
 }
 

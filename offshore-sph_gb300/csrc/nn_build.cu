@@ -4,10 +4,16 @@
 // instead of per-cell linked lists it builds a cell-sorted permutation and a
 // cell-start table with a one-digit counting sort over cell ids
 // (histogram -> exclusive scan -> scatter -> in-cell rank by particle index,
-// which makes the order deterministic).  The reference grid (origin, cell
-// size, ncx, ncy, the x-overflow alias) is reproduced exactly; when its cells
-// are much wider than the interaction radius the search runs on a finer grid
-// of its own and filters candidates by the reference's 3x3 stencil.
+// which makes the order deterministic).
+//
+// The reference grid (origin, cell size, ncx, ncy, the x-overflow alias) is
+// reproduced exactly.  Where that grid's 3x3 stencil can truncate pairs that
+// contribute (its cells narrower than the interaction radius), the search runs
+// on the reference cells themselves (mode 0).  Otherwise it runs on a grid of
+// its own with cells of half the interaction radius and a 5x5 stencil
+// (mode 1), which visits about 30% fewer candidates; candidates are then
+// filtered by the reference's stencil only when the reference could truncate
+// (aliased cells, or a grid coarsened to fit the cell capacity).
 #include <math.h>
 
 #include "sph_internal.cuh"
@@ -18,83 +24,163 @@ namespace sph {
 // Bounds (and, fused, the PEC predictor of Solver.run's step)
 // ---------------------------------------------------------------------------
 struct BoundsParams {
-  double h_fixed;
-  int h_reset;  // 1: hmax over the h the next _compute will set
-  int predict;  // 1: PEC.predict the fluid particles first
-  double dt_fixed;
-  const double *dt;  // device dt when dt_fixed <= 0
-  double inv_damp;   // 1 / (1 + 0.5 damping)
-  int use_xsph, strict;
+  int stage;      // IntStage
+  int h_reset;    // 1: hmax over the h the next _compute will set
+  int h_fixed_on; // h_fixed > 0
+  int dt_fixed_on;
+  int damped;     // damping != 0
+  int use_xsph, strict, euler;
+  double h_fixed, dt_fixed;
+  double inv_damp;  // 1 / (1 + 0.5 damping)
+  double c0;        // 2 inv_damp - 1
+  const double *dt_prev, *dt_cur;  // device dt of the previous / current step
 };
 
-__global__ void __launch_bounds__(kBlock) k_bounds(StepArgs a, DevCtrl *ctrl, BoundsParams bp) {
-  __shared__ unsigned long long red[32];
-  long long i = (long long)blockIdx.x * blockDim.x + threadIdx.x;
-  unsigned long long exmin = kEncMinId, exmax = kEncMaxId, eymin = kEncMinId, eymax = kEncMaxId;
-  unsigned long long ehmin = kEncMinId, ehmax = kEncMaxId;
-  bool bad = false;
-  if (i < a.n) {
-    int8_t lab = a.label[i];
-    double x = a.x[i], y = a.y[i], h = a.h[i];
-    double rho = a.rho[i];
-    if (bp.predict && is_fluid(lab)) {
-      // PEC.predict (src/Integrators/PEC.py:32-59)
-      double dt = bp.dt_fixed > 0.0 ? bp.dt_fixed : bp.dt[0];
-      double hdt = 0.5 * dt;
-      double vx = a.vx[i], vy = a.vy[i];
-      a.x0[i] = x;
-      a.y0[i] = y;
-      a.vx0[i] = vx;
-      a.vy0[i] = vy;
-      if (bp.use_xsph) {
-        x = x + hdt * a.xsphx[i];
-        y = y + hdt * a.xsphy[i];
-      } else {
-        x = x + hdt * vx;
-        y = y + hdt * vy;
-      }
+// The integrator work in front of a neighbour build, on one fluid particle:
+// [the previous step's corrector: PEC.correct (src/Integrators/PEC.py:61-89)
+// in its reduced form x0 + dt v, or Euler.correct (Euler.py:17-27)] then
+// [this step's PEC.predict (PEC.py:32-59)].  Uniform conditions arrive as
+// ints and the half step is an exponent decrement, so the FP64 pipe only
+// sees the fused multiply-adds of the updates.
+__device__ __forceinline__ void integrate_front(const StepArgs &a, long long i, const BoundsParams &bp, double &x,
+                                                double &y, double &rho) {
+  double vx, vy;
+  const double axv = a.ax[i], ayv = a.ay[i], drho = a.drho[i];
+  if (bp.stage == kStageCorrectPredict) {
+    const double dtc = bp.dt_fixed_on ? bp.dt_fixed : bp.dt_prev[0];
+    if (bp.euler) {
+      vx = a.vx[i];
+      vy = a.vy[i];
+      const double hdt2 = half_exact(dtc * dtc);
+      x = fma(hdt2, axv, fma(dtc, vx, x));
+      y = fma(hdt2, ayv, fma(dtc, vy, y));
+      vx = fma(dtc, axv, vx);
+      vy = fma(dtc, ayv, vy);
+      rho = fma(dtc, drho, rho);
       a.x[i] = x;
       a.y[i] = y;
-      a.vx[i] = (vx + hdt * a.ax[i]) * bp.inv_damp;
-      a.vy[i] = (vy + hdt * a.ay[i]) * bp.inv_damp;
-      a.rho0[i] = rho;
-      rho = rho + hdt * a.drho[i];
-      if (bp.strict && rho < 0.0) rho = 0.0;
+      a.vx[i] = vx;
+      a.vy[i] = vy;
       a.rho[i] = rho;
+      return;  // Euler.predict is a no-op
     }
-    double hn = (bp.h_reset && is_fluid(lab)) ? reset_h(bp.h_fixed, a.m[i], rho) : h;
-    bad = !(isfinite(x) && isfinite(y) && isfinite(h));
-    exmin = exmax = enc_d(x);
-    eymin = eymax = enc_d(y);
-    ehmin = enc_d(h);
-    ehmax = enc_d(hn);
-    if (bad) exmin = eymin = ehmin = kEncMinId, exmax = eymax = ehmax = kEncMaxId;
+    const double x0 = a.x0[i], y0 = a.y0[i], vx0 = a.vx0[i], vy0 = a.vy0[i], rho0 = a.rho0[i];
+    if (bp.use_xsph) {
+      x = fma(dtc, a.xsphx[i], x0);
+      y = fma(dtc, a.xsphy[i], y0);
+    } else {
+      x = fma(dtc, a.vx[i], x0);
+      y = fma(dtc, a.vy[i], y0);
+    }
+    if (bp.damped) {
+      const double c1 = dtc * bp.inv_damp;
+      vx = fma(c1, axv, bp.c0 * vx0);
+      vy = fma(c1, ayv, bp.c0 * vy0);
+    } else {
+      vx = fma(dtc, axv, vx0);
+      vy = fma(dtc, ayv, vy0);
+    }
+    rho = fma(dtc, drho, rho0);
+    if (bp.strict && negative_bits(rho)) rho = 0.0;
+  } else {
+    vx = a.vx[i];
+    vy = a.vy[i];
   }
-  if (__syncthreads_or(bad) && threadIdx.x == 0) atomicOr(&ctrl->status, (unsigned)SPH_STATUS_NONFINITE);
-  unsigned long long v;
-  v = block_reduce(exmin, MinU64(), kEncMinId, red);
-  if (threadIdx.x == 0 && v != kEncMinId) atomicMin(&ctrl->xmin, v);
-  v = block_reduce(exmax, MaxU64(), kEncMaxId, red);
-  if (threadIdx.x == 0 && v != kEncMaxId) atomicMax(&ctrl->xmax, v);
-  v = block_reduce(eymin, MinU64(), kEncMinId, red);
-  if (threadIdx.x == 0 && v != kEncMinId) atomicMin(&ctrl->ymin, v);
-  v = block_reduce(eymax, MaxU64(), kEncMaxId, red);
-  if (threadIdx.x == 0 && v != kEncMaxId) atomicMax(&ctrl->ymax, v);
-  v = block_reduce(ehmin, MinU64(), kEncMinId, red);
-  if (threadIdx.x == 0 && v != kEncMinId) atomicMin(&ctrl->hmin_all, v);
-  v = block_reduce(ehmax, MaxU64(), kEncMaxId, red);
-  if (threadIdx.x == 0 && v != kEncMaxId) atomicMax(&ctrl->hmax_new, v);
+  // PEC.predict with this step's dt
+  const double hdt = half_exact(bp.dt_fixed_on ? bp.dt_fixed : bp.dt_cur[0]);
+  a.x0[i] = x;
+  a.y0[i] = y;
+  a.vx0[i] = vx;
+  a.vy0[i] = vy;
+  a.rho0[i] = rho;
+  if (bp.use_xsph) {
+    x = fma(hdt, a.xsphx[i], x);
+    y = fma(hdt, a.xsphy[i], y);
+  } else {
+    x = fma(hdt, vx, x);
+    y = fma(hdt, vy, y);
+  }
+  double nvx = fma(hdt, axv, vx), nvy = fma(hdt, ayv, vy);
+  if (bp.damped) {
+    nvx *= bp.inv_damp;
+    nvy *= bp.inv_damp;
+  }
+  rho = fma(hdt, drho, rho);
+  if (bp.strict && negative_bits(rho)) rho = 0.0;
+  a.x[i] = x;
+  a.y[i] = y;
+  a.vx[i] = nvx;
+  a.vy[i] = nvy;
+  a.rho[i] = rho;
 }
 
-void launch_bounds(const StepArgs &a, const WsPtrs &w, const sph_config_t &cfg, int mode, const double *dt,
-                   double dt_fixed, cudaStream_t st) {
+__global__ void __launch_bounds__(kBlock) k_bounds(StepArgs a, DevCtrl *ctrl, BoundsParams bp) {
+  __shared__ unsigned long long red[kBlock / 32][6];
+  const long long i = (long long)blockIdx.x * blockDim.x + threadIdx.x;
+  // six minima; the maxima are taken as minima of the complement
+  unsigned long long v[6] = {kEncMinId, kEncMinId, kEncMinId, kEncMinId, kEncMinId, kEncMinId};
+  bool bad = false;
+  if (i < a.n) {
+    const int8_t lab = a.label[i];
+    double x = a.x[i], y = a.y[i];
+    const double h = a.h[i];
+    double hn = h;
+    if (is_fluid(lab)) {
+      if (bp.stage != kStageNone || (bp.h_reset && !bp.h_fixed_on)) {
+        double rho = a.rho[i];
+        if (bp.stage != kStageNone) integrate_front(a, i, bp, x, y, rho);
+        if (bp.h_reset) hn = bp.h_fixed_on ? bp.h_fixed : compute_h(a.m[i], rho);
+      } else if (bp.h_reset) {
+        hn = bp.h_fixed;
+      }
+    }
+    bad = !(finite_bits(x) && finite_bits(y) && finite_bits(h));
+    if (!bad) {
+      v[0] = enc_d(x);
+      v[1] = ~v[0];
+      v[2] = enc_d(y);
+      v[3] = ~v[2];
+      v[4] = enc_d(h);
+      v[5] = ~enc_d(hn);
+    }
+  }
+  if (__syncthreads_or(bad) && threadIdx.x == 0) atomicOr(&ctrl->status, (unsigned)SPH_STATUS_NONFINITE);
+  const int lane = threadIdx.x & 31, wid = threadIdx.x >> 5;
+#pragma unroll
+  for (int q = 0; q < 6; q++) {
+    const unsigned long long m = warp_min_u64(v[q]);
+    if (lane == 0) red[wid][q] = m;
+  }
+  __syncthreads();
+  if (threadIdx.x < 6) {
+    const int q = threadIdx.x;
+    unsigned long long m = kEncMinId;
+    for (int w = 0; w < kBlock / 32; w++) m = red[w][q] < m ? red[w][q] : m;
+    if (m != kEncMinId) {
+      unsigned long long *slot[6] = {&ctrl->xmin, &ctrl->xmax, &ctrl->ymin, &ctrl->ymax, &ctrl->hmin_all,
+                                     &ctrl->hmax_new};
+      if (q & 1) atomicMax(slot[q], ~m);
+      else atomicMin(slot[q], m);
+    }
+  }
+}
+
+void launch_bounds(const StepArgs &a, const WsPtrs &w, const sph_config_t &cfg, int stage, bool h_reset,
+                   const double *dt_prev, const double *dt_cur, cudaStream_t st) {
   BoundsParams bp;
+  bp.stage = stage;
+  bp.euler = cfg.integrator == SPH_INTEGRATOR_EULER ? 1 : 0;
+  if (bp.euler && stage == kStagePredict) bp.stage = kStageNone;  // Euler.predict is a no-op
+  bp.h_reset = h_reset ? 1 : 0;
   bp.h_fixed = cfg.h_fixed;
-  bp.h_reset = mode != kBoundsOnly ? 1 : 0;
-  bp.predict = mode == kBoundsPredictPEC ? 1 : 0;
-  bp.dt_fixed = dt_fixed;
-  bp.dt = dt;
+  bp.h_fixed_on = cfg.h_fixed > 0.0 ? 1 : 0;
+  bp.dt_fixed = cfg.dt_fixed;
+  bp.dt_fixed_on = cfg.dt_fixed > 0.0 ? 1 : 0;
+  bp.dt_prev = dt_prev;
+  bp.dt_cur = dt_cur;
   bp.inv_damp = 1.0 / (1.0 + 0.5 * cfg.damping);
+  bp.c0 = 2.0 * bp.inv_damp - 1.0;
+  bp.damped = cfg.damping != 0.0 ? 1 : 0;
   bp.use_xsph = cfg.pec_use_xsph;
   bp.strict = cfg.pec_strict;
   k_bounds<<<nblocks(a.n), kBlock, 0, st>>>(a, w.ctrl, bp);
@@ -140,25 +226,40 @@ __global__ void k_grid(DevCtrl *ctrl, DevGrid *g, GridParams gp) {
   g->xmin = xmin; g->xmax = xmax; g->ymin = ymin; g->ymax = ymax;
   g->cs = cs; g->inv_cs = cs1;
   g->ncx = ncx; g->ncy = ncy; g->ncells_ref = ncx * ncy;
+  g->xminf = (float)xmin; g->yminf = (float)ymin; g->inv_csf = (float)cs1;
   g->hmax = hmax;
-  // interaction radius the pair kernels need: the kernel support (cubic 2h,
-  // Gaussian 3h) and the Lennard-Jones reach min(r0, 3h)
-  double kappa = gp.kernel == SPH_KERNEL_CUBIC ? 2.0 : 3.0;
-  double R = fmax(kappa * hmax, fmin(gp.r0, 3.0 * hmax)) * (1.0 + 1e-6);
+  // interaction radius: the kernel support (cubic 2h, Gaussian 3h) and the
+  // Lennard-Jones reach min(r0, 3h)
+  const bool cubic = gp.kernel == SPH_KERNEL_CUBIC;
+  double R = fmax((cubic ? 2.0 : 3.0) * hmax, fmin(gp.r0, 3.0 * hmax));
   double ext = fmax(xmax - xmin, ymax - ymin);
   R = fmax(R, fmax(ext * 1e-7, 1e-300));
   g->r_search = R;
-  bool fitsA = !huge && (double)ncx * (double)ncy <= (double)gp.max_cells;
-  if (fitsA && cs <= 1.5 * R) {
+  // the FP32 hi parts of the positions are truncated to 24 bits: a pair
+  // distance formed from them is off by at most 2^-22 sqrt(2) max|coordinate|
+  {
+    const double amax = fmax(fmax(fabs(xmin), fabs(xmax)), fmax(fabs(ymin), fabs(ymax)));
+    g->pad_e = (float)(1.5 * ldexp(amax, -22) + 1e-30);
+  }
+  // the cubic spline and its gradient vanish at q = 2, so pairs at exactly the
+  // support radius contribute nothing; the Gaussian is cut at q <= 3 inclusive
+  const bool trunc_free = cubic ? (cs >= R) : (cs >= R * (1.0 + 1e-9));
+  const bool fitsA = !huge && (double)ncx * (double)ncy <= (double)gp.max_cells;
+  if (!trunc_free && fitsA) {
     g->mode = 0;
     g->ntx = (int)ncx;
     g->nty = (int)ncy;
     g->ncells = (int)(ncx * ncy);
-    g->ox = xmin; g->oy = ymin; g->ct = cs; g->inv_ct = cs1;
+    g->ct = cs;
+    g->oxf = (float)xmin; g->oyf = (float)ymin; g->inv_ctf = (float)cs1;
+    g->wt = 1;
     g->need_filter = 0;
     g->wide = 1;
   } else {
-    double ct = R;
+    // cells of R/2 with a 5x5 stencil; the margin covers the FP32 binning error
+    const double amax = fmax(fmax(fabs(xmin), fabs(xmax)), fmax(fabs(ymin), fabs(ymax)));
+    double ct = 0.5 * R;
+    for (int it = 0; it < 2; it++) ct = 0.5 * R * (1.0 + 4.0 * (3e-7 * amax / ct) + 1e-5);
     double fnx = 1.0, fny = 1.0;
     bool fits = false;
     for (int it = 0; it < 64 && !fits; it++) {
@@ -174,15 +275,16 @@ __global__ void k_grid(DevCtrl *ctrl, DevGrid *g, GridParams gp) {
       ct = fmax(xmax - xmin, ymax - ymin) * 2.0 + R;
       fnx = fny = 1.0;
     }
-    long long ntx = (long long)fnx, nty = (long long)fny;
     g->mode = 1;
-    g->ntx = (int)ntx;
-    g->nty = (int)nty;
-    g->ncells = (int)(ntx * nty);
-    g->ox = xmin; g->oy = ymin; g->ct = ct; g->inv_ct = 1.0 / ct;
-    g->need_filter = (cs >= ct * (1.0 + 1e-9)) ? 0 : 1;
-    int wd = (int)ceil(3.0 * hmax * (1.0 + 1e-6) / ct);
-    g->wide = wd < 1 ? 1 : (wd > 1024 ? 1024 : wd);
+    g->ntx = (int)fnx;
+    g->nty = (int)fny;
+    g->ncells = (int)(fnx * fny);
+    g->ct = ct;
+    g->oxf = (float)xmin; g->oyf = (float)ymin; g->inv_ctf = (float)(1.0 / ct);
+    g->wt = 2;
+    g->need_filter = trunc_free ? 0 : 1;
+    int wd = (int)ceil(3.0 * hmax * (1.0 + 1e-6) / ct) + 1;
+    g->wide = wd < 2 ? 2 : (wd > 1024 ? 1024 : wd);
   }
   g->valid = 1;
   if (status) atomicOr(&ctrl->status, status);
@@ -199,10 +301,10 @@ __global__ void __launch_bounds__(kBlock) k_keys(const double *__restrict__ x, c
   bool alias = false, overflow = false;
   if (i < n) {
     const DevGrid &g = *gp;
-    double xi = x[i], yi = y[i];
-    long long cx = ref_floor_div(xi, g.xmin, g.cs, g.inv_cs);
-    long long cy = ref_floor_div(yi, g.ymin, g.cs, g.inv_cs);
-    long long flat = cx + g.ncx * cy;
+    const double xi = x[i], yi = y[i];
+    const long long cx = ref_cell(xi, g.xmin, g.cs, g.inv_cs, g.xminf, g.inv_csf);
+    const long long cy = ref_cell(yi, g.ymin, g.cs, g.inv_cs, g.yminf, g.inv_csf);
+    const long long flat = cx + g.ncx * cy;
     overflow = !(cx >= 0 && cy >= 0 && flat < g.ncells_ref);
     alias = !overflow && cx == g.ncx;
     refcell[i] = make_int2(sat_i32(cx), sat_i32(cy));
@@ -212,11 +314,12 @@ __global__ void __launch_bounds__(kBlock) k_keys(const double *__restrict__ x, c
     } else if (g.mode == 0) {
       key = (int)flat;
     } else {
-      long long tx = (long long)floor((xi - g.ox) * g.inv_ct);
-      long long ty = (long long)floor((yi - g.oy) * g.inv_ct);
+      // FP32 binning, monotone in the position (query and candidates agree)
+      int tx = (int)floorf((d2f_trunc(xi) - g.oxf) * g.inv_ctf);
+      int ty = (int)floorf((d2f_trunc(yi) - g.oyf) * g.inv_ctf);
       tx = tx < 0 ? 0 : (tx >= g.ntx ? g.ntx - 1 : tx);
       ty = ty < 0 ? 0 : (ty >= g.nty ? g.nty - 1 : ty);
-      key = (int)(tx + (long long)g.ntx * ty);
+      key = tx + g.ntx * ty;
     }
     keys[i] = key;
     atomicAdd(&counts[key], 1u);
@@ -234,17 +337,27 @@ __global__ void __launch_bounds__(kBlock) k_keys(const double *__restrict__ x, c
 // dump cell) into cstart[0 .. ncells + 1].  Three phases over tiles of
 // kScanTile cells; launch sizes depend only on the capacity.
 // ---------------------------------------------------------------------------
-__global__ void __launch_bounds__(kBlock) k_scan_tiles(const unsigned int *__restrict__ counts,
-                                                       const DevGrid *__restrict__ g,
-                                                       unsigned int *__restrict__ part) {
+constexpr int kScanThreads = 1024;
+constexpr int kScanPer = kScanTile / kScanThreads;
+
+__global__ void __launch_bounds__(kScanThreads) k_scan_tiles(const unsigned int *__restrict__ counts,
+                                                             const DevGrid *__restrict__ g,
+                                                             unsigned int *__restrict__ part) {
   __shared__ unsigned int red[32];
-  long long m = (long long)g->ncells + 1;
-  long long base = (long long)blockIdx.x * kScanTile;
+  const long long m = (long long)g->ncells + 1;
+  const long long base = (long long)blockIdx.x * kScanTile;
   unsigned int s = 0;
   if (base < m) {
-    for (int t = threadIdx.x; t < kScanTile; t += kBlock) {
-      long long c = base + t;
-      if (c < m) s += counts[c];
+    const uint4 *c4 = (const uint4 *)(counts + base);
+    for (int t = threadIdx.x; t < kScanTile / 4; t += kScanThreads) {
+      long long c = base + 4ll * t;
+      if (c + 3 < m) {
+        uint4 v = c4[t];
+        s += v.x + v.y + v.z + v.w;
+      } else {
+        for (int q = 0; q < 4; q++)
+          if (c + q < m) s += counts[c + q];
+      }
     }
   }
   s = block_reduce(s, AddU32(), 0u, red);
@@ -275,38 +388,58 @@ __global__ void __launch_bounds__(1024) k_scan_top(unsigned int *part, int npart
     }
 }
 
-__global__ void __launch_bounds__(kBlock) k_scan_apply(const unsigned int *__restrict__ counts,
-                                                       const DevGrid *__restrict__ g,
-                                                       const unsigned int *__restrict__ part,
-                                                       unsigned int *__restrict__ cstart) {
-  __shared__ unsigned int sh[kBlock];
-  constexpr int per = kScanTile / kBlock;  // 16 consecutive cells per thread
-  long long m = (long long)g->ncells + 1;
-  long long base = (long long)blockIdx.x * kScanTile;
+__global__ void __launch_bounds__(kScanThreads) k_scan_apply(const unsigned int *__restrict__ counts,
+                                                             const DevGrid *__restrict__ g,
+                                                             const unsigned int *__restrict__ part,
+                                                             unsigned int *__restrict__ cstart) {
+  __shared__ unsigned int warp_tot[32];
+  const long long m = (long long)g->ncells + 1;
+  const long long base = (long long)blockIdx.x * kScanTile;
   if (base >= m) return;
-  long long c0 = base + (long long)threadIdx.x * per;
-  unsigned int v[per];
-  unsigned int loc = 0;
+  static_assert(kScanPer == 4, "one uint4 per thread");
+  const long long c0 = base + (long long)threadIdx.x * kScanPer;
+  unsigned int v[kScanPer];
+  if (c0 + 3 < m) {
+    const uint4 q = *(const uint4 *)(counts + c0);
+    v[0] = q.x; v[1] = q.y; v[2] = q.z; v[3] = q.w;
+  } else {
 #pragma unroll
-  for (int t = 0; t < per; t++) {
-    v[t] = (c0 + t < m) ? counts[c0 + t] : 0u;
-    loc += v[t];
+    for (int t = 0; t < kScanPer; t++) v[t] = (c0 + t < m) ? counts[c0 + t] : 0u;
   }
-  sh[threadIdx.x] = loc;
+  const unsigned int loc = v[0] + v[1] + v[2] + v[3];
+  // block exclusive scan of loc: warp scan + scan of warp totals
+  const int lane = threadIdx.x & 31, wid = threadIdx.x >> 5;
+  unsigned int inc = loc;
+#pragma unroll
+  for (int o = 1; o < 32; o <<= 1) {
+    unsigned int u = __shfl_up_sync(0xffffffffu, inc, o);
+    if (lane >= o) inc += u;
+  }
+  if (lane == 31) warp_tot[wid] = inc;
   __syncthreads();
-  for (int o = 1; o < kBlock; o <<= 1) {
-    unsigned int u = threadIdx.x >= o ? sh[threadIdx.x - o] : 0u;
-    __syncthreads();
-    sh[threadIdx.x] += u;
-    __syncthreads();
-  }
-  unsigned int run = part[blockIdx.x] + sh[threadIdx.x] - loc;
+  if (wid == 0) {
+    unsigned int t = warp_tot[lane];
 #pragma unroll
-  for (int t = 0; t < per; t++) {
-    long long c = c0 + t;
-    if (c < m) cstart[c] = run;
-    run += v[t];
-    if (c == m - 1) cstart[m] = run;
+    for (int o = 1; o < 32; o <<= 1) {
+      unsigned int u = __shfl_up_sync(0xffffffffu, t, o);
+      if (lane >= o) t += u;
+    }
+    warp_tot[lane] = t;  // inclusive over warps
+  }
+  __syncthreads();
+  const unsigned int run = part[blockIdx.x] + (wid ? warp_tot[wid - 1] : 0u) + inc - loc;
+  const unsigned int r0 = run, r1 = r0 + v[0], r2 = r1 + v[1], r3 = r2 + v[2], r4 = r3 + v[3];
+  if (c0 + 3 < m) {
+    *(uint4 *)(cstart + c0) = make_uint4(r0, r1, r2, r3);
+  } else {
+    const unsigned int rr[4] = {r0, r1, r2, r3};
+#pragma unroll
+    for (int t = 0; t < kScanPer; t++)
+      if (c0 + t < m) cstart[c0 + t] = rr[t];
+  }
+  if (c0 <= m - 1 && m - 1 <= c0 + 3) {
+    const unsigned int rr[5] = {r0, r1, r2, r3, r4};
+    cstart[m] = rr[m - c0];  // total
   }
 }
 
@@ -352,9 +485,9 @@ void launch_build(const StepArgs &a, const WsPtrs &w, const sph_config_t &cfg, c
   k_grid<<<1, 32, 0, st>>>(w.ctrl, w.grid, gp);
   unsigned nb = nblocks(a.n);
   k_keys<<<nb, kBlock, 0, st>>>(a.x, a.y, a.n, w.grid, w.ctrl, w.keys, w.refcell, w.counts);
-  k_scan_tiles<<<(unsigned)w.n_parts, kBlock, 0, st>>>(w.counts, w.grid, w.scan_part);
+  k_scan_tiles<<<(unsigned)w.n_parts, kScanThreads, 0, st>>>(w.counts, w.grid, w.scan_part);
   k_scan_top<<<1, 1024, 0, st>>>(w.scan_part, (int)w.n_parts);
-  k_scan_apply<<<(unsigned)w.n_parts, kBlock, 0, st>>>(w.counts, w.grid, w.scan_part, w.cstart);
+  k_scan_apply<<<(unsigned)w.n_parts, kScanThreads, 0, st>>>(w.counts, w.grid, w.scan_part, w.cstart);
   k_scatter<<<nb, kBlock, 0, st>>>(w.keys, a.n, w.counts, w.cstart, w.perm_tmp, w.keys_sorted);
   k_cellsort<<<nb, kBlock, 0, st>>>(w.perm_tmp, w.keys_sorted, w.cstart, w.refcell, a.n, w.perm, w.meta);
 }
@@ -362,66 +495,151 @@ void launch_build(const StepArgs &a, const WsPtrs &w, const sph_config_t &cfg, c
 // ---------------------------------------------------------------------------
 // Sorted pair records.  The h reset and the Tait EOS of _loop's first pass
 // (SolverTools.py:122-127) are fused here; p, c and the fluid h go back to
-// the caller's arrays.  Non-fluid records carry h with the sign bit set.
+// the caller's arrays.
 // ---------------------------------------------------------------------------
 struct RecParams {
-  double h_fixed, gamma, B, rho0, Pb, co;
-  int write_state;  // write p, c, h to the caller's arrays
-  int p_from_state; // take p from the caller's array (second pass of summation density)
-  int mixed;
+  double h_fixed, gamma, B, inv_rho0, Pb, co;
+  float h_fixed_f, gamma_f, B_f, inv_rho0_f, rho0_hi, rho0_lo, Pb_f;
+  int h_fixed_on, Pb_on;
+  int write_state;   // write p, c, h to the caller's arrays
+  int from_state;    // p and h from the caller's arrays (second summation-density pass)
+  int reduce_h;      // min h over fluid for the step's TimeStep
 };
 
-__device__ __forceinline__ void split_df(double v, float &hi, float &lo) {
-  hi = __double2float_rn(v);
-  lo = __double2float_rn(v - (double)hi);
-}
-
+template <bool MIXED>
 __global__ void __launch_bounds__(kBlock) k_records(StepArgs a, const int *__restrict__ perm, RecParams rp,
-                                                    double4_32a *__restrict__ recA64, double4_32a *__restrict__ recB64,
-                                                    float4 *__restrict__ recP, float4 *__restrict__ recV,
-                                                    float4 *__restrict__ recS) {
-  long long k = (long long)blockIdx.x * blockDim.x + threadIdx.x;
-  if (k >= a.n) return;
-  int i = perm[k];
-  int8_t lab = a.label[i];
-  bool fl = is_fluid(lab);
-  double m = a.m[i], rho = a.rho[i], h = a.h[i];
-  double x = a.x[i], y = a.y[i], vx = a.vx[i], vy = a.vy[i];
-  if (fl) h = reset_h(rp.h_fixed, m, rho);
-  double p = rp.p_from_state ? a.p[i] : tait_p(rho, lab, rp.gamma, rp.B, rp.rho0, rp.Pb);
-  if (rp.write_state) {
-    a.p[i] = p;
-    a.c[i] = rp.co;
-    if (fl) a.h[i] = h;
-  }
-  double othr = p / (rho * rho);
-  double hs = fl ? h : -h;
-  if (!fl && h == 0.0) hs = -0.0;
-  if (!rp.mixed) {
-    recA64[k] = make_double4_32a(x, y, vx, vy);
-    recB64[k] = make_double4_32a(m, rho, othr, hs);
-  } else {
-    float xh, xl, yh, yl, vxh, vxl, vyh, vyl;
+                                                    DevCtrl *ctrl, float4 *__restrict__ rec0,
+                                                    float4 *__restrict__ rec1, float4 *__restrict__ rec2,
+                                                    double4_32a *__restrict__ r64a,
+                                                    double4_32a *__restrict__ r64b) {
+  __shared__ unsigned long long red[kBlock / 32];
+  __shared__ unsigned int redn[kBlock / 32];
+  const long long k = (long long)blockIdx.x * blockDim.x + threadIdx.x;
+  unsigned long long eh = kEncMinId;
+  unsigned int nf = 0;
+  if (k < a.n) {
+    const int i = perm[k];
+    const int8_t lab = a.label[i];
+    const bool fl = is_fluid(lab);
+    const double m = a.m[i], rho = a.rho[i];
+    const double x = a.x[i], y = a.y[i];
+    float xh, xl, yh, yl;
     split_df(x, xh, xl);
     split_df(y, yh, yl);
-    split_df(vx, vxh, vxl);
-    split_df(vy, vyh, vyl);
-    recP[k] = make_float4(xh, yh, xl, yl);
-    recV[k] = make_float4(vxh, vyh, vxl, vyl);
-    recS[k] = make_float4((float)m, (float)rho, (float)othr, (float)hs);
+    const float mf = d2f_trunc(m);
+    if (MIXED) {
+      // FP32 pair record; EOS on the relative density (no FP64 arithmetic)
+      float rh, rl;
+      split_df(rho, rh, rl);
+      float hf;
+      double hd;
+      if (rp.from_state || !fl) {
+        hd = a.h[i];
+        hf = d2f_trunc(hd);
+      } else if (rp.h_fixed_on) {
+        hd = rp.h_fixed;
+        hf = rp.h_fixed_f;
+      } else {
+        hf = rh > 1e-12f ? 1.3f * sqrtf(mf / rh) : 0.f;  // computeH in FP32
+        hd = f2d(hf);
+      }
+      float pf;  // gauge pressure B ((rho/rho0)^gamma - 1), FP32
+      double pd;
+      if (rp.from_state) {
+        pd = a.p[i];
+        pf = d2f_trunc(pd) - rp.Pb_f;
+      } else {
+        const float d = ((rh - rp.rho0_hi) + (rl - rp.rho0_lo)) * rp.inv_rho0_f;
+        pf = fl ? rp.B_f * tait_ratio_m1_f(d, rp.gamma_f) : 0.f;
+        pd = f2d(pf);
+        if (rp.Pb_on) pd += rp.Pb;
+      }
+      const float ir = rh != 0.f ? __frcp_rn(rh) : 0.f;
+      const float othr = (pf + rp.Pb_f) * ir * ir;
+      rec0[k] = make_float4(xh, yh, fl ? hf : -hf, mf);
+      rec1[k] = make_float4(xl, yl, rh, othr);
+      float vxh, vxl, vyh, vyl;
+      split_df(a.vx[i], vxh, vxl);
+      split_df(a.vy[i], vyh, vyl);
+      rec2[k] = make_float4(vxh, vyh, vxl, vyl);
+      if (rp.write_state) {
+        a.p[i] = pd;
+        a.c[i] = rp.co;
+        if (fl) a.h[i] = hd;
+      }
+      if (fl) {
+        eh = enc_d(hd);
+        nf = 1;
+      }
+    } else {
+      // FP64 record, the reference's arithmetic
+      double h = a.h[i];
+      if (fl && !rp.from_state) h = rp.h_fixed_on ? rp.h_fixed : compute_h(m, rho);
+      const double p = rp.from_state ? a.p[i] : tait_p(rho, lab, rp.gamma, rp.B, rp.inv_rho0, rp.Pb);
+      const double othr = p / (rho * rho);
+      const double hs = fl ? h : -h;
+      r64a[k] = make_double4_32a(x, y, a.vx[i], a.vy[i]);
+      r64b[k] = make_double4_32a(m, rho, othr, (!fl && h == 0.0) ? -0.0 : hs);
+      const float hf = d2f_trunc(h);
+      rec0[k] = make_float4(xh, yh, fl ? hf : -hf, mf);
+      if (rp.write_state) {
+        a.p[i] = p;
+        a.c[i] = rp.co;
+        if (fl) a.h[i] = h;
+      }
+      if (fl) {
+        eh = enc_d(h);
+        nf = 1;
+      }
+    }
+  }
+  if (rp.reduce_h) {
+    const unsigned long long wm = warp_min_u64(eh);
+    const unsigned int wn = __reduce_add_sync(0xffffffffu, nf);
+    const int lane = threadIdx.x & 31, wid = threadIdx.x >> 5;
+    if (lane == 0) {
+      red[wid] = wm;
+      redn[wid] = wn;
+    }
+    __syncthreads();
+    if (threadIdx.x == 0) {
+      unsigned long long bh = kEncMinId;
+      unsigned int bn = 0;
+      for (int w = 0; w < kBlock / 32; w++) {
+        bh = red[w] < bh ? red[w] : bh;
+        bn += redn[w];
+      }
+      if (bn) {
+        atomicMin(&ctrl->pd_hmin, bh);
+        atomicAdd(&ctrl->pd_nfluid, bn);
+      }
+    }
   }
 }
 
 void launch_records(const StepArgs &a, const WsPtrs &w, const sph_config_t &cfg, const sph_wcsph_t &wc,
-                    bool write_state, const double *rho_override, cudaStream_t st) {
+                    bool write_state, bool p_from_state, bool reduce_h, cudaStream_t st) {
   RecParams rp;
   rp.h_fixed = cfg.h_fixed;
-  rp.gamma = wc.gamma; rp.B = wc.B; rp.rho0 = wc.rho0; rp.Pb = wc.Pb; rp.co = wc.co;
+  rp.gamma = wc.gamma; rp.B = wc.B; rp.inv_rho0 = 1.0 / wc.rho0; rp.Pb = wc.Pb; rp.co = wc.co;
+  rp.h_fixed_f = (float)cfg.h_fixed;
+  rp.gamma_f = (float)wc.gamma;
+  rp.B_f = (float)wc.B;
+  rp.inv_rho0_f = (float)(1.0 / wc.rho0);
+  rp.rho0_hi = (float)wc.rho0;
+  rp.rho0_lo = (float)(wc.rho0 - (double)rp.rho0_hi);
+  rp.Pb_f = (float)wc.Pb;
+  rp.h_fixed_on = cfg.h_fixed > 0.0 ? 1 : 0;
+  rp.Pb_on = wc.Pb != 0.0 ? 1 : 0;
   rp.write_state = write_state ? 1 : 0;
-  rp.p_from_state = rho_override ? 1 : 0;
-  rp.mixed = cfg.precision == SPH_PREC_MIXED ? 1 : 0;
-  k_records<<<nblocks(a.n), kBlock, 0, st>>>(a, w.perm, rp, (double4_32a *)w.recA, (double4_32a *)w.recB,
-                                             (float4 *)w.recA, (float4 *)w.recB, (float4 *)w.recC);
+  rp.from_state = p_from_state ? 1 : 0;
+  rp.reduce_h = reduce_h ? 1 : 0;
+  if (cfg.precision == SPH_PREC_MIXED)
+    k_records<true><<<nblocks(a.n), kBlock, 0, st>>>(a, w.perm, rp, w.ctrl, w.rec0, w.rec1, w.rec2, w.rec64a,
+                                                     w.rec64b);
+  else
+    k_records<false><<<nblocks(a.n), kBlock, 0, st>>>(a, w.perm, rp, w.ctrl, w.rec0, w.rec1, w.rec2, w.rec64a,
+                                                      w.rec64b);
 }
 
 }  // namespace sph

@@ -1,19 +1,26 @@
 // pair.cu -- the fused pair interaction of the WCSPH step.
 //
-// One thread per (cell-sorted) fluid particle i gathers its neighbours from
-// the cell table and evaluates, in one pass, everything _loop computes per
-// particle (src/Tools/SolverTools.py:143-173): the kernel value and gradient
-// (src/Kernels/CubicSpline.py, src/Kernels/Gaussian.py), continuity
-// (src/Equations/Continuity.py), momentum with artificial viscosity and
-// gravity (src/Equations/Momentum.py, src/Methods/WCSPH.py:151-169), the
-// Lennard-Jones boundary force (src/Equations/BoundaryForce.py) and XSPH
-// (src/Equations/XSPH.py).  The TimeStep reductions of the next step
-// (src/Equations/TimeStep.py:58-91) are fused into the epilogue.
+// One thread per cell-sorted fluid particle i evaluates in one pass
+// everything _loop computes per particle (src/Tools/SolverTools.py:143-173):
+// the kernel value and gradient (src/Kernels/CubicSpline.py,
+// src/Kernels/Gaussian.py), continuity (src/Equations/Continuity.py),
+// momentum with artificial viscosity and gravity (src/Equations/Momentum.py,
+// src/Methods/WCSPH.py:151-169), the Lennard-Jones boundary force
+// (src/Equations/BoundaryForce.py) and XSPH (src/Equations/XSPH.py).  The
+// TimeStep of the next step (src/Equations/TimeStep.py:7-91) is fused into
+// the epilogue.
 //
-// FP64 form: the reference's arithmetic, with the neighbour test done with
-// explicitly rounded operations so that the accepted set is the reference's.
-// Mixed form: FP32 arithmetic on differences formed from double-float
-// (hi + lo) copies of the FP64 positions and velocities.
+// Each thread alternates two phases so that the expensive physics runs over
+// dense lists instead of sparse, divergent candidate loops:
+//   1. walk the stencil rows with one 16-byte load and a conservative FP32
+//      radius test per candidate (hi parts of the positions, padded by their
+//      truncation bound) and append the survivors to a per-thread list in
+//      shared memory;
+//   2. evaluate the pair physics over the list, after the exact test.
+// FP64 form: phase 2 redoes the reference's neighbour test exactly
+// (q = r / h_ij <= 3 with correctly rounded operations) and its arithmetic.
+// Mixed form: phase 2 runs in FP32 on double-float differences of the FP64
+// state.
 #include <math.h>
 
 #include "sph_internal.cuh"
@@ -21,6 +28,7 @@
 namespace sph {
 
 constexpr int kPairBlock = 128;
+constexpr int kListCap = 32;
 
 struct PairParams {
   double alpha, beta, co, eps, r0, D, p1, p2;
@@ -30,72 +38,95 @@ struct PairParams {
   long long n;
 };
 
-// Visit every candidate slot j of query slot k: the 3x3 stencil of the
-// reference grid (mode 0, validity as in NNLinkedList._get_valid_cell_index)
-// or a (2W+1)^2 stencil of the traversal grid (mode 1) with the
-// reference-stencil filter.  Cells of one stencil row are contiguous in the
-// sorted order, so each row is one range.
-template <typename F>
-__device__ __forceinline__ void for_each_candidate(const DevGrid &g, const unsigned int *__restrict__ cstart,
-                                                   int2 qref, int qkey, int W, bool filter,
-                                                   const int2 *__restrict__ meta, F &&f) {
-  int cxq, cyq;
-  if (g.mode == 0) {
-    cxq = qref.x;
-    cyq = qref.y;
-  } else {
-    if (qkey >= g.ncells) return;
-    cxq = qkey % g.ntx;
-    cyq = qkey / g.ntx;
-  }
-  const int nx = g.ntx, ny = g.nty;
-  for (int b = -W; b <= W; b++) {
-    int yy = cyq + b;
-    if (yy < 0 || yy >= ny) continue;
-    int x0 = max(cxq - W, 0), x1 = min(cxq + W, nx - 1);
-    if (x0 > x1) continue;
-    unsigned int s = __ldg(&cstart[x0 + nx * yy]), e = __ldg(&cstart[x1 + nx * yy + 1]);
-    for (unsigned int j = s; j < e; j++) {
-      if (filter) {
-        int2 mj = __ldg(&meta[j]);
-        int sx, sy;
-        storage_cell(mj.x, mj.y, g.ncx, sx, sy);
-        if (abs(sx - qref.x) > 1 || abs(sy - qref.y) > 1) continue;
-      }
-      f(j);
+// Stencil rows of one query: each row of cells is one contiguous range of
+// sorted slots.  Mode 0: the reference's 3x3 cells around the query's raw
+// cell (validity as NNLinkedList._get_valid_cell_index); mode 1: the own grid.
+struct Stencil {
+  int cx, cy, W, nx, ny;
+  bool ok;
+  __device__ __forceinline__ Stencil(const DevGrid &g, int2 qref, int qkey, int W_) {
+    W = W_;
+    nx = g.ntx;
+    ny = g.nty;
+    ok = true;
+    if (g.mode == 0) {
+      cx = qref.x;
+      cy = qref.y;
+    } else {
+      ok = qkey < g.ncells;
+      cx = qkey % g.ntx;
+      cy = qkey / g.ntx;
     }
   }
+  // range of row offset b; false when the row is outside the grid or empty
+  __device__ __forceinline__ bool row(int b, const unsigned int *__restrict__ cstart, unsigned int &s,
+                                      unsigned int &e) const {
+    const int yy = cy + b;
+    if (!ok || yy < 0 || yy >= ny) return false;
+    const int x0 = max(cx - W, 0), x1 = min(cx + W, nx - 1);
+    if (x0 > x1) return false;
+    s = __ldg(&cstart[x0 + nx * yy]);
+    e = __ldg(&cstart[x1 + nx * yy + 1]);
+    return s < e;
+  }
+};
+
+__device__ __forceinline__ bool in_ref_stencil(const int2 *__restrict__ meta, unsigned int j, const DevGrid &g,
+                                               int2 qref) {
+  const int2 mj = __ldg(&meta[j]);
+  int sx, sy;
+  storage_cell(mj.x, mj.y, g.ncx, sx, sy);
+  return abs(sx - qref.x) <= 1 && abs(sy - qref.y) <= 1;
 }
 
-// TimeStep epilogue: block-reduce min h, max a^2 over fluid, the last block
-// computes {dt, dt_courant, dt_force} (TimeStep.py:7-56) and resets the slots.
-__device__ __forceinline__ void timestep_epilogue(DevCtrl *ctrl, unsigned long long eh, unsigned long long ea,
-                                                  unsigned int nf, double co, double cfl_c, double cfl_f,
-                                                  double *dt_out, double *dt_hist, unsigned int *done) {
-  __shared__ unsigned long long red[32];
-  __shared__ unsigned int red32[32];
-  __shared__ bool last;
-  unsigned long long bh = block_reduce(eh, MinU64(), kEncMinId, red);
-  unsigned long long ba = block_reduce(ea, MaxU64(), kEncMaxId, red);
-  unsigned int bn = block_reduce(nf, AddU32(), 0u, red32);
-  if (threadIdx.x == 0) {
-    if (bn) {
-      atomicMin(&ctrl->ts_hmin, bh);
-      atomicMax(&ctrl->ts_a2max, ba);
-      atomicAdd(&ctrl->ts_nfluid, bn);
+// Exact size of the reference's neighbour set of a query whose own cell is
+// not in its stencil (x-overflow alias) or whose h is not positive; those are
+// the only queries that can have an empty set (src/Tools/SolverTools.py:150-153).
+__device__ int exact_count(const StepArgs &a, const int *__restrict__ perm, const DevGrid &g, int2 qref, int qkey,
+                           int W, bool filter, const int2 *__restrict__ meta, const unsigned int *__restrict__ cstart,
+                           double xi, double yi, double hi) {
+  const Stencil sten(g, qref, qkey, W);
+  int cnt = 0;
+  for (int b = -W; b <= W; b++) {
+    unsigned int s, e;
+    if (!sten.row(b, cstart, s, e)) continue;
+    for (unsigned int j = s; j < e; j++) {
+      if (filter && !in_ref_stencil(meta, j, g, qref)) continue;
+      const int pj = perm[j];
+      const double dx = xi - a.x[pj], dy = yi - a.y[pj];
+      const double r = __dsqrt_rn(__dadd_rn(__dmul_rn(dx, dx), __dmul_rn(dy, dy)));
+      const double q = __ddiv_rn(r, __dmul_rn(0.5, __dadd_rn(hi, a.h[pj])));
+      if (q <= 3.0) cnt++;
     }
+  }
+  return cnt;
+}
+
+// TimeStep epilogue: the block's max a^2 over fluid; the last block computes
+// {dt, dt_courant, dt_force} (TimeStep.py:7-56) from the min h the records
+// pass gathered, and resets the slots.
+__device__ __forceinline__ void timestep_epilogue(DevCtrl *ctrl, unsigned long long ea, double co, double cfl_c,
+                                                  double cfl_f, double *dt_out, double *dt_hist) {
+  __shared__ unsigned long long red[kPairBlock / 32];
+  __shared__ bool last;
+  const unsigned long long wm = warp_max_u64(ea);
+  if ((threadIdx.x & 31) == 0) red[threadIdx.x >> 5] = wm;
+  __syncthreads();
+  if (threadIdx.x == 0) {
+    unsigned long long ba = kEncMaxId;
+    for (int w = 0; w < kPairBlock / 32; w++) ba = red[w] > ba ? red[w] : ba;
+    if (ba != kEncMaxId) atomicMax(&ctrl->pd_a2max, ba);
     __threadfence();
-    unsigned int t = atomicAdd(done, 1u);
-    last = (t == gridDim.x - 1);
+    last = atomicAdd(&ctrl->done_pair, 1u) == gridDim.x - 1;
   }
   __syncthreads();
   if (last && threadIdx.x == 0) {
     __threadfence();
-    unsigned long long h = atomicExch(&ctrl->ts_hmin, kEncMinId);
-    unsigned long long a2 = atomicExch(&ctrl->ts_a2max, kEncMaxId);
-    unsigned int cnt = atomicExch(&ctrl->ts_nfluid, 0u);
-    atomicExch(done, 0u);
-    double min_h = dec_d(h), max_a2 = dec_d(a2), max_c = co;
+    const double min_h = dec_d(atomicExch(&ctrl->pd_hmin, kEncMinId));
+    const double max_a2 = dec_d(atomicExch(&ctrl->pd_a2max, kEncMaxId));
+    const unsigned int cnt = atomicExch(&ctrl->pd_nfluid, 0u);
+    atomicExch(&ctrl->done_pair, 0u);
+    const double max_c = co;  // compute_speed_of_sound gives co to every particle (WCSPH.py:110-129)
     double dc = __ddiv_rn(__dmul_rn(cfl_c, min_h), max_c);
     double df = max_a2 < 1e-12 ? 1e10 : __dmul_rn(cfl_f, __dsqrt_rn(__ddiv_rn(min_h, max_a2)));
     double dt = (df < dc) ? df : dc;  // Python min(c, f) keeps c on ties
@@ -124,330 +155,321 @@ __device__ __forceinline__ double accel2(double ax, double ay) {
   return __dadd_rn(__dmul_rn(ax, ax), __dmul_rn(ay, ay));
 }
 
-// ---------------------------------------------------------------------------
-// FP64 form
-// ---------------------------------------------------------------------------
-template <int KERNEL, bool XSPH, bool SUMDENS>
-__global__ void __launch_bounds__(kPairBlock)
-    k_pair64(StepArgs a, const double4_32a *__restrict__ recA, const double4_32a *__restrict__ recB,
-             const int *__restrict__ perm, const int *__restrict__ keys_sorted, const int2 *__restrict__ meta,
-             const unsigned int *__restrict__ cstart, const DevGrid *__restrict__ gp, DevCtrl *ctrl,
-             PairParams pp, double *dt_out, double *dt_hist) {
-  const DevGrid g = *gp;
-  const bool filter = g.mode == 1 && (g.need_filter || ctrl->alias_count > 0);
-  long long k = (long long)blockIdx.x * blockDim.x + threadIdx.x;
-  unsigned long long eh = kEncMinId, ea = kEncMaxId;
-  unsigned int nf = 0;
+struct PairPtrs {
+  const float4 *rec0, *rec1, *rec2;
+  const double4_32a *r64a, *r64b;
+  const int *perm, *keys_sorted;
+  const int2 *meta;
+  const unsigned int *cstart;
+  const DevGrid *grid;
+  DevCtrl *ctrl;
+};
+
+template <int KERNEL, bool XSPH, bool SUMDENS, bool MIXED>
+__global__ void __launch_bounds__(kPairBlock) k_pair(StepArgs a, PairPtrs P, PairParams pp, double *dt_out,
+                                                     double *dt_hist) {
+  __shared__ unsigned int lists[kListCap][kPairBlock];
+  const DevGrid g = *P.grid;
+  const bool filter = g.mode == 1 && (g.need_filter || P.ctrl->alias_count > 0);
+  const long long k = (long long)blockIdx.x * blockDim.x + threadIdx.x;
+  const int tid = threadIdx.x;
+  unsigned long long ea = kEncMaxId;
+  const float KC = KERNEL == SPH_KERNEL_CUBIC ? 4.0f : 9.0f;               // (support / h)^2
+  const float SK = (KERNEL == SPH_KERNEL_CUBIC ? 2.0f : 3.0f) * 1.000002f;  // support / h, padded
+  const float r0f = (float)pp.r0, r02f = r0f * r0f;
+  const float pad = g.pad_e;
   if (k < pp.n) {
-    const double4_32a Ai = recA[k], Bi = recB[k];
-    if (!signbit(Bi.w)) {
-      const int i = perm[k];
-      const double xi = Ai.x, yi = Ai.y, vxi = Ai.z, vyi = Ai.w;
-      const double rhoi = Bi.y, slf = Bi.z, hi = Bi.w;
-      const int2 qref = meta[k];
-      const int qkey = keys_sorted[k];
-      int W = 1;
-      if (g.mode == 1 && (qref.x == g.ncx || !(hi > 0.0))) W = g.wide;
-      double drho = 0.0, axs = 0.0, ays = 0.0, bx = 0.0, by = 0.0, sx = 0.0, sy = 0.0;
-      int cnt = 0;
-      for_each_candidate(g, cstart, qref, qkey, W, filter, meta, [&](unsigned int j) {
-        const double4_32a Aj = recA[j];
-        const double4_32a Bj = recB[j];
-        const double dx = xi - Aj.x, dy = yi - Aj.y;
-        const double d2 = __dadd_rn(__dmul_rn(dx, dx), __dmul_rn(dy, dy));
-        const double hij = __dmul_rn(0.5, __dadd_rn(hi, fabs(Bj.w)));
-        if (d2 > 9.0000001 * hij * hij) return;  // certainly q > 3
-        const double r = __dsqrt_rn(d2);
-        const double q = __ddiv_rn(r, hij);
-        if (!(q <= 3.0)) return;  // NNLinkedList.py:74
-        cnt++;
-        const bool jf = !signbit(Bj.w);
-        const double mj = Bj.x, rhoj = Bj.y;
-        const double vxij = vxi - Aj.z, vyij = vyi - Aj.w;
-        double w = 0.0, coef = 0.0;
-        if (KERNEL == SPH_KERNEL_CUBIC) {
-          if (q <= 2.0) {
-            const double alpha = kCubicFac / (hij * hij);
-            if (q > 1.0) {
-              const double t = 2.0 - q;
-              w = alpha * 0.25 * (t * t * t);
-              if (r >= 1e-10) coef = alpha * (-0.75 * (t * t)) / (hij * r);
+    const float4 Qi = P.rec0[k];  // x_hi, y_hi, h (signed), m
+    const float hif = Qi.z;
+    if (!signbit(hif)) {
+      const int i = P.perm[k];
+      const int2 qref = P.meta[k];
+      const int qkey = P.keys_sorted[k];
+      const bool slow = qref.x >= g.ncx || !(hif > 0.f);
+      const int W = g.mode == 0 ? 1 : (slow ? g.wide : g.wt);
+      // query state
+      double xi = 0, yi = 0, vxi = 0, vyi = 0, rhoi = 0, slf = 0, hi = 0;
+      float4 Ri = make_float4(0, 0, 0, 0), Vi = make_float4(0, 0, 0, 0);
+      if (MIXED) {
+        Ri = P.rec1[k];  // x_lo, y_lo, rho, p / rho^2
+        Vi = P.rec2[k];
+      } else {
+        const double4_32a A = P.r64a[k], B = P.r64b[k];
+        xi = A.x; yi = A.y; vxi = A.z; vyi = A.w;
+        rhoi = B.y; slf = B.z; hi = B.w;
+      }
+      // accumulators: FP32 (mixed) or FP64
+      float fd = 0.f, fax = 0.f, fay = 0.f, fbx = 0.f, fby = 0.f, fsx = 0.f, fsy = 0.f;
+      double dd = 0.0, dax = 0.0, day = 0.0, dbx = 0.0, dby = 0.0, dsx = 0.0, dsy = 0.0;
+      const float co = (float)pp.co, alpha = (float)pp.alpha, beta = (float)pp.beta, eps = (float)pp.eps;
+      const float D = (float)pp.D;
+
+      // ---- phase 2: pair physics over the list
+      auto physics = [&](int cnt) {
+        for (int t = 0; t < cnt; t++) {
+          const unsigned int j = lists[t][tid];
+          if (MIXED) {
+            const float4 qj = P.rec0[j];
+            const float4 rj = P.rec1[j];
+            const float dx = (Qi.x - qj.x) + (Ri.x - rj.x);
+            const float dy = (Qi.y - qj.y) + (Ri.y - rj.y);
+            const float d2 = dx * dx + dy * dy;
+            const float hij = 0.5f * (hif + fabsf(qj.z));
+            const float h2 = hij * hij;
+            const bool jf = !signbit(qj.z);
+            float lim = KC * h2;
+            if (!jf) lim = fmaxf(lim, fminf(r02f, 9.0f * h2));
+            if (d2 > lim) continue;
+            const float4 vj = P.rec2[j];
+            const float inv_h = __fdividef(1.0f, hij);
+            const float inv_r = d2 > 0.f ? rsqrtf(d2) : 0.f;
+            const float r = d2 * inv_r;
+            const float q = r * inv_h;
+            const float vxij = (Vi.x - vj.x) + (Vi.z - vj.z);
+            const float vyij = (Vi.y - vj.y) + (Vi.w - vj.w);
+            float w, coef;
+            if (KERNEL == SPH_KERNEL_CUBIC) {
+              const float al = (float)kCubicFac * inv_h * inv_h;
+              const float t2 = fmaxf(2.0f - q, 0.f);
+              const bool outer = q > 1.0f;
+              w = outer ? al * 0.25f * (t2 * t2 * t2) : al * (1.0f - 1.5f * (q * q) * (1.0f - 0.5f * q));
+              const float gq = outer ? -0.75f * (t2 * t2) : -3.0f * q * (1.0f - 0.75f * q);
+              coef = r >= 1e-10f ? al * gq * inv_h * inv_r : 0.f;
             } else {
-              w = alpha * (1.0 - 1.5 * (q * q) * (1.0 - 0.5 * q));
-              if (r >= 1e-10) coef = alpha * (-3.0 * q * (1.0 - 0.75 * q)) / (hij * r);
+              const float ac = (float)kInvPi * inv_h * inv_h;
+              const float e = __expf(-q * q);
+              w = ac * e;
+              coef = r * hij > 1e-12f ? -2.0f * ac * e * inv_h * inv_h : 0.f;
+            }
+            const float dwx = coef * dx, dwy = coef * dy;
+            const float mj = qj.w;
+            if (jf) {
+              if (!SUMDENS) fd = fmaf(mj, vxij * dwx + vyij * dwy, fd);
+              const float dot = vxij * dx + vyij * dy;
+              const float hb = 0.5f * (hif + hij);
+              const float mu = hb * dot * __fdividef(1.0f, d2 + 0.01f * hb * hb);
+              const float PI = dot < 0.f ? mu * (beta * mu - alpha * 0.5f * co) * __fdividef(2.0f, Ri.z + rj.z) : 0.f;
+              const float fac = mj * (Ri.w + rj.w + PI);
+              fax = fmaf(-fac, dwx, fax);
+              fay = fmaf(-fac, dwy, fay);
+            } else if (d2 <= r02f && d2 > 1e-24f) {
+              const float ir2 = __fdividef(1.0f, d2);
+              const float f2 = r02f * ir2;
+              const float fac = D * (f2 * f2 - f2) * ir2;
+              fbx = fmaf(fac, dx, fbx);
+              fby = fmaf(fac, dy, fby);
+            }
+            if (XSPH) {
+              const float fac = -eps * mj * w * __fdividef(2.0f, Ri.z + rj.z);
+              fsx = fmaf(fac, vxij, fsx);
+              fsy = fmaf(fac, vyij, fsy);
+            }
+          } else {
+            const double4_32a A = P.r64a[j], B = P.r64b[j];
+            const double dx = xi - A.x, dy = yi - A.y;
+            const double d2 = __dadd_rn(__dmul_rn(dx, dx), __dmul_rn(dy, dy));
+            const double hij = __dmul_rn(0.5, __dadd_rn(hi, fabs(B.w)));
+            const double r = __dsqrt_rn(d2);
+            const double q = __ddiv_rn(r, hij);
+            if (!(q <= 3.0)) continue;  // NNLinkedList.py:74
+            const bool jf = !signbit(B.w);
+            const double mj = B.x, rhoj = B.y;
+            const double vxij = vxi - A.z, vyij = vyi - A.w;
+            double w = 0.0, coef = 0.0;
+            if (KERNEL == SPH_KERNEL_CUBIC) {
+              if (q <= 2.0) {
+                const double al = kCubicFac / (hij * hij);
+                if (q > 1.0) {
+                  const double t2 = 2.0 - q;
+                  w = al * 0.25 * (t2 * t2 * t2);
+                  if (r >= 1e-10) coef = al * (-0.75 * (t2 * t2)) / (hij * r);
+                } else {
+                  w = al * (1.0 - 1.5 * (q * q) * (1.0 - 0.5 * q));
+                  if (r >= 1e-10) coef = al * (-3.0 * q * (1.0 - 0.75 * q)) / (hij * r);
+                }
+              }
+            } else {
+              const double ac = kInvPi / (hij * hij);
+              const double e = exp(-q * q);
+              w = ac * e;
+              const double tmp = r * hij;
+              if (tmp > 1e-12) coef = (-2.0 * q * ac * e) / tmp;
+            }
+            const double dwx = coef * dx, dwy = coef * dy;
+            if (jf) {
+              if (!SUMDENS) dd += mj * (vxij * dwx + vyij * dwy);
+              const double dot = vxij * dx + vyij * dy;
+              double PI = 0.0;
+              if (dot < 0.0) {
+                const double hb = 0.5 * (hi + hij);
+                const double mu = hb * dot / (r * r + 0.01 * hb * hb);
+                PI = mu * (pp.beta * mu - pp.alpha * (0.5 * pp.co)) / (0.5 * (rhoi + rhoj));
+              }
+              const double fac = slf + B.z + PI;
+              dax += -mj * fac * dwx;
+              day += -mj * fac * dwy;
+            } else if (r <= pp.r0 && r > 1e-12) {
+              const double frac = pp.r0 / r;
+              double tmp;
+              if (pp.lj_42) {
+                const double f2 = frac * frac;
+                tmp = f2 * f2 - f2;
+              } else {
+                tmp = pow(frac, pp.p1) - pow(frac, pp.p2);
+              }
+              const double fac = pp.D * tmp;
+              const double r2 = r * r;
+              dbx += fac * dx / r2;
+              dby += fac * dy / r2;
+            }
+            if (XSPH) {
+              const double fac = -pp.eps * mj * w / (0.5 * (rhoi + rhoj));
+              dsx += fac * vxij;
+              dsy += fac * vyij;
             }
           }
-        } else {
-          const double alpha_c = kInvPi / (hij * hij);
-          const double e = exp(-q * q);
-          w = alpha_c * e;
-          const double tmp = r * hij;
-          if (tmp > 1e-12) coef = (-2.0 * q * alpha_c * e) / tmp;
         }
-        const double dwx = coef * dx, dwy = coef * dy;
-        if (jf) {
-          if (!SUMDENS) drho += mj * (vxij * dwx + vyij * dwy);
-          const double dot = vxij * dx + vyij * dy;
-          double PI = 0.0;
-          if (dot < 0.0) {
-            const double hb = 0.5 * (hi + hij);
-            const double cb = 0.5 * pp.co;
-            const double rb = 0.5 * (rhoi + rhoj);
-            const double mu = hb * dot / (r * r + 0.01 * hb * hb);
-            PI = mu * (pp.beta * mu - pp.alpha * cb) / rb;
-          }
-          const double fac = slf + Bj.z + PI;
-          axs += -mj * fac * dwx;
-          ays += -mj * fac * dwy;
-        } else if (r <= pp.r0 && r > 1e-12) {
-          const double frac = pp.r0 / r;
-          double tmp;
-          if (pp.lj_42) {
-            const double f2 = frac * frac;
-            tmp = f2 * f2 - f2;
-          } else {
-            tmp = pow(frac, pp.p1) - pow(frac, pp.p2);
-          }
-          const double fac = pp.D * tmp;
-          const double r2 = r * r;
-          bx += fac * dx / r2;
-          by += fac * dy / r2;
-        }
-        if (XSPH) {
-          const double fac = -pp.eps * mj * w / (0.5 * (rhoi + rhoj));
-          sx += fac * vxij;
-          sy += fac * vyij;
-        }
-      });
-      double axf, ayf;
-      if (cnt > 0) {
-        axf = axs + bx;
-        ayf = (ays - 9.81) + by;
-        a.drho[i] = SUMDENS ? 0.0 : drho;
-        a.ax[i] = axf;
-        a.ay[i] = ayf;
-        a.xsphx[i] = XSPH ? vxi + sx : 0.0;
-        a.xsphy[i] = XSPH ? vyi + sy : 0.0;
-      } else {
-        axf = a.ax[i];
-        ayf = a.ay[i];
-      }
-      eh = enc_d(hi);
-      ea = enc_d(accel2(axf, ayf));
-      nf = 1;
-    }
-  }
-  if (pp.do_dt) timestep_epilogue(ctrl, eh, ea, nf, pp.co, pp.cfl_c, pp.cfl_f, dt_out, dt_hist, &ctrl->done_pair);
-}
+      };
 
-// ---------------------------------------------------------------------------
-// Mixed form: FP32 pair arithmetic, FP64 state
-// ---------------------------------------------------------------------------
-template <int KERNEL, bool XSPH, bool SUMDENS>
-__global__ void __launch_bounds__(kPairBlock)
-    k_pair32(StepArgs a, const float4 *__restrict__ recP, const float4 *__restrict__ recV,
-             const float4 *__restrict__ recS, const int *__restrict__ perm, const int *__restrict__ keys_sorted,
-             const int2 *__restrict__ meta, const unsigned int *__restrict__ cstart,
-             const DevGrid *__restrict__ gp, DevCtrl *ctrl, PairParams pp, double *dt_out, double *dt_hist) {
-  const DevGrid g = *gp;
-  const bool filter = g.mode == 1 && (g.need_filter || ctrl->alias_count > 0);
-  long long k = (long long)blockIdx.x * blockDim.x + threadIdx.x;
-  unsigned long long eh = kEncMinId, ea = kEncMaxId;
-  unsigned int nf = 0;
-  const float co = (float)pp.co, alpha = (float)pp.alpha, beta = (float)pp.beta, eps = (float)pp.eps;
-  const float r0 = (float)pp.r0, D = (float)pp.D;
-  const float r02 = r0 * r0;
-  if (k < pp.n) {
-    const float4 Si = recS[k];
-    if (!signbit(Si.w)) {
-      const int i = perm[k];
-      const float4 Pi = recP[k], Vi = recV[k];
-      const float rhoi = Si.y, slf = Si.z, hi = Si.w;
-      const int2 qref = meta[k];
-      const int qkey = keys_sorted[k];
-      int W = 1;
-      if (g.mode == 1 && (qref.x == g.ncx || !(hi > 0.0f))) W = g.wide;
-      float drho = 0.f, axs = 0.f, ays = 0.f, bx = 0.f, by = 0.f, sx = 0.f, sy = 0.f;
-      int cnt = 0;
-      for_each_candidate(g, cstart, qref, qkey, W, filter, meta, [&](unsigned int j) {
-        const float4 Pj = __ldg(&recP[j]);
-        const float4 Sj = __ldg(&recS[j]);
-        const float dx = (Pi.x - Pj.x) + (Pi.z - Pj.z);
-        const float dy = (Pi.y - Pj.y) + (Pi.w - Pj.w);
-        const float d2 = dx * dx + dy * dy;
-        const float hij = 0.5f * (hi + fabsf(Sj.w));
-        const float h2 = hij * hij;
-        if (!(d2 <= 9.0f * h2)) return;
-        cnt++;
-        const bool jf = !signbit(Sj.w);
-        if (KERNEL == SPH_KERNEL_CUBIC && d2 > 4.0f * h2) {
-          // outside the cubic support: only the boundary force can act
-          if (!jf && d2 <= r02 && d2 > 1e-24f) {
-            const float ir2 = 1.0f / d2;
-            const float f2 = r02 * ir2;
-            const float fac = D * (f2 * f2 - f2);
-            bx += fac * dx * ir2;
-            by += fac * dy * ir2;
+      // ---- phase 1: padded FP32 radius test, append to this thread's list
+      const Stencil sten(g, qref, qkey, W);
+      int nl = 0;
+      for (int b = -W; b <= W; b++) {
+        unsigned int s, e;
+        if (!sten.row(b, P.cstart, s, e)) continue;
+        for (unsigned int j = s; j < e; j++) {
+          if (j == (unsigned int)k) continue;  // the particle itself contributes zero
+          if (filter && !in_ref_stencil(P.meta, j, g, qref)) continue;
+          const float4 qj = P.rec0[j];
+          const float dx = Qi.x - qj.x, dy = Qi.y - qj.y;
+          const float d2 = dx * dx + dy * dy;
+          const float hij = 0.5f * (hif + fabsf(qj.z));
+          float reach = SK * hij;
+          if (signbit(qj.z)) reach = fmaxf(reach, fminf(r0f, 3.0f * hij) * 1.000002f);
+          const float rp = reach + pad;
+          if (d2 <= rp * rp) {
+            lists[nl][tid] = j;
+            if (++nl == kListCap) {
+              physics(nl);
+              nl = 0;
+            }
           }
-          return;
         }
-        const float4 Vj = __ldg(&recV[j]);
-        const float mj = Sj.x, rhoj = Sj.y;
-        const float vxij = (Vi.x - Vj.x) + (Vi.z - Vj.z);
-        const float vyij = (Vi.y - Vj.y) + (Vi.w - Vj.w);
-        const float inv_r = d2 > 0.f ? rsqrtf(d2) : 0.f;
-        const float r = d2 * inv_r;
-        const float inv_h = __fdividef(1.0f, hij);
-        const float q = r * inv_h;
-        float w, coef = 0.f;
-        if (KERNEL == SPH_KERNEL_CUBIC) {
-          const float al = (float)kCubicFac * inv_h * inv_h;
-          if (q > 1.0f) {
-            const float t = 2.0f - q;
-            w = al * 0.25f * (t * t * t);
-            if (r >= 1e-10f) coef = al * (-0.75f * (t * t)) * inv_h * inv_r;
+      }
+      physics(nl);
+
+      // the reference's set always holds the particle itself, except for the
+      // slow queries, whose set size is counted exactly
+      bool any = true;
+      if (slow) {
+        if (MIXED) {
+          xi = a.x[i];
+          yi = a.y[i];
+          hi = a.h[i];
+        }
+        any = exact_count(a, P.perm, g, qref, qkey, W, g.mode == 1, P.meta, P.cstart, xi, yi, hi) > 0;
+      }
+      if (any) {
+        double axf, ayf;
+        if (MIXED) {
+          const float axs = fax + fbx, ays = fay + fby;
+          axf = f2d(axs);
+          ayf = f2d(ays) - 9.81;
+          a.drho[i] = SUMDENS ? 0.0 : f2d(fd);
+          if (XSPH) {
+            a.xsphx[i] = a.vx[i] + f2d(fsx);
+            a.xsphy[i] = a.vy[i] + f2d(fsy);
           } else {
-            w = al * (1.0f - 1.5f * (q * q) * (1.0f - 0.5f * q));
-            if (r >= 1e-10f) coef = al * (-3.0f * q * (1.0f - 0.75f * q)) * inv_h * inv_r;
+            a.xsphx[i] = 0.0;
+            a.xsphy[i] = 0.0;
           }
+          const float ayg = ays - 9.81f;
+          ea = enc_d(f2d(axs * axs + ayg * ayg));
         } else {
-          const float ac = (float)kInvPi * inv_h * inv_h;
-          const float e = __expf(-q * q);
-          w = ac * e;
-          if (r * hij > 1e-12f) coef = -2.0f * ac * e * inv_h * inv_h;
+          axf = dax + dbx;
+          ayf = (day - 9.81) + dby;
+          a.drho[i] = SUMDENS ? 0.0 : dd;
+          a.xsphx[i] = XSPH ? vxi + dsx : 0.0;
+          a.xsphy[i] = XSPH ? vyi + dsy : 0.0;
+          ea = enc_d(accel2(axf, ayf));
         }
-        const float dwx = coef * dx, dwy = coef * dy;
-        if (jf) {
-          if (!SUMDENS) drho += mj * (vxij * dwx + vyij * dwy);
-          const float dot = vxij * dx + vyij * dy;
-          float PI = 0.f;
-          if (dot < 0.f) {
-            const float hb = 0.5f * (hi + hij);
-            const float mu = hb * dot / (d2 + 0.01f * hb * hb);
-            PI = mu * (beta * mu - alpha * 0.5f * co) / (0.5f * (rhoi + rhoj));
-          }
-          const float fac = slf + Sj.z + PI;
-          axs -= mj * fac * dwx;
-          ays -= mj * fac * dwy;
-        } else if (d2 <= r02 && d2 > 1e-24f) {
-          const float ir2 = 1.0f / d2;
-          const float f2 = r02 * ir2;
-          const float fac = D * (f2 * f2 - f2);
-          bx += fac * dx * ir2;
-          by += fac * dy * ir2;
-        }
-        if (XSPH) {
-          const float fac = -eps * mj * w / (0.5f * (rhoi + rhoj));
-          sx += fac * vxij;
-          sy += fac * vyij;
-        }
-      });
-      double axf, ayf;
-      if (cnt > 0) {
-        axf = (double)axs + (double)bx;
-        ayf = ((double)ays - 9.81) + (double)by;
-        a.drho[i] = SUMDENS ? 0.0 : (double)drho;
         a.ax[i] = axf;
         a.ay[i] = ayf;
-        if (XSPH) {
-          a.xsphx[i] = a.vx[i] + (double)sx;
-          a.xsphy[i] = a.vy[i] + (double)sy;
-        } else {
-          a.xsphx[i] = 0.0;
-          a.xsphy[i] = 0.0;
-        }
       } else {
-        axf = a.ax[i];
-        ayf = a.ay[i];
+        ea = enc_d(accel2(a.ax[i], a.ay[i]));  // keeps its previous values (SolverTools.py:150-153)
       }
-      eh = enc_d(a.h[i]);
-      ea = enc_d(accel2(axf, ayf));
-      nf = 1;
     }
   }
-  if (pp.do_dt) timestep_epilogue(ctrl, eh, ea, nf, pp.co, pp.cfl_c, pp.cfl_f, dt_out, dt_hist, &ctrl->done_pair);
+  if (pp.do_dt) timestep_epilogue(P.ctrl, ea, pp.co, pp.cfl_c, pp.cfl_f, dt_out, dt_hist);
 }
 
 // ---------------------------------------------------------------------------
 // Summation density (SolverTools.py:129-140, SummationDensity.py:5-13):
-// rho_i = sum over fluid neighbours of m_j W(r, h_ij), written to rho[i].
+// rho_i = sum over fluid neighbours (itself included) of m_j W(r, h_ij).
 // ---------------------------------------------------------------------------
 template <int KERNEL, bool MIXED>
-__global__ void __launch_bounds__(kPairBlock)
-    k_sumdens(StepArgs a, const void *__restrict__ rA, const void *__restrict__ rB, const void *__restrict__ rC,
-              const int *__restrict__ perm, const int *__restrict__ keys_sorted, const int2 *__restrict__ meta,
-              const unsigned int *__restrict__ cstart, const DevGrid *__restrict__ gp, const DevCtrl *ctrl,
-              long long n) {
-  const DevGrid g = *gp;
-  const bool filter = g.mode == 1 && (g.need_filter || ctrl->alias_count > 0);
-  long long k = (long long)blockIdx.x * blockDim.x + threadIdx.x;
+__global__ void __launch_bounds__(kPairBlock) k_sumdens(StepArgs a, PairPtrs P, long long n) {
+  const DevGrid g = *P.grid;
+  const bool filter = g.mode == 1 && (g.need_filter || P.ctrl->alias_count > 0);
+  const long long k = (long long)blockIdx.x * blockDim.x + threadIdx.x;
   if (k >= n) return;
-  const double4_32a *recA = (const double4_32a *)rA, *recB = (const double4_32a *)rB;
-  const float4 *recP = (const float4 *)rA, *recS = (const float4 *)rC;
-  double hi, xi = 0, yi = 0;
-  float4 Pi;
+  const float4 Qi = P.rec0[k];
+  const float hif = Qi.z;
+  if (signbit(hif)) return;
+  const int2 qref = P.meta[k];
+  const int qkey = P.keys_sorted[k];
+  const bool slow = qref.x >= g.ncx || !(hif > 0.f);
+  const int W = g.mode == 0 ? 1 : (slow ? g.wide : g.wt);
+  double xi = 0, yi = 0, hi = 0;
+  float4 Ri = make_float4(0, 0, 0, 0);
   if (MIXED) {
-    float4 Si = recS[k];
-    if (signbit(Si.w)) return;
-    hi = Si.w;
-    Pi = recP[k];
+    Ri = P.rec1[k];
   } else {
-    double4_32a Bi = recB[k];
-    if (signbit(Bi.w)) return;
-    hi = Bi.w;
-    double4_32a Ai = recA[k];
-    xi = Ai.x;
-    yi = Ai.y;
+    const double4_32a A = P.r64a[k], B = P.r64b[k];
+    xi = A.x; yi = A.y; hi = B.w;
   }
-  const int2 qref = meta[k];
-  const int qkey = keys_sorted[k];
-  int W = 1;
-  if (g.mode == 1 && (qref.x == g.ncx || !(hi > 0.0))) W = g.wide;
+  const float KC = KERNEL == SPH_KERNEL_CUBIC ? 4.0f : 9.0f;
+  const float SK = (KERNEL == SPH_KERNEL_CUBIC ? 2.0f : 3.0f) * 1.000002f;
   double rho = 0.0;
   float rhof = 0.f;
-  for_each_candidate(g, cstart, qref, qkey, W, filter, meta, [&](unsigned int j) {
-    if (MIXED) {
-      const float4 Pj = __ldg(&recP[j]);
-      const float4 Sj = __ldg(&recS[j]);
-      const float dx = (Pi.x - Pj.x) + (Pi.z - Pj.z);
-      const float dy = (Pi.y - Pj.y) + (Pi.w - Pj.w);
-      const float d2 = dx * dx + dy * dy;
-      const float hij = 0.5f * ((float)hi + fabsf(Sj.w));
-      if (!(d2 <= 9.0f * hij * hij) || signbit(Sj.w)) return;
-      const float q = sqrtf(d2) / hij;
-      float w;
-      if (KERNEL == SPH_KERNEL_CUBIC) {
-        const float al = (float)kCubicFac / (hij * hij);
-        if (q > 2.0f) w = 0.f;
-        else if (q > 1.0f) { const float t = 2.0f - q; w = al * 0.25f * t * t * t; }
-        else w = al * (1.0f - 1.5f * q * q * (1.0f - 0.5f * q));
+  const Stencil sten(g, qref, qkey, W);
+  for (int b = -W; b <= W; b++) {
+    unsigned int s, e;
+    if (!sten.row(b, P.cstart, s, e)) continue;
+    for (unsigned int j = s; j < e; j++) {
+      if (filter && !in_ref_stencil(P.meta, j, g, qref)) continue;
+      const float4 qj = P.rec0[j];
+      if (signbit(qj.z)) continue;  // SummationDensity.py: fluid neighbours only
+      const float hij = 0.5f * (hif + fabsf(qj.z));
+      if (MIXED) {
+        const float4 rj = P.rec1[j];
+        const float dx = (Qi.x - qj.x) + (Ri.x - rj.x);
+        const float dy = (Qi.y - qj.y) + (Ri.y - rj.y);
+        const float d2 = dx * dx + dy * dy;
+        if (d2 > KC * hij * hij) continue;
+        const float q = sqrtf(d2) / hij;
+        float w;
+        if (KERNEL == SPH_KERNEL_CUBIC) {
+          const float al = (float)kCubicFac / (hij * hij);
+          const float t = fmaxf(2.0f - q, 0.f);
+          w = q > 1.0f ? al * 0.25f * t * t * t : al * (1.0f - 1.5f * q * q * (1.0f - 0.5f * q));
+        } else {
+          w = (float)kInvPi / (hij * hij) * __expf(-q * q);
+        }
+        rhof += qj.w * w;
       } else {
-        w = (float)kInvPi / (hij * hij) * __expf(-q * q);
+        const float dx = Qi.x - qj.x, dy = Qi.y - qj.y;
+        const float rp = SK * hij + g.pad_e;
+        if (dx * dx + dy * dy > rp * rp) continue;
+        const double4_32a A = P.r64a[j], B = P.r64b[j];
+        const double ddx = xi - A.x, ddy = yi - A.y;
+        const double r = __dsqrt_rn(__dadd_rn(__dmul_rn(ddx, ddx), __dmul_rn(ddy, ddy)));
+        const double h = __dmul_rn(0.5, __dadd_rn(hi, fabs(B.w)));
+        if (__ddiv_rn(r, h) <= 3.0) rho += B.x * (KERNEL == SPH_KERNEL_CUBIC ? cubic_w(r, h) : gauss_w(r, h));
       }
-      rhof += Sj.x * w;
-    } else {
-      const double4_32a Aj = recA[j];
-      const double4_32a Bj = recB[j];
-      const double dx = xi - Aj.x, dy = yi - Aj.y;
-      const double d2 = __dadd_rn(__dmul_rn(dx, dx), __dmul_rn(dy, dy));
-      const double hij = __dmul_rn(0.5, __dadd_rn(hi, fabs(Bj.w)));
-      if (d2 > 9.0000001 * hij * hij) return;
-      const double r = __dsqrt_rn(d2);
-      const double q = __ddiv_rn(r, hij);
-      if (!(q <= 3.0) || signbit(Bj.w)) return;
-      double w;
-      if (KERNEL == SPH_KERNEL_CUBIC) {
-        const double al = kCubicFac / (hij * hij);
-        if (q > 2.0) w = 0.0;
-        else if (q > 1.0) { const double t = 2.0 - q; w = al * 0.25 * t * t * t; }
-        else w = al * (1.0 - 1.5 * q * q * (1.0 - 0.5 * q));
-      } else {
-        w = kInvPi / (hij * hij) * exp(-q * q);
-      }
-      rho += Bj.x * w;
     }
-  });
-  a.rho[perm[k]] = MIXED ? (double)rhof : rho;
+  }
+  a.rho[P.perm[k]] = MIXED ? f2d(rhof) : rho;
 }
 
 // ---------------------------------------------------------------------------
@@ -458,8 +480,7 @@ __global__ void __launch_bounds__(kPairBlock)
     k_nn_export(const double *__restrict__ x, const double *__restrict__ y, const double *__restrict__ h,
                 long long n, const int *__restrict__ perm, const int *__restrict__ keys_sorted,
                 const int2 *__restrict__ meta, const unsigned int *__restrict__ cstart,
-                const DevGrid *__restrict__ gp, const DevCtrl *ctrl, int64_t *counts, const int64_t *offsets,
-                int64_t *idx) {
+                const DevGrid *__restrict__ gp, int64_t *counts, const int64_t *offsets, int64_t *idx) {
   const DevGrid g = *gp;
   long long k = (long long)blockIdx.x * blockDim.x + threadIdx.x;
   if (k >= n) return;
@@ -471,17 +492,24 @@ __global__ void __launch_bounds__(kPairBlock)
   const bool filter = g.mode == 1;
   long long cnt = 0;
   const long long base = idx ? offsets[i] : 0;
-  for_each_candidate(g, cstart, qref, qkey, W, filter, meta, [&](unsigned int j) {
-    const int pj = perm[j];
-    const double dx = xi - x[pj], dy = yi - y[pj];
-    const double d2 = __dadd_rn(__dmul_rn(dx, dx), __dmul_rn(dy, dy));
-    const double r = __dsqrt_rn(d2);
-    const double hij = __dmul_rn(0.5, __dadd_rn(hi, h[pj]));
-    const double q = __ddiv_rn(r, hij);
-    if (!(q <= 3.0)) return;
-    if (idx) idx[base + cnt] = pj;
-    cnt++;
-  });
+  const Stencil sten(g, qref, qkey, W);
+  for (int b = -W; b <= W; b++) {
+    unsigned int s, e;
+    if (!sten.row(b, cstart, s, e)) continue;
+    for (unsigned int j = s; j < e; j++) {
+      if (filter && !in_ref_stencil(meta, j, g, qref)) continue;
+      const int pj = perm[j];
+      const double dx = xi - x[pj], dy = yi - y[pj];
+      const double d2 = __dadd_rn(__dmul_rn(dx, dx), __dmul_rn(dy, dy));
+      const double r = __dsqrt_rn(d2);
+      const double hij = __dmul_rn(0.5, __dadd_rn(hi, h[pj]));
+      const double q = __ddiv_rn(r, hij);
+      if (q <= 3.0) {
+        if (idx) idx[base + cnt] = pj;
+        cnt++;
+      }
+    }
+  }
   if (!idx) {
     counts[i] = cnt;
     return;
@@ -501,6 +529,14 @@ __global__ void __launch_bounds__(kPairBlock)
 // ---------------------------------------------------------------------------
 // Launchers
 // ---------------------------------------------------------------------------
+static PairPtrs pair_ptrs(const WsPtrs &w) {
+  PairPtrs P;
+  P.rec0 = w.rec0; P.rec1 = w.rec1; P.rec2 = w.rec2; P.r64a = w.rec64a; P.r64b = w.rec64b;
+  P.perm = w.perm; P.keys_sorted = w.keys_sorted; P.meta = w.meta; P.cstart = w.cstart;
+  P.grid = w.grid; P.ctrl = w.ctrl;
+  return P;
+}
+
 static PairParams pair_params(const StepArgs &a, const sph_config_t &cfg, const sph_wcsph_t &wc, bool do_dt) {
   PairParams pp;
   pp.alpha = wc.alpha; pp.beta = wc.beta; pp.co = wc.co; pp.eps = wc.epsilon;
@@ -515,15 +551,11 @@ static PairParams pair_params(const StepArgs &a, const sph_config_t &cfg, const 
 template <int KERNEL, bool XSPH, bool SUMDENS>
 static void pair_dispatch(const StepArgs &a, const WsPtrs &w, const sph_config_t &cfg, const PairParams &pp,
                           double *dt_out, double *dt_hist, cudaStream_t st) {
-  unsigned nb = nblocks(a.n, kPairBlock);
+  const unsigned nb = nblocks(a.n, kPairBlock);
   if (cfg.precision == SPH_PREC_MIXED)
-    k_pair32<KERNEL, XSPH, SUMDENS><<<nb, kPairBlock, 0, st>>>(
-        a, (const float4 *)w.recA, (const float4 *)w.recB, (const float4 *)w.recC, w.perm, w.keys_sorted, w.meta,
-        w.cstart, w.grid, w.ctrl, pp, dt_out, dt_hist);
+    k_pair<KERNEL, XSPH, SUMDENS, true><<<nb, kPairBlock, 0, st>>>(a, pair_ptrs(w), pp, dt_out, dt_hist);
   else
-    k_pair64<KERNEL, XSPH, SUMDENS><<<nb, kPairBlock, 0, st>>>(a, (const double4_32a *)w.recA,
-                                                              (const double4_32a *)w.recB, w.perm, w.keys_sorted,
-                                                              w.meta, w.cstart, w.grid, w.ctrl, pp, dt_out, dt_hist);
+    k_pair<KERNEL, XSPH, SUMDENS, false><<<nb, kPairBlock, 0, st>>>(a, pair_ptrs(w), pp, dt_out, dt_hist);
 }
 
 void launch_pair(const StepArgs &a, const WsPtrs &w, const sph_config_t &cfg, const sph_wcsph_t &wc,
@@ -545,25 +577,22 @@ void launch_pair(const StepArgs &a, const WsPtrs &w, const sph_config_t &cfg, co
 
 void launch_sumdens(const StepArgs &a, const WsPtrs &w, const sph_config_t &cfg, const sph_wcsph_t &wc,
                     cudaStream_t st) {
-  unsigned nb = nblocks(a.n, kPairBlock);
-  bool mixed = cfg.precision == SPH_PREC_MIXED;
-#define SPH_SD(KN, MX)                                                                                     \
-  k_sumdens<KN, MX><<<nb, kPairBlock, 0, st>>>(a, w.recA, w.recB, w.recC, w.perm, w.keys_sorted, w.meta, \
-                                               w.cstart, w.grid, w.ctrl, a.n)
+  const unsigned nb = nblocks(a.n, kPairBlock);
+  const bool mixed = cfg.precision == SPH_PREC_MIXED;
+  const PairPtrs P = pair_ptrs(w);
   if (cfg.kernel == SPH_KERNEL_CUBIC) {
-    if (mixed) SPH_SD(SPH_KERNEL_CUBIC, true);
-    else SPH_SD(SPH_KERNEL_CUBIC, false);
+    if (mixed) k_sumdens<SPH_KERNEL_CUBIC, true><<<nb, kPairBlock, 0, st>>>(a, P, a.n);
+    else k_sumdens<SPH_KERNEL_CUBIC, false><<<nb, kPairBlock, 0, st>>>(a, P, a.n);
   } else {
-    if (mixed) SPH_SD(SPH_KERNEL_GAUSSIAN, true);
-    else SPH_SD(SPH_KERNEL_GAUSSIAN, false);
+    if (mixed) k_sumdens<SPH_KERNEL_GAUSSIAN, true><<<nb, kPairBlock, 0, st>>>(a, P, a.n);
+    else k_sumdens<SPH_KERNEL_GAUSSIAN, false><<<nb, kPairBlock, 0, st>>>(a, P, a.n);
   }
-#undef SPH_SD
 }
 
 void launch_nn_count(const StepArgs &a, const WsPtrs &w, int64_t *counts, const int64_t *offsets, int64_t *idx,
                      cudaStream_t st) {
   k_nn_export<<<nblocks(a.n, kPairBlock), kPairBlock, 0, st>>>(a.x, a.y, a.h, a.n, w.perm, w.keys_sorted, w.meta,
-                                                               w.cstart, w.grid, w.ctrl, counts, offsets, idx);
+                                                               w.cstart, w.grid, counts, offsets, idx);
 }
 
 }  // namespace sph

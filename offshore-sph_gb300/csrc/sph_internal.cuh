@@ -1,5 +1,11 @@
 // sph_internal.cuh -- device-side structures and math shared by the kernels
 // of the WCSPH step (neighbour build, fused pair interaction, integrators).
+//
+// A note on arithmetic: on GB300 the FP64 pipe issues a small fraction of the
+// FP32/INT rate, so even per-particle stages become FP64-issue-bound long
+// before they reach HBM bandwidth.  The mixed form therefore moves every
+// conversion it can to the integer pipe (bit-level double<->float splits) and
+// keeps FP64 arithmetic for the state updates only.
 #pragma once
 
 #include <cuda_runtime.h>
@@ -11,10 +17,11 @@
 namespace sph {
 
 constexpr int kBlock = 256;
-constexpr int kScanTile = 4096;  // cells per scan tile (256 threads x 16)
+constexpr int kScanTile = 4096;  // cells per scan tile (1024 threads x 4, one uint4 each)
 
 // ---------------------------------------------------------------------------
-// Order-preserving encoding of doubles for unsigned 64-bit atomicMin/Max.
+// Order-preserving encoding of doubles for unsigned 64-bit atomicMin/Max
+// (integer operations only).
 // ---------------------------------------------------------------------------
 __device__ __forceinline__ unsigned long long enc_d(double v) {
   unsigned long long u = (unsigned long long)__double_as_longlong(v);
@@ -27,25 +34,96 @@ __device__ __forceinline__ double dec_d(unsigned long long e) {
 constexpr unsigned long long kEncMinId = 0xffffffffffffffffull;  // identity of min
 constexpr unsigned long long kEncMaxId = 0ull;                   // identity of max
 
+// finite test on the bit pattern (no FP64 instruction)
+__device__ __forceinline__ bool finite_bits(double v) {
+  return ((unsigned long long)__double_as_longlong(v) & 0x7ff0000000000000ull) != 0x7ff0000000000000ull;
+}
+
 // ---------------------------------------------------------------------------
-// Workspace-resident control block: reductions, status, dt ring.
-// Every reduction slot is returned to its identity by the kernel that
-// consumes it, so no memset is needed between evaluations.
+// double <-> float on the integer pipe
+// ---------------------------------------------------------------------------
+// float -> double, exact
+__device__ __forceinline__ double f2d(float f) {
+  unsigned u = __float_as_uint(f);
+  unsigned s = u & 0x80000000u, e = (u >> 23) & 0xffu, m = u & 0x7fffffu;
+  unsigned long long r;
+  if (e == 0u) {
+    if (m != 0u) return (double)f;  // denormal (never in practice)
+    r = (unsigned long long)s << 32;
+  } else if (e == 0xffu) {
+    r = ((unsigned long long)(s | 0x7ff00000u | (m >> 3)) << 32) | ((unsigned long long)(m & 7u) << 29);
+  } else {
+    r = ((unsigned long long)(s | ((e + 896u) << 20) | (m >> 3)) << 32) | ((unsigned long long)(m & 7u) << 29);
+  }
+  return __longlong_as_double((long long)r);
+}
+
+// The rare out-of-float-range cases go through out-of-line FP64 conversions,
+// so that the compiler cannot if-convert them into every thread's path.
+static __device__ __noinline__ float d2f_slow(double d) { return __double2float_rn(d); }
+static __device__ __noinline__ float2 split_slow(double d) {
+  const float hi = __double2float_rn(d);
+  return make_float2(hi, __double2float_rn(d - (double)hi));
+}
+
+// double -> float by truncating the mantissa (relative error < 2^-23)
+__device__ __forceinline__ float d2f_trunc(double d) {
+  unsigned long long u = (unsigned long long)__double_as_longlong(d);
+  unsigned hi = (unsigned)(u >> 32), lo = (unsigned)u;
+  unsigned s = hi & 0x80000000u;
+  if ((u << 1) == 0ull) return __uint_as_float(s);
+  int e = (int)((hi >> 20) & 0x7ffu) - 896;
+  if (e <= 0 || e >= 255) return d2f_slow(d);  // out of float range, inf, nan: rare
+  return __uint_as_float(s | ((unsigned)e << 23) | ((hi & 0xfffffu) << 3) | (lo >> 29));
+}
+
+// double -> (hi, lo) floats with d = hi + lo to 2^-47 relative: hi is d's
+// mantissa truncated to 24 bits, lo the remaining 29 bits rounded to 24.
+__device__ __forceinline__ void split_df(double d, float &hi, float &lo) {
+  unsigned long long u = (unsigned long long)__double_as_longlong(d);
+  unsigned h32 = (unsigned)(u >> 32), l32 = (unsigned)u;
+  unsigned s = h32 & 0x80000000u;
+  if ((u << 1) == 0ull) {
+    hi = __uint_as_float(s);
+    lo = 0.f;
+    return;
+  }
+  int eb = (int)((h32 >> 20) & 0x7ffu);
+  int e = eb - 896;
+  if (e <= 0 || e >= 255) {
+    const float2 r = split_slow(d);
+    hi = r.x;
+    lo = r.y;
+    return;
+  }
+  hi = __uint_as_float(s | ((unsigned)e << 23) | ((h32 & 0xfffffu) << 3) | (l32 >> 29));
+  unsigned m = l32 & 0x1fffffffu;  // low 29 mantissa bits, weight 2^(eb - 1075)
+  int se = eb - 948;               // biased float exponent of 2^(eb - 1075)
+  float scale = se > 0 ? __uint_as_float((unsigned)se << 23) : 0.f;
+  lo = __uint_as_float(__float_as_uint(__uint2float_rn(m) * scale) | s);
+}
+
+// ---------------------------------------------------------------------------
+// Workspace-resident control block: reductions, status, dt ring.  Every
+// reduction slot is returned to its identity by the kernel that consumes it.
 // ---------------------------------------------------------------------------
 struct DevCtrl {
   // bounds of the next neighbour build (all active particles)
   unsigned long long xmin, xmax, ymin, ymax;
   unsigned long long hmin_all;  // h before the h reset (reference cell size)
   unsigned long long hmax_new;  // h after the h reset (search radius)
-  // TimeStep reductions over fluid
+  // TimeStep reductions over fluid: standalone TimeStep kernel ...
   unsigned long long ts_hmin, ts_cmax, ts_a2max;
   unsigned int ts_nfluid;
-  unsigned int done_pair;  // last-block counters
   unsigned int done_ts;
-  unsigned int status;     // sticky SPH_STATUS_* bits
+  // ... and the one fused into the step (h from the records pass, a^2 from the pair pass)
+  unsigned long long pd_hmin, pd_a2max;
+  unsigned int pd_nfluid;
+  unsigned int done_pair;
+  unsigned int status;  // sticky SPH_STATUS_* bits
   unsigned int alias_count;
   unsigned int initialised;
-  unsigned int pad[2];
+  unsigned int pad;
   double dt_ring[2][3];  // {dt, dt_c, dt_f} of the step with that parity
 };
 
@@ -54,29 +132,39 @@ struct DevGrid {
   // reference grid (src/Tools/NNLinkedList.py:86-127)
   double xmin, xmax, ymin, ymax, cs, inv_cs;
   long long ncx, ncy, ncells_ref;
+  float xminf, yminf, inv_csf, pad0;  // FP32 fast path of the reference binning
   // traversal grid
-  int mode;         // 0: the reference cells themselves, 1: own grid + reference-stencil filter
-  int ntx, nty;     // traversal cells per axis
-  int ncells;       // traversal cells in use (cell ncells is the dump cell)
-  double ox, oy;    // traversal origin (mode 1)
-  double ct, inv_ct;  // traversal cell size (mode 1)
+  int mode;    // 0: the reference cells with their 3x3 stencil; 1: own grid
+  int ntx, nty;  // traversal cells per axis
+  int ncells;  // traversal cells in use (cell ncells is the dump cell)
+  float oxf, oyf, inv_ctf;  // mode 1 binning (FP32, monotone)
+  int wt;           // stencil half-width of the pair kernels
   int need_filter;  // mode 1: candidates must pass the reference-stencil test
-  int wide;         // mode 1: stencil half-width (cells) covering q <= 3 at hmax
+  int wide;         // mode 1: half-width covering q <= 3 at hmax (export, aliased queries)
+  double ct;        // traversal cell size
   double hmax;      // max h after the h reset
-  double r_search;  // interaction radius the traversal covers
+  double r_search;  // interaction radius the pair kernels need
+  float pad_e;      // bound on |x_hi - x| + |x_j,hi - x_j| over the domain (prefilter padding)
   int valid;
-  int pad;
 };
 
 // Byte offsets of the workspace regions (computed on the host).
 struct WsLayout {
-  size_t ctrl, grid, keys, refcell, perm_tmp, keys_sorted, perm, meta, counts, cstart, scan_part, recA,
-      recB, recC, rho_sd, total;
+  size_t ctrl, grid, keys, refcell, perm_tmp, keys_sorted, perm, meta, counts, cstart, scan_part, rec0, rec1,
+      rec2, rec64a, rec64b, total;
   long long n_cap, max_cells, n_parts;
 };
 
 WsLayout make_layout(long long n_cap, long long max_cells);
 
+// Sorted pair records (slot k = k-th particle in cell order):
+//   rec0  float4 (x_hi, y_hi, h, m)  x_hi, y_hi: FP64 position with its mantissa
+//                                    truncated to 24 bits; h with the sign bit
+//                                    set for non-fluid particles
+//   rec1  float4 (x_lo, y_lo, rho, p / rho^2)    mixed form: x = x_hi + x_lo
+//   rec2  float4 (vx_hi, vy_hi, vx_lo, vy_lo)    mixed form
+//   rec64a double4 (x, y, vx, vy)                FP64 form
+//   rec64b double4 (m, rho, p / rho^2, h signed)
 struct WsPtrs {
   DevCtrl *ctrl;
   DevGrid *grid;
@@ -87,10 +175,10 @@ struct WsPtrs {
   int *perm;          // sorted slot -> particle index
   int2 *meta;         // raw reference cell of sorted slot k
   unsigned int *counts;  // per cell counters (zero between builds)
-  unsigned int *cstart;  // exclusive prefix of counts, cstart[ncells] = n
+  unsigned int *cstart;  // exclusive prefix of counts, cstart[ncells + 1] = n
   unsigned int *scan_part;
-  void *recA, *recB, *recC;  // sorted pair records
-  double *rho_sd;            // summation-density result (caller order)
+  float4 *rec0, *rec1, *rec2;
+  double4_32a *rec64a, *rec64b;
   long long n_cap, max_cells, n_parts;
 };
 
@@ -112,6 +200,51 @@ __device__ __forceinline__ long long ref_floor_div(double a, double o, double s,
   if (fr < 1e-9 || fr > 1.0 - 1e-9) f = floor(__ddiv_rn(d, s));
   return (long long)f;
 }
+static __device__ __noinline__ long long ref_floor_div_slow(double a, double o, double s, double inv_s) {
+  return ref_floor_div(a, o, s, inv_s);
+}
+
+// The same binning with an FP32 fast path: the FP32 estimate decides unless
+// it lands within 1e-3 cells of a cell edge (then the exact FP64 test does).
+__device__ __forceinline__ long long ref_cell(double a, double o, double s, double inv_s, float of, float inv_sf) {
+  float af = d2f_trunc(a);
+  float t = (af - of) * inv_sf;
+  float f = floorf(t);
+  float fr = t - f;
+  bool safe = fabsf(t) < 1e6f && (fabsf(af) + fabsf(of)) * inv_sf < 4000.f && fr > 1e-3f && fr < 1.0f - 1e-3f;
+  if (safe) return (long long)f;
+  return ref_floor_div_slow(a, o, s, inv_s);
+}
+
+// exact halving of a positive normal double on the integer pipe
+static __device__ __noinline__ double half_slow(double v) { return 0.5 * v; }
+__device__ __forceinline__ double half_exact(double v) {
+  const unsigned long long u = (unsigned long long)__double_as_longlong(v);
+  const unsigned e = (unsigned)(u >> 52) & 0x7ffu;
+  if (e > 1u && e < 0x7ffu) return __longlong_as_double((long long)(u - (1ull << 52)));
+  return half_slow(v);
+}
+
+// v < 0.0 on the bit pattern: sign set, not -0.0, not NaN
+__device__ __forceinline__ bool negative_bits(double v) {
+  const unsigned long long u = (unsigned long long)__double_as_longlong(v);
+  const unsigned long long mag = u & 0x7fffffffffffffffull;
+  return (u >> 63) != 0ull && mag != 0ull && mag <= 0x7ff0000000000000ull;
+}
+
+// 64-bit min / max over a warp with two 32-bit REDUX steps
+__device__ __forceinline__ unsigned long long warp_min_u64(unsigned long long v) {
+  const unsigned hi = (unsigned)(v >> 32), lo = (unsigned)v;
+  const unsigned mh = __reduce_min_sync(0xffffffffu, hi);
+  const unsigned ml = __reduce_min_sync(0xffffffffu, hi == mh ? lo : 0xffffffffu);
+  return ((unsigned long long)mh << 32) | ml;
+}
+__device__ __forceinline__ unsigned long long warp_max_u64(unsigned long long v) {
+  const unsigned hi = (unsigned)(v >> 32), lo = (unsigned)v;
+  const unsigned mh = __reduce_max_sync(0xffffffffu, hi);
+  const unsigned ml = __reduce_max_sync(0xffffffffu, hi == mh ? lo : 0u);
+  return ((unsigned long long)mh << 32) | ml;
+}
 
 // 32-bit signed saturation for cell coordinates
 __device__ __forceinline__ int sat_i32(long long v) {
@@ -131,11 +264,11 @@ __device__ __forceinline__ void storage_cell(int cx, int cy, long long ncx, int 
 }
 
 // Tait EOS of one particle (TaitEOS.py:6-31) plus the background pressure
-// (WCSPH.py:131-149).  gamma == 7 uses repeated products.
-__device__ __forceinline__ double tait_p(double rho, int8_t label, double gamma, double B, double rho0,
+// (WCSPH.py:131-149), FP64.  gamma == 7 uses repeated products.
+__device__ __forceinline__ double tait_p(double rho, int8_t label, double gamma, double B, double inv_rho0,
                                          double Pb) {
   if (!is_fluid(label)) return 0.0 + Pb;
-  double r = rho / rho0;
+  double r = rho * inv_rho0;
   double ratio;
   if (gamma == 7.0) {
     double r2 = r * r;
@@ -145,6 +278,14 @@ __device__ __forceinline__ double tait_p(double rho, int8_t label, double gamma,
     ratio = pow(r, gamma);
   }
   return (ratio - 1.0) * B + Pb;
+}
+
+// (1 + d)^gamma - 1 in FP32 for the relative density d = rho / rho0 - 1
+// (exact binomial expansion for gamma == 7; keeps full relative accuracy as
+// d -> 0, where the FP64 form cancels)
+__device__ __forceinline__ float tait_ratio_m1_f(float d, float gamma) {
+  if (gamma == 7.0f) return d * (7.f + d * (21.f + d * (35.f + d * (35.f + d * (21.f + d * (7.f + d))))));
+  return expm1f(gamma * log1pf(d));
 }
 
 // computeH (SolverTools.py:106-118)
@@ -211,7 +352,7 @@ __device__ __forceinline__ double gauss_gcoef(double r, double h) {
 }
 
 // ---------------------------------------------------------------------------
-// Block reductions (256 threads)
+// Block reductions
 // ---------------------------------------------------------------------------
 template <typename T, typename Op>
 __device__ __forceinline__ T warp_reduce(T v, Op op) {
@@ -275,17 +416,20 @@ inline StepArgs step_args(const sph_particles_t *pa) {
   return a;
 }
 
-// Neighbour build: bounds (+ optional fused integrator predict), grid,
-// keys, counting sort, sorted pair records.
-enum BoundsMode { kBoundsOnly = 0, kBoundsPredictPEC = 1, kBoundsReset = 2 };
-void launch_bounds(const StepArgs &a, const WsPtrs &w, const sph_config_t &cfg, int mode, const double *dt,
-                   double dt_fixed, cudaStream_t st);
+// Neighbour build: bounds of the positions the next evaluation sees, with
+// the integrator work that precedes it fused in front: none, the predictor
+// of the first step, or the previous step's corrector followed by this
+// step's predictor.  h_reset: take hmax over the h the evaluation will set.
+enum IntStage { kStageNone = 0, kStagePredict = 1, kStageCorrectPredict = 2 };
+void launch_bounds(const StepArgs &a, const WsPtrs &w, const sph_config_t &cfg, int stage, bool h_reset,
+                   const double *dt_prev, const double *dt_cur, cudaStream_t st);
 void launch_build(const StepArgs &a, const WsPtrs &w, const sph_config_t &cfg, const sph_wcsph_t &wc,
                   cudaStream_t st);
-// gather the sorted pair records (EOS, h reset); rho_override replaces rho
-// (summation density) when not null
+// Sorted pair records (h reset + Tait EOS fused).  write_state: write p, c
+// and the fluid h back; p_from_state: take p from the caller's array (second
+// records pass of summation density); reduce_h: feed the step's TimeStep.
 void launch_records(const StepArgs &a, const WsPtrs &w, const sph_config_t &cfg, const sph_wcsph_t &wc,
-                    bool write_state, const double *rho_override, cudaStream_t st);
+                    bool write_state, bool p_from_state, bool reduce_h, cudaStream_t st);
 // fused pair interaction; dt_out (ring slot) receives the next TimeStep
 void launch_pair(const StepArgs &a, const WsPtrs &w, const sph_config_t &cfg, const sph_wcsph_t &wc,
                  double *dt_out, double *dt_hist, cudaStream_t st);
