@@ -315,11 +315,13 @@ __global__ void __launch_bounds__(kBlock) k_keys(const double *__restrict__ x, c
       key = (int)flat;
     } else {
       // FP32 binning, monotone in the position (query and candidates agree)
-      int tx = (int)floorf((d2f_trunc(xi) - g.oxf) * g.inv_ctf);
-      int ty = (int)floorf((d2f_trunc(yi) - g.oyf) * g.inv_ctf);
-      tx = tx < 0 ? 0 : (tx >= g.ntx ? g.ntx - 1 : tx);
-      ty = ty < 0 ? 0 : (ty >= g.nty ? g.nty - 1 : ty);
-      key = tx + g.ntx * ty;
+      float ft;
+      const float tx = fminf(fmaxf((d2f_trunc(xi) - g.oxf) * g.inv_ctf, 0.f), (float)(g.ntx - 1));
+      const float ty = fminf(fmaxf((d2f_trunc(yi) - g.oyf) * g.inv_ctf, 0.f), (float)(g.nty - 1));
+      if (g.ntx < (1 << 22) && g.nty < (1 << 22))
+        key = floor_small(tx, ft) + g.ntx * floor_small(ty, ft);
+      else
+        key = min(max((int)floorf(tx), 0), g.ntx - 1) + g.ntx * min(max((int)floorf(ty), 0), g.nty - 1);
     }
     keys[i] = key;
     atomicAdd(&counts[key], 1u);

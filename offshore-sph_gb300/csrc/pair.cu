@@ -29,6 +29,13 @@ namespace sph {
 
 constexpr int kPairBlock = 128;
 constexpr int kListCap = 32;
+#ifndef SPH_PAIR_MIXED_BLOCKS
+#define SPH_PAIR_MIXED_BLOCKS 8
+#endif
+#ifndef SPH_PHASE1_UNROLL
+#define SPH_PHASE1_UNROLL 1
+#endif
+constexpr int kPhase1Unroll = SPH_PHASE1_UNROLL;
 
 struct PairParams {
   double alpha, beta, co, eps, r0, D, p1, p2;
@@ -165,9 +172,16 @@ struct PairPtrs {
   DevCtrl *ctrl;
 };
 
+// resident blocks per SM the register allocation targets: the mixed form is
+// latency-bound and wants occupancy; the FP64 form is FP64-issue-bound
+template <bool MIXED>
+struct PairOcc {
+  static constexpr int blocks = MIXED ? SPH_PAIR_MIXED_BLOCKS : 4;
+};
+
 template <int KERNEL, bool XSPH, bool SUMDENS, bool MIXED>
-__global__ void __launch_bounds__(kPairBlock) k_pair(StepArgs a, PairPtrs P, PairParams pp, double *dt_out,
-                                                     double *dt_hist) {
+__global__ void __launch_bounds__(kPairBlock, PairOcc<MIXED>::blocks)
+    k_pair(StepArgs a, PairPtrs P, PairParams pp, double *dt_out, double *dt_hist) {
   __shared__ unsigned int lists[kListCap][kPairBlock];
   const DevGrid g = *P.grid;
   const bool filter = g.mode == 1 && (g.need_filter || P.ctrl->alias_count > 0);
@@ -337,6 +351,7 @@ __global__ void __launch_bounds__(kPairBlock) k_pair(StepArgs a, PairPtrs P, Pai
       for (int b = -W; b <= W; b++) {
         unsigned int s, e;
         if (!sten.row(b, P.cstart, s, e)) continue;
+#pragma unroll kPhase1Unroll
         for (unsigned int j = s; j < e; j++) {
           if (j == (unsigned int)k) continue;  // the particle itself contributes zero
           if (filter && !in_ref_stencil(P.meta, j, g, qref)) continue;

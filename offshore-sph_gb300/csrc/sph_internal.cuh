@@ -97,10 +97,24 @@ __device__ __forceinline__ void split_df(double d, float &hi, float &lo) {
     return;
   }
   hi = __uint_as_float(s | ((unsigned)e << 23) | ((h32 & 0xfffffu) << 3) | (l32 >> 29));
-  unsigned m = l32 & 0x1fffffffu;  // low 29 mantissa bits, weight 2^(eb - 1075)
-  int se = eb - 948;               // biased float exponent of 2^(eb - 1075)
-  float scale = se > 0 ? __uint_as_float((unsigned)se << 23) : 0.f;
-  lo = __uint_as_float(__float_as_uint(__uint2float_rn(m) * scale) | s);
+  // low 29 mantissa bits m, weight 2^(eb - 1075), converted without the
+  // conversion unit: 2^23 + k is exact in FP32 for k < 2^23, so m = mh 2^23 + ml
+  // becomes two exact subtractions and one correctly rounded FMA
+  const unsigned m = l32 & 0x1fffffffu;
+  const float fl = __uint_as_float(0x4B000000u | (m & 0x7fffffu)) - 8388608.0f;
+  const float fh = __uint_as_float(0x4B000000u | (m >> 23)) - 8388608.0f;
+  const float mf = fmaf(fh, 8388608.0f, fl);
+  const int se = eb - 948;  // biased float exponent of 2^(eb - 1075)
+  const float scale = se > 0 ? __uint_as_float((unsigned)se << 23) : 0.f;
+  lo = __uint_as_float(__float_as_uint(mf * scale) | s);
+}
+
+// floor(t) for 0 <= t < 2^23 as an int and as a float, on the FMA pipe:
+// t + 2^23 rounded down is 2^23 + floor(t)
+__device__ __forceinline__ int floor_small(float t, float &ft) {
+  const float b = __fadd_rd(t, 8388608.0f);
+  ft = b - 8388608.0f;
+  return (int)(__float_as_uint(b) - 0x4B000000u);
 }
 
 // ---------------------------------------------------------------------------
@@ -207,12 +221,13 @@ static __device__ __noinline__ long long ref_floor_div_slow(double a, double o, 
 // The same binning with an FP32 fast path: the FP32 estimate decides unless
 // it lands within 1e-3 cells of a cell edge (then the exact FP64 test does).
 __device__ __forceinline__ long long ref_cell(double a, double o, double s, double inv_s, float of, float inv_sf) {
-  float af = d2f_trunc(a);
-  float t = (af - of) * inv_sf;
-  float f = floorf(t);
-  float fr = t - f;
-  bool safe = fabsf(t) < 1e6f && (fabsf(af) + fabsf(of)) * inv_sf < 4000.f && fr > 1e-3f && fr < 1.0f - 1e-3f;
-  if (safe) return (long long)f;
+  const float af = d2f_trunc(a);
+  const float t = (af - of) * inv_sf;
+  const bool range = t >= 0.f && t < 1e6f && (fabsf(af) + fabsf(of)) * inv_sf < 4000.f;
+  float f;
+  const int c = floor_small(range ? t : 0.f, f);
+  const float fr = t - f;
+  if (range && fr > 1e-3f && fr < 1.0f - 1e-3f) return c;
   return ref_floor_div_slow(a, o, s, inv_s);
 }
 
