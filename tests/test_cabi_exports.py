@@ -1,0 +1,66 @@
+"""The C ABI library loads and exports every function include/*.h declares.
+Host-only calls (no GPU needed): version, workspace sizing, status strings,
+argument validation."""
+import ctypes as C
+import glob
+import os
+import re
+
+import pytest
+
+REPO = os.path.dirname(os.path.dirname(os.path.abspath(__file__)))
+
+
+def declared_functions():
+    names = set()
+    for h in glob.glob(os.path.join(REPO, "include", "*.h")):
+        text = open(h).read()
+        text = re.sub(r"/\*.*?\*/", "", text, flags=re.S)
+        for m in re.finditer(r"^\s*(?:const\s+)?(?:int|int64_t|void|char|size_t)\s*\*?\s*(sph_\w+)\s*\(", text,
+                             re.M):
+            names.add(m.group(1))
+    return sorted(names)
+
+
+@pytest.fixture(scope="module")
+def lib():
+    from sph import _lib, build
+    build.build()
+    return _lib.load()
+
+
+def test_header_declares_functions():
+    names = declared_functions()
+    assert "sph_compute" in names and "sph_run" in names and len(names) >= 15
+
+
+def test_every_declared_function_is_exported(lib):
+    from sph import _lib
+    missing = [n for n in declared_functions() if not hasattr(lib, n)]
+    assert not missing, missing
+    assert set(declared_functions()) == set(_lib.EXPORTS)
+
+
+def test_host_only_calls(lib):
+    assert lib.sph_abi_version() == 1
+    nbytes = C.c_size_t()
+    assert lib.sph_workspace_size(1000, 0, C.byref(nbytes)) == 0
+    assert nbytes.value > 1000 * 100
+    assert lib.sph_workspace_size(-1, 0, C.byref(nbytes)) != 0
+    assert lib.sph_default_max_cells(10) == 65536
+    assert lib.sph_status_string(0) == b"ok"
+    assert b"workspace" in lib.sph_status_string(2)
+
+
+def test_invalid_arguments_rejected_on_host(lib):
+    from sph import _lib, core
+    wc = core.wcsph_struct(1.0, 0.01, 1000.0)
+    cfg = core.config_struct()
+    bad = core.config_struct()
+    bad.kernel = 7
+    pa = _lib.Particles()
+    pa.n = 10  # null arrays
+    ws = _lib.Workspace()
+    assert lib.sph_compute(C.byref(pa), C.byref(wc), C.byref(cfg), C.byref(ws), None) == 1  # invalid argument
+    assert lib.sph_run(None, C.byref(wc), C.byref(cfg), C.byref(ws), 1, None, None) != 0
+    assert lib.sph_compute(C.byref(pa), C.byref(wc), C.byref(bad), C.byref(ws), None) == 1
