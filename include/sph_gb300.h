@@ -61,7 +61,8 @@ enum {
   SPH_ERR_INVALID_ARGUMENT = 1,
   SPH_ERR_WORKSPACE_TOO_SMALL = 2,
   SPH_ERR_CUDA = 3,
-  SPH_ERR_NOT_INITIALISED = 4
+  SPH_ERR_NOT_INITIALISED = 4,
+  SPH_ERR_STATIC_LIMIT = 5 /* more particles than sph_compute_static's scratch holds */
 };
 
 /* device status bits (sticky, see sph_get_status) */
@@ -198,6 +199,30 @@ int sph_nn_export(const sph_particles_t *pa, const sph_config_t *cfg, const sph_
  * workspace the reductions the next sph_timestep would compute. */
 int sph_compute(sph_particles_t *pa, const sph_wcsph_t *w, const sph_config_t *cfg, const sph_workspace_t *ws,
                 sph_stream_t stream);
+
+/* sph_compute without a caller workspace: the same evaluation, with the
+ * scratch in a device array that the library owns.  It has no counterpart in
+ * the reference; it is for callers that cannot allocate device memory
+ * themselves (an application whose GPU memory belongs to another allocator or
+ * a fixed budget, a foreign-function binding without a CUDA allocator).  The
+ * caller still passes the particle arrays.
+ *  - Limit: at most SPH_STATIC_MAX_PARTICLES particles (SPH_ERR_STATIC_LIMIT
+ *    otherwise); the search grid is capped at SPH_STATIC_MAX_CELLS cells and
+ *    is coarsened beyond that (results unchanged, search slower).
+ *  - Every GPU that loads the library holds the SPH_STATIC_WS_BYTES array
+ *    until the process exits.  The call itself allocates nothing.
+ *  - The first call on a device looks up the array's device address (once per
+ *    device); make that first call before any stream capture.
+ *  - All calls share the one array: calls whose work overlaps on the GPU (on
+ *    different streams, or from different host threads without ordering) race
+ *    on it.  Order them on one stream.
+ *  - status: optional DEVICE pointer that receives the SPH_STATUS_* bits of
+ *    this call (asynchronously, on the stream). */
+#define SPH_STATIC_MAX_PARTICLES 32768
+#define SPH_STATIC_MAX_CELLS 131072
+#define SPH_STATIC_WS_BYTES 6291456
+int sph_compute_static(sph_particles_t *pa, const sph_wcsph_t *w, const sph_config_t *cfg, uint32_t *status,
+                       sph_stream_t stream);
 
 /* TimeStep.compute over the fluid particles (src/Equations/TimeStep.py:7-91,
  * gamma_c = cfg->cfl_c, gamma_f = cfg->cfl_f): dt3[0..2] = {dt, dt_courant,

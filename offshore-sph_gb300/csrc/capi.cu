@@ -166,6 +166,7 @@ const char *sph_status_string(int code) {
     case SPH_ERR_WORKSPACE_TOO_SMALL: return "workspace too small";
     case SPH_ERR_CUDA: return "CUDA error";
     case SPH_ERR_NOT_INITIALISED: return "workspace not initialised";
+    case SPH_ERR_STATIC_LIMIT: return "more particles than the static scratch of sph_compute_static holds";
     default: break;
   }
   switch ((unsigned)code) {

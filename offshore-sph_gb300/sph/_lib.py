@@ -55,7 +55,10 @@ class Workspace(C.Structure):
 EXPORTS = ("sph_abi_version", "sph_workspace_size", "sph_default_max_cells", "sph_workspace_init",
            "sph_get_status", "sph_status_string", "sph_initialize", "sph_eos", "sph_nn_update",
            "sph_nn_count", "sph_nn_export", "sph_compute", "sph_timestep", "sph_predict", "sph_correct",
-           "sph_run", "sph_kernel_eval", "sph_kernel_grad", "sph_gauss_deriv", "sph_run_profiled")
+           "sph_run", "sph_kernel_eval", "sph_kernel_grad", "sph_gauss_deriv", "sph_run_profiled",
+           "sph_compute_static")
+SPH_ERR_STATIC_LIMIT = 5
+STATIC_MAX_PARTICLES = 32768
 
 STAGES = ("timestep", "predict", "build", "records", "pair", "correct")
 
@@ -97,6 +100,7 @@ def load():
         "sph_kernel_grad": (C.c_int, [C.c_int, C.c_int64, vp, vp, vp, vp, vp]),
         "sph_gauss_deriv": (C.c_int, [C.c_int64, vp, vp, vp, vp]),
         "sph_run_profiled": (C.c_int, [PP, WP, CP, WS, C.c_int64, C.POINTER(C.c_double), vp]),
+        "sph_compute_static": (C.c_int, [PP, WP, CP, vp, vp]),
     }
     for name, (res, args) in sig.items():
         f = getattr(L, name)
