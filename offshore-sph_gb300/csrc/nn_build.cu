@@ -244,12 +244,26 @@ __global__ void k_grid(DevCtrl *ctrl, DevGrid *g, GridParams gp) {
   // the cubic spline and its gradient vanish at q = 2, so pairs at exactly the
   // support radius contribute nothing; the Gaussian is cut at q <= 3 inclusive
   const bool trunc_free = cubic ? (cs >= R) : (cs >= R * (1.0 + 1e-9));
-  const bool fitsA = !huge && (double)ncx * (double)ncy <= (double)gp.max_cells;
+  // the largest tile shift (up to ts_max) whose padded cell count fits
+  auto tile_fit = [&](double nx, double ny, int ts_max, int &ts_out) {
+    for (int ts = ts_max; ts >= 0; ts--) {
+      const double T = (double)(1 << ts);
+      if (ceil(nx / T) * ceil(ny / T) * T * T <= (double)gp.max_cells) {
+        ts_out = ts;
+        return true;
+      }
+    }
+    return false;
+  };
+  int tsA = 0;
+  const bool fitsA = !huge && tile_fit((double)ncx, (double)ncy, SPH_TILE_SHIFT_REF, tsA);
   if (!trunc_free && fitsA) {
     g->mode = 0;
     g->ntx = (int)ncx;
     g->nty = (int)ncy;
-    g->ncells = (int)(ncx * ncy);
+    g->ts = tsA;
+    g->ntlx = (int)((ncx + (1 << tsA) - 1) >> tsA);
+    g->ncells = g->ntlx * (int)((ncy + (1 << tsA) - 1) >> tsA) << (2 * tsA);
     g->ct = cs;
     g->oxf = (float)xmin; g->oyf = (float)ymin; g->inv_ctf = (float)cs1;
     g->wt = 1;
@@ -262,10 +276,11 @@ __global__ void k_grid(DevCtrl *ctrl, DevGrid *g, GridParams gp) {
     for (int it = 0; it < 2; it++) ct = 0.5 * R * (1.0 + 4.0 * (3e-7 * amax / ct) + 1e-5);
     double fnx = 1.0, fny = 1.0;
     bool fits = false;
+    int ts = 0;
     for (int it = 0; it < 64 && !fits; it++) {
       fnx = floor((xmax - xmin) / ct) + 1.0;
       fny = floor((ymax - ymin) / ct) + 1.0;
-      fits = fnx * fny <= (double)gp.max_cells;
+      fits = tile_fit(fnx, fny, SPH_TILE_SHIFT_OWN, ts);
       if (!fits) {
         status |= SPH_STATUS_GRID_COARSENED;
         ct *= sqrt(fnx * fny / (double)gp.max_cells) * 1.05 + 1e-3;
@@ -274,11 +289,14 @@ __global__ void k_grid(DevCtrl *ctrl, DevGrid *g, GridParams gp) {
     if (!fits) {  // one cell holding everything: exact, only slower
       ct = fmax(xmax - xmin, ymax - ymin) * 2.0 + R;
       fnx = fny = 1.0;
+      ts = 0;
     }
     g->mode = 1;
     g->ntx = (int)fnx;
     g->nty = (int)fny;
-    g->ncells = (int)(fnx * fny);
+    g->ts = ts;
+    g->ntlx = (g->ntx + (1 << ts) - 1) >> ts;
+    g->ncells = g->ntlx * ((g->nty + (1 << ts) - 1) >> ts) << (2 * ts);
     g->ct = ct;
     g->oxf = (float)xmin; g->oyf = (float)ymin; g->inv_ctf = (float)(1.0 / ct);
     g->wt = 2;
@@ -312,16 +330,19 @@ __global__ void __launch_bounds__(kBlock) k_keys(const double *__restrict__ x, c
     if (overflow) {
       key = g.ncells;  // dump cell: never part of a stencil
     } else if (g.mode == 0) {
-      key = (int)flat;
+      int sx, sy;
+      storage_cell((int)cx, (int)cy, g.ncx, sx, sy);
+      key = tiled_key(sx, sy, g.ts, g.ntlx);
     } else {
       // FP32 binning, monotone in the position (query and candidates agree)
       float ft;
       const float tx = fminf(fmaxf((d2f_trunc(xi) - g.oxf) * g.inv_ctf, 0.f), (float)(g.ntx - 1));
       const float ty = fminf(fmaxf((d2f_trunc(yi) - g.oyf) * g.inv_ctf, 0.f), (float)(g.nty - 1));
       if (g.ntx < (1 << 22) && g.nty < (1 << 22))
-        key = floor_small(tx, ft) + g.ntx * floor_small(ty, ft);
+        key = tiled_key(floor_small(tx, ft), floor_small(ty, ft), g.ts, g.ntlx);
       else
-        key = min(max((int)floorf(tx), 0), g.ntx - 1) + g.ntx * min(max((int)floorf(ty), 0), g.nty - 1);
+        key = tiled_key(min(max((int)floorf(tx), 0), g.ntx - 1), min(max((int)floorf(ty), 0), g.nty - 1), g.ts,
+                        g.ntlx);
     }
     keys[i] = key;
     atomicAdd(&counts[key], 1u);

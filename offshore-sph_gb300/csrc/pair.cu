@@ -28,14 +28,17 @@
 namespace sph {
 
 constexpr int kPairBlock = 128;
-constexpr int kListCap = 32;
+// per-thread neighbour-list capacity: above the typical number of pairs inside
+// the support (about 21 for the cubic spline at h = 1.3 dx, 43 for the
+// Gaussian cut at 3h), so that the mid-walk flush -- which runs divergently --
+// stays rare
+template <int KERNEL>
+struct ListCap {
+  static constexpr int value = KERNEL == SPH_KERNEL_CUBIC ? 32 : 64;
+};
 #ifndef SPH_PAIR_MIXED_BLOCKS
 #define SPH_PAIR_MIXED_BLOCKS 8
 #endif
-#ifndef SPH_PHASE1_UNROLL
-#define SPH_PHASE1_UNROLL 1
-#endif
-constexpr int kPhase1Unroll = SPH_PHASE1_UNROLL;
 
 struct PairParams {
   double alpha, beta, co, eps, r0, D, p1, p2;
@@ -45,38 +48,84 @@ struct PairParams {
   long long n;
 };
 
-// Stencil rows of one query: each row of cells is one contiguous range of
-// sorted slots.  Mode 0: the reference's 3x3 cells around the query's raw
-// cell (validity as NNLinkedList._get_valid_cell_index); mode 1: the own grid.
+// Stencil of one query.  Mode 0: the reference's 3x3 cells around the
+// query's raw cell (validity as NNLinkedList._get_valid_cell_index); mode 1:
+// the own grid.  Cell ids are tiled (tiled_key), so the cells of one stencil
+// row are one contiguous range of sorted slots per tile they touch.  The key
+// of (x, y) splits into a row part and a column part; the column parts of the
+// segment bounds are the same for every row and are computed once.
 struct Stencil {
-  int cx, cy, W, nx, ny;
-  bool ok;
-  __device__ __forceinline__ Stencil(const DevGrid &g, int2 qref, int qkey, int W_) {
-    W = W_;
-    nx = g.ntx;
-    ny = g.nty;
-    ok = true;
+  int y0, y1;          // rows, clipped (empty when y0 > y1)
+  int x0, x1;          // columns, clipped
+  int ca, cb, cc, cd;  // column parts: first segment [ca, cb), second [cc, cd)
+  int ts, ntlx;
+  bool multi;          // columns span more than two tiles
+  __device__ __forceinline__ static int colpart(int x, int ts) {
+    return ((x >> ts) << (2 * ts)) + (x & ((1 << ts) - 1));
+  }
+  __device__ __forceinline__ int rowpart(int y) const {
+    return (((y >> ts) * ntlx) << (2 * ts)) + ((y & ((1 << ts) - 1)) << ts);
+  }
+  __device__ __forceinline__ Stencil(const DevGrid &g, int2 qref, int qkey, int W) {
+    ts = g.ts;
+    ntlx = g.ntlx;
+    int cx, cy;
+    bool ok = true;
     if (g.mode == 0) {
       cx = qref.x;
       cy = qref.y;
     } else {
       ok = qkey < g.ncells;
-      cx = qkey % g.ntx;
-      cy = qkey / g.ntx;
+      tiled_cell(qkey, ts, ntlx, cx, cy);
+    }
+    x0 = max(cx - W, 0);
+    x1 = min(cx + W, g.ntx - 1);
+    y0 = max(cy - W, 0);
+    y1 = min(cy + W, g.nty - 1);
+    if (!ok || x0 > x1) y1 = y0 - 1;
+    multi = (x1 >> ts) - (x0 >> ts) > 1;
+    const int xs = ((x0 >> ts) + 1) << ts;  // first column of the next tile
+    ca = colpart(x0, ts);
+    if (xs <= x1) {
+      cb = colpart(xs - 1, ts) + 1;
+      cc = colpart(xs, ts);
+      cd = colpart(x1, ts) + 1;
+    } else {
+      cb = colpart(x1, ts) + 1;
+      cc = cd = cb;
     }
   }
-  // range of row offset b; false when the row is outside the grid or empty
-  __device__ __forceinline__ bool row(int b, const unsigned int *__restrict__ cstart, unsigned int &s,
-                                      unsigned int &e) const {
-    const int yy = cy + b;
-    if (!ok || yy < 0 || yy >= ny) return false;
-    const int x0 = max(cx - W, 0), x1 = min(cx + W, nx - 1);
-    if (x0 > x1) return false;
-    s = __ldg(&cstart[x0 + nx * yy]);
-    e = __ldg(&cstart[x1 + nx * yy + 1]);
-    return s < e;
-  }
 };
+
+// visit(j) for every slot j of the stencil.  Each row is one loop over its
+// (at most two) segments, with the four bounds loaded up front, so that the
+// threads of a warp -- whose split points differ -- stay converged.  Columns
+// spanning more than two tiles (tiles narrower than the stencil) walk the
+// tiles one by one.
+template <class F>
+__device__ __forceinline__ void for_stencil(const Stencil &sten, const unsigned int *__restrict__ cstart,
+                                            F &&visit) {
+  if (!sten.multi) {
+    for (int yy = sten.y0; yy <= sten.y1; yy++) {
+      const unsigned int *c = cstart + sten.rowpart(yy);
+      const unsigned int s0 = __ldg(c + sten.ca), e0 = __ldg(c + sten.cb);
+      const unsigned int s1 = __ldg(c + sten.cc), e1 = __ldg(c + sten.cd);
+      // slots [s0, e0) then [s1, e1) as one uniform index range
+      const unsigned int jump = s1 - e0, jend = e0 + (e1 - s1);
+      for (unsigned int j = s0; j < jend; j++) visit(j >= e0 ? j + jump : j);
+    }
+  } else {
+    const int m = (1 << sten.ts) - 1;
+    for (int yy = sten.y0; yy <= sten.y1; yy++) {
+      const unsigned int *c = cstart + sten.rowpart(yy);
+      for (int xs = sten.x0; xs <= sten.x1; xs = (xs | m) + 1) {
+        const int xe = min(sten.x1, xs | m);
+        const unsigned int e = __ldg(c + Stencil::colpart(xe, sten.ts) + 1);
+        for (unsigned int j = __ldg(c + Stencil::colpart(xs, sten.ts)); j < e; j++) visit(j);
+      }
+    }
+  }
+}
 
 __device__ __forceinline__ bool in_ref_stencil(const int2 *__restrict__ meta, unsigned int j, const DevGrid &g,
                                                int2 qref) {
@@ -94,18 +143,14 @@ __device__ int exact_count(const StepArgs &a, const int *__restrict__ perm, cons
                            double xi, double yi, double hi) {
   const Stencil sten(g, qref, qkey, W);
   int cnt = 0;
-  for (int b = -W; b <= W; b++) {
-    unsigned int s, e;
-    if (!sten.row(b, cstart, s, e)) continue;
-    for (unsigned int j = s; j < e; j++) {
-      if (filter && !in_ref_stencil(meta, j, g, qref)) continue;
-      const int pj = perm[j];
-      const double dx = xi - a.x[pj], dy = yi - a.y[pj];
-      const double r = __dsqrt_rn(__dadd_rn(__dmul_rn(dx, dx), __dmul_rn(dy, dy)));
-      const double q = __ddiv_rn(r, __dmul_rn(0.5, __dadd_rn(hi, a.h[pj])));
-      if (q <= 3.0) cnt++;
-    }
-  }
+  for_stencil(sten, cstart, [&](unsigned int j) {
+    if (filter && !in_ref_stencil(meta, j, g, qref)) return;
+    const int pj = perm[j];
+    const double dx = xi - a.x[pj], dy = yi - a.y[pj];
+    const double r = __dsqrt_rn(__dadd_rn(__dmul_rn(dx, dx), __dmul_rn(dy, dy)));
+    const double q = __ddiv_rn(r, __dmul_rn(0.5, __dadd_rn(hi, a.h[pj])));
+    if (q <= 3.0) cnt++;
+  });
   return cnt;
 }
 
@@ -182,6 +227,7 @@ struct PairOcc {
 template <int KERNEL, bool XSPH, bool SUMDENS, bool MIXED>
 __global__ void __launch_bounds__(kPairBlock, PairOcc<MIXED>::blocks)
     k_pair(StepArgs a, PairPtrs P, PairParams pp, double *dt_out, double *dt_hist) {
+  constexpr int kListCap = ListCap<KERNEL>::value;
   __shared__ unsigned int lists[kListCap][kPairBlock];
   const DevGrid g = *P.grid;
   const bool filter = g.mode == 1 && (g.need_filter || P.ctrl->alias_count > 0);
@@ -348,29 +394,24 @@ __global__ void __launch_bounds__(kPairBlock, PairOcc<MIXED>::blocks)
       // ---- phase 1: padded FP32 radius test, append to this thread's list
       const Stencil sten(g, qref, qkey, W);
       int nl = 0;
-      for (int b = -W; b <= W; b++) {
-        unsigned int s, e;
-        if (!sten.row(b, P.cstart, s, e)) continue;
-#pragma unroll kPhase1Unroll
-        for (unsigned int j = s; j < e; j++) {
-          if (j == (unsigned int)k) continue;  // the particle itself contributes zero
-          if (filter && !in_ref_stencil(P.meta, j, g, qref)) continue;
-          const float4 qj = P.rec0[j];
-          const float dx = Qi.x - qj.x, dy = Qi.y - qj.y;
-          const float d2 = dx * dx + dy * dy;
-          const float hij = 0.5f * (hif + fabsf(qj.z));
-          float reach = SK * hij;
-          if (signbit(qj.z)) reach = fmaxf(reach, fminf(r0f, 3.0f * hij) * 1.000002f);
-          const float rp = reach + pad;
-          if (d2 <= rp * rp) {
-            lists[nl][tid] = j;
-            if (++nl == kListCap) {
-              physics(nl);
-              nl = 0;
-            }
+      for_stencil(sten, P.cstart, [&](unsigned int j) {
+        if (j == (unsigned int)k) return;  // the particle itself contributes zero
+        if (filter && !in_ref_stencil(P.meta, j, g, qref)) return;
+        const float4 qj = P.rec0[j];
+        const float dx = Qi.x - qj.x, dy = Qi.y - qj.y;
+        const float d2 = dx * dx + dy * dy;
+        const float hij = 0.5f * (hif + fabsf(qj.z));
+        float reach = SK * hij;
+        if (signbit(qj.z)) reach = fmaxf(reach, fminf(r0f, 3.0f * hij) * 1.000002f);
+        const float rp = reach + pad;
+        if (d2 <= rp * rp) {
+          lists[nl][tid] = j;
+          if (++nl == kListCap) {
+            physics(nl);
+            nl = 0;
           }
         }
-      }
+      });
       physics(nl);
 
       // the reference's set always holds the particle itself, except for the
@@ -448,20 +489,17 @@ __global__ void __launch_bounds__(kPairBlock) k_sumdens(StepArgs a, PairPtrs P, 
   double rho = 0.0;
   float rhof = 0.f;
   const Stencil sten(g, qref, qkey, W);
-  for (int b = -W; b <= W; b++) {
-    unsigned int s, e;
-    if (!sten.row(b, P.cstart, s, e)) continue;
-    for (unsigned int j = s; j < e; j++) {
-      if (filter && !in_ref_stencil(P.meta, j, g, qref)) continue;
+  for_stencil(sten, P.cstart, [&](unsigned int j) {
+      if (filter && !in_ref_stencil(P.meta, j, g, qref)) return;
       const float4 qj = P.rec0[j];
-      if (signbit(qj.z)) continue;  // SummationDensity.py: fluid neighbours only
+      if (signbit(qj.z)) return;  // SummationDensity.py: fluid neighbours only
       const float hij = 0.5f * (hif + fabsf(qj.z));
       if (MIXED) {
         const float4 rj = P.rec1[j];
         const float dx = (Qi.x - qj.x) + (Ri.x - rj.x);
         const float dy = (Qi.y - qj.y) + (Ri.y - rj.y);
         const float d2 = dx * dx + dy * dy;
-        if (d2 > KC * hij * hij) continue;
+        if (d2 > KC * hij * hij) return;
         const float q = sqrtf(d2) / hij;
         float w;
         if (KERNEL == SPH_KERNEL_CUBIC) {
@@ -475,15 +513,14 @@ __global__ void __launch_bounds__(kPairBlock) k_sumdens(StepArgs a, PairPtrs P, 
       } else {
         const float dx = Qi.x - qj.x, dy = Qi.y - qj.y;
         const float rp = SK * hij + g.pad_e;
-        if (dx * dx + dy * dy > rp * rp) continue;
+        if (dx * dx + dy * dy > rp * rp) return;
         const double4_32a A = P.r64a[j], B = P.r64b[j];
         const double ddx = xi - A.x, ddy = yi - A.y;
         const double r = __dsqrt_rn(__dadd_rn(__dmul_rn(ddx, ddx), __dmul_rn(ddy, ddy)));
         const double h = __dmul_rn(0.5, __dadd_rn(hi, fabs(B.w)));
         if (__ddiv_rn(r, h) <= 3.0) rho += B.x * (KERNEL == SPH_KERNEL_CUBIC ? cubic_w(r, h) : gauss_w(r, h));
       }
-    }
-  }
+   });
   a.rho[P.perm[k]] = MIXED ? f2d(rhof) : rho;
 }
 
@@ -508,11 +545,8 @@ __global__ void __launch_bounds__(kPairBlock)
   long long cnt = 0;
   const long long base = idx ? offsets[i] : 0;
   const Stencil sten(g, qref, qkey, W);
-  for (int b = -W; b <= W; b++) {
-    unsigned int s, e;
-    if (!sten.row(b, cstart, s, e)) continue;
-    for (unsigned int j = s; j < e; j++) {
-      if (filter && !in_ref_stencil(meta, j, g, qref)) continue;
+  for_stencil(sten, cstart, [&](unsigned int j) {
+      if (filter && !in_ref_stencil(meta, j, g, qref)) return;
       const int pj = perm[j];
       const double dx = xi - x[pj], dy = yi - y[pj];
       const double d2 = __dadd_rn(__dmul_rn(dx, dx), __dmul_rn(dy, dy));
@@ -523,8 +557,7 @@ __global__ void __launch_bounds__(kPairBlock)
         if (idx) idx[base + cnt] = pj;
         cnt++;
       }
-    }
-  }
+   });
   if (!idx) {
     counts[i] = cnt;
     return;

@@ -18,6 +18,14 @@ namespace sph {
 
 constexpr int kBlock = 256;
 constexpr int kScanTile = 4096;  // cells per scan tile (1024 threads x 4, one uint4 each)
+// largest tile shift of the cell numbering: tiles of 2^s x 2^s cells over the
+// reference grid and over the own grid (0 = plain row-major cells)
+#ifndef SPH_TILE_SHIFT_REF
+#define SPH_TILE_SHIFT_REF 2
+#endif
+#ifndef SPH_TILE_SHIFT_OWN
+#define SPH_TILE_SHIFT_OWN 3
+#endif
 
 // ---------------------------------------------------------------------------
 // Order-preserving encoding of doubles for unsigned 64-bit atomicMin/Max
@@ -150,7 +158,9 @@ struct DevGrid {
   // traversal grid
   int mode;    // 0: the reference cells with their 3x3 stencil; 1: own grid
   int ntx, nty;  // traversal cells per axis
-  int ncells;  // traversal cells in use (cell ncells is the dump cell)
+  int ncells;  // cell ids in use, tiles padded (id ncells is the dump cell)
+  int ts;      // cells are numbered in tiles of 2^ts x 2^ts, row-major inside a tile
+  int ntlx;    // tiles per row
   float oxf, oyf, inv_ctf;  // mode 1 binning (FP32, monotone)
   int wt;           // stencil half-width of the pair kernels
   int need_filter;  // mode 1: candidates must pass the reference-stencil test
@@ -264,6 +274,20 @@ __device__ __forceinline__ unsigned long long warp_max_u64(unsigned long long v)
 // 32-bit signed saturation for cell coordinates
 __device__ __forceinline__ int sat_i32(long long v) {
   return v > (1ll << 30) ? (1 << 30) : (v < -(1ll << 30) ? -(1 << 30) : (int)v);
+}
+
+// Cell id of traversal cell (cx, cy): tiles of 2^ts x 2^ts cells in
+// row-major order, cells row-major inside a tile, so that consecutive ids
+// cover compact patches of the domain.
+__device__ __forceinline__ int tiled_key(int cx, int cy, int ts, int ntlx) {
+  const int m = (1 << ts) - 1;
+  return ((((cy >> ts) * ntlx + (cx >> ts)) << ts) + (cy & m)) * (1 << ts) + (cx & m);
+}
+__device__ __forceinline__ void tiled_cell(int key, int ts, int ntlx, int &cx, int &cy) {
+  const int m = (1 << ts) - 1;
+  const int tile = key >> (2 * ts), local = key & ((1 << (2 * ts)) - 1);
+  cx = (tile % ntlx) * (1 << ts) + (local & m);
+  cy = (tile / ntlx) * (1 << ts) + (local >> ts);
 }
 
 // Storage (flat-id) cell of a raw reference cell: the x-overflow cx == ncx

@@ -1,0 +1,300 @@
+"""Drop-in Solver (src/Solver.py:26-531) for the GB300 WCSPH step.
+
+Same constructor, attributes and methods as the reference's Solver; the
+particle state lives on the GPU between calls and every stage of the step
+(TimeStep, predict, neighbour build, EOS, continuity, momentum, boundary
+force, XSPH, correct) runs in libsph_gb300.  Extra keyword arguments:
+``precision`` ("fp64", the reference's arithmetic, or "mixed", FP32 pair
+arithmetic over FP64 state) and ``device``.
+
+run() follows the reference's loop (Solver.py:346-475): a settling phase with
+damping until the kinetic energy drops below kE times its initial value (or
+maxSettle steps, or customSettle), then the temporary boundary is removed,
+damping switches off and time advances.  step(n) runs n bare steps (dt ->
+predict -> _compute -> correct) without settling or storage, all on the
+device.
+"""
+import math
+import sys
+from time import perf_counter
+
+import numpy as np
+import torch
+
+from . import _lib, core, state
+from .Common import FLOAT_FIELDS, ParticleType, particle_dtype
+from .Tools.NNLinkedList import NNLinkedList
+
+
+class Solver:
+    def __init__(self, method, integrator, kernel, duration: float = 1.0, quick: bool = True,
+                 incrementalWriteout: bool = True, incrementalFile: str = "export", incrementalFreq: int = 1000,
+                 exportProperties=("x", "y", "p"), kE: float = 0.8, maxSettle: int = 500, timeStep: float = None,
+                 h: float = None, coupling=None, couplingIntegrator=None, couplingProperties=None,
+                 customSettle=None, damping: float = 0.05, precision: str = "fp64", device: str = "cuda"):
+        self.method = method
+        self.integrator = integrator
+        self.kernel = kernel
+        self.nn = NNLinkedList(scale=2.0)
+        self.duration = duration
+        self.quick = quick
+        self.kEF = kE
+        self.maxSettle = maxSettle
+        self.timeStep = timeStep
+        self.h = h
+        self.ts_error = 0
+        self.damping = damping
+        self.coupling = coupling
+        self.couplingIntegrator = couplingIntegrator
+        self.couplingProperties = couplingProperties
+        self.customSettle = customSettle
+        self.incrementalWriteout = incrementalWriteout
+        self.incrementalFreq = incrementalFreq
+        self.incrementalFile = incrementalFile
+        self.exportProperties = list(exportProperties)
+        self.precision = precision
+        self.device = device
+        self.particleArray = None
+        self.num_particles = 0
+        self.data = []
+        self.export = {}
+        self.settleTime = 0.0
+        self.dt_a, self.dt_c, self.dt_f = [], [], []
+        self.timing_data = {k: 0.0 for k in ("total", "storage", "integrate_correction", "integrate_prediction",
+                                             "compute", "time_step", "neighbour_hood", "coupling")}
+        self._dp = None
+        self._ws = None
+
+    # ------------------------------------------------------------------ state
+    def addParticles(self, particles):
+        """Solver.addParticles (Solver.py:160-171)."""
+        if self.particleArray is None:
+            self.particleArray = np.array(particles, dtype=particle_dtype)
+        else:
+            self.particleArray = np.concatenate((self.particleArray, np.array(particles, dtype=particle_dtype)))
+
+    def _masks(self):
+        pa = self.particleArray
+        self.indexes = ~pa["deleted"]
+        self.num_particles = int(np.sum(self.indexes))
+        self.f_indexes = (pa["label"] == ParticleType.Fluid) & (~pa["deleted"])
+        self.c_indexes = (pa["label"] == ParticleType.Coupled) & (~pa["deleted"])
+        self.fluid_count = int(np.sum(self.f_indexes))
+
+    def _upload(self):
+        """Device copy of the active particles (the reference's pA[indexes])."""
+        active = self.particleArray[self.indexes]
+        if self._dp is None or self._dp.n != len(active):
+            self._dp = state.DeviceParticles(len(active), self.device)
+            self._ws = state.DeviceWorkspace(len(active), 0, self.device)
+        self._dp.upload(active)
+
+    def _download(self):
+        """Bring the device state back into particleArray."""
+        act = self._dp.to_array()
+        full = self.particleArray
+        idx = np.nonzero(self.indexes)[0]
+        for k in FLOAT_FIELDS:
+            full[k][idx] = act[k]
+
+    def _cfg(self, damping=None):
+        it = self.integrator
+        return core.config_struct(kernel=self.kernel.kernel_id, precision=self.precision,
+                                  integrator=it.integrator_id, pec_use_xsph=getattr(it, "useXSPH", False),
+                                  pec_strict=getattr(it, "strict", False), nn_scale=self.nn.scale,
+                                  h_fixed=self.h if self.h is not None else 0.0, cfl_c=0.25, cfl_f=0.25,
+                                  damping=self.damping if damping is None else damping,
+                                  dt_fixed=self.timeStep if self.timeStep is not None else 0.0)
+
+    # ------------------------------------------------------------------ setup
+    def setup(self):
+        """Solver.setup (Solver.py:173-208) on the device: h for fluid (fixed
+        or computeH), WCSPH.initialize, p and c for fluid, initial KE."""
+        self._masks()
+        self._upload()
+        core.initialize(self._dp, self.method.wcsph_struct(), self._cfg())
+        self.kE = self._kinetic_energy() * self.kEF
+        for key in self.exportProperties:
+            self.export[key] = []
+        self.data = [self.particleArray.copy()]
+
+    def _kinetic_energy(self):
+        """KineticEnergy over fluid (src/Equations/KineticEnergy.py:5-12)."""
+        dp = self._dp
+        f = dp.label == ParticleType.Fluid
+        return float((0.5 * dp.m[f] * (dp.vx[f] ** 2 + dp.vy[f] ** 2)).sum().item())
+
+    # ------------------------------------------------------------------ steps
+    def _minTimeStep(self) -> float:
+        """TimeStep over fluid with gamma 0.25 / 0.25 (Solver.py:210-230)."""
+        start = perf_counter()
+        dt3 = core.timestep(self._dp, self.method.wcsph_struct(), self._cfg(), self._ws).cpu().numpy()
+        m, c, f = float(dt3[0]), float(dt3[1]), float(dt3[2])
+        if m < 1e-6:
+            self.ts_error = len(self.dt_a)
+        self.dt_c.append(c)
+        self.dt_f.append(f)
+        self.dt_a.append(m)
+        self.timing_data["time_step"] += perf_counter() - start
+        return m
+
+    def _compute(self):
+        """Solver._compute (Solver.py:232-256): neighbour build, h, _loop."""
+        start = perf_counter()
+        core.compute(self._dp, self.method.wcsph_struct(), self._cfg(), self._ws)
+        torch.cuda.synchronize()
+        self.timing_data["compute"] += perf_counter() - start
+
+    def step(self, nsteps: int = 1, damping: float = 0.0):
+        """nsteps bare steps on the device (dt -> predict -> _compute ->
+        correct); appends the dt history."""
+        hist = torch.zeros((max(nsteps, 1), 3), dtype=torch.float64, device=self.device)
+        start = perf_counter()
+        core.run(self._dp, self.method.wcsph_struct(), self._cfg(damping), self._ws, nsteps, hist)
+        h = hist.cpu().numpy()
+        self.timing_data["compute"] += perf_counter() - start
+        self._ws.check()
+        for s in range(nsteps):
+            self.dt_a.append(float(h[s, 0]))
+            if self.timeStep is None:
+                self.dt_c.append(float(h[s, 1]))
+                self.dt_f.append(float(h[s, 2]))
+        return h[:nsteps]
+
+    def run(self):
+        """Solver.run (Solver.py:346-475)."""
+        start_all = perf_counter()
+        if self.particleArray is None or len(self.particleArray) == 0 or \
+                len(self.particleArray) != self.num_particles:
+            raise Exception("No or invalid particles set!")
+        t_step = 0
+        self.t = 0.0
+        self.settled = False
+        dt_dev = torch.zeros(1, dtype=torch.float64, device=self.device)
+        while self.t < self.duration:
+            if self.timeStep is None:
+                self.dt = self._minTimeStep()
+            else:
+                self.dt_a.append(self.timeStep)
+                self.dt = self.timeStep
+            dt_dev.fill_(self.dt)
+            cfg = self._cfg()
+            start = perf_counter()
+            core.predict(self._dp, cfg, dt_dev)
+            self.timing_data["integrate_prediction"] += perf_counter() - start
+            self._compute()
+            if self.coupling is not None:
+                start = perf_counter()
+                self._download()
+                self.particleArray = self.coupling(self.particleArray, self)
+                self._dp.upload(self.particleArray[self.indexes])
+                self.timing_data["coupling"] += perf_counter() - start
+            start = perf_counter()
+            core.correct(self._dp, cfg, dt_dev)
+            self.timing_data["integrate_correction"] += perf_counter() - start
+            start = perf_counter()
+            self._store(t_step)
+            self.timing_data["storage"] += perf_counter() - start
+            if self.settled:
+                self.t += self.dt
+            t_step += 1
+            if not self.settled and t_step > 1:
+                ke, cs = 1e12, False
+                if self.customSettle is None:
+                    ke = self._kinetic_energy()
+                else:
+                    self._download()
+                    cs = self.customSettle(self.particleArray, self)
+                if (ke < self.kE) or (t_step > self.maxSettle) or cs:
+                    if t_step > self.maxSettle:
+                        print("\nWARNING! Maximum settle steps reached, check configuration, maybe increase "
+                              "spacing between wall and particles.")
+                    self._settle()
+        self._download()
+        self.timing_data["total"] = perf_counter() - start_all
+        self.t_step = t_step
+
+    def _settle(self):
+        """End of settling (Solver.py:420-451): delete TempBoundary
+        particles (p = -1e15), damping off, settleTime."""
+        self._download()
+        pa = self.particleArray
+        inds = np.nonzero((pa["label"] == ParticleType.TempBoundary) & (~pa["deleted"]))[0]
+        pa["deleted"][inds] = True
+        self._masks()
+        pa["p"][inds] = -1e15
+        self._upload()
+        self.settleTime = float(sum(self.dt_a))
+        self.damping = 0.0
+        self.settled = True
+
+    def _store(self, t_step: int):
+        """Solver._store (Solver.py:477-486): the export properties of this
+        step; the full array of the latest step in data; incremental save."""
+        need = set(self.exportProperties)
+        active = self._dp.soa([k for k in FLOAT_FIELDS if k in need]) if need else {}
+        idx = np.nonzero(self.indexes)[0]
+        for key in self.exportProperties:
+            full = np.array(self.particleArray[key], copy=True)
+            full[idx] = active[key] if key in active else full[idx]
+            self.export[key].append(full)
+        if self.incrementalWriteout and t_step % self.incrementalFreq == 0:
+            self._download()
+            self.data = [self.particleArray.copy()]
+            self.save("{0}-{1}.hdf5".format(self.incrementalFile, t_step), printLocation=False)
+
+    # ------------------------------------------------------------------ io
+    def timing(self):
+        """Timing table (Solver.py:489-495)."""
+        total = self.timing_data["total"] or 1e-30
+        print("\nDetailed timing statistics:")
+        print("%-24s %12s %16s" % ("Name", "Time [s]", "Percentage [%]"))
+        for k, v in self.timing_data.items():
+            print("%-24s %12.3f %16.2f" % (k, v, v / total * 100))
+
+    def save(self, location: str, printLocation: bool = True, extraProperties: dict = None):
+        """Solver.save (Solver.py:497-531): the HDF5 layout of the reference
+        (particleArray, dt_a, dt_c, dt_f, settleTime, one dataset per export
+        key); written with h5py, or as an .npz of the same datasets when h5py
+        is not installed."""
+        if self._dp is not None:
+            self._download()
+        data = {"particleArray": self.particleArray, "dt_a": np.asarray(self.dt_a), "dt_c": np.asarray(self.dt_c),
+                "dt_f": np.asarray(self.dt_f), "settleTime": np.asarray(self.settleTime)}
+        for key in self.exportProperties:
+            if self.export.get(key):
+                data[key] = np.stack(self.export[key])
+        if extraProperties:
+            data.update(extraProperties)
+        try:
+            import h5py
+        except ImportError:
+            h5py = None
+        if h5py is not None:
+            with h5py.File(location, "w") as h5f:
+                for k, v in data.items():
+                    if np.ndim(v) == 0:
+                        h5f.create_dataset(k, data=v)
+                    else:
+                        h5f.create_dataset(k, data=v, shuffle=True, compression="gzip")
+        else:
+            np.savez_compressed(location if location.endswith(".npz") else location + ".npz", **data)
+        if printLocation:
+            print('\nExported arrays to: "{0}".'.format(location))
+
+    def load(self, file: str):
+        """Solver.load (Solver.py:143-158): particleArray and the dt series."""
+        try:
+            import h5py
+        except ImportError:
+            h5py = None
+        if h5py is not None and not file.endswith(".npz"):
+            with h5py.File(file, "r") as h5f:
+                self.particleArray = h5f["particleArray"][:]
+                self.dt_a = list(h5f["dt_a"][:])
+                self.dt_c = list(h5f["dt_c"][:])
+                self.dt_f = list(h5f["dt_f"][:])
+        else:
+            z = np.load(file if file.endswith(".npz") else file + ".npz")
+            self.particleArray = z["particleArray"]
+            self.dt_a, self.dt_c, self.dt_f = list(z["dt_a"]), list(z["dt_c"]), list(z["dt_f"])

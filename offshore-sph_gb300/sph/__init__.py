@@ -1,1 +1,24 @@
-"""GB300-native WCSPH step behind Offshore-SPH's plugin surface."""
+"""GB300-native WCSPH step behind Offshore-SPH's plugin surface.
+
+Drop-in classes with the reference's names and constructors:
+
+    from sph import Solver, WCSPH, CubicSpline, Gaussian, PEC, Euler
+    solver = Solver(WCSPH(height, r0, rho0, useXSPH, Pb), PEC(useXSPH, strict), CubicSpline(), duration, h=...)
+    solver.addParticles(particles)      # a particle_dtype array
+    solver.setup(); solver.run()
+
+Every stage of the step runs in libsph_gb300.so (CUDA, sm_103a) through its C
+ABI (include/sph_gb300.h); there is no CPU fallback.
+"""
+from .Common import ParticleType, particle_dtype, get_label_code
+from .Methods.WCSPH import WCSPH
+from .Kernels.CubicSpline import CubicSpline
+from .Kernels.Gaussian import Gaussian
+from .Integrators.PEC import PEC
+from .Integrators.Euler import Euler
+from .Tools.NNLinkedList import NNLinkedList
+from .Equations.TimeStep import TimeStep
+from .Solver import Solver
+
+__all__ = ["ParticleType", "particle_dtype", "get_label_code", "WCSPH", "CubicSpline", "Gaussian", "PEC", "Euler",
+           "NNLinkedList", "TimeStep", "Solver"]

@@ -136,3 +136,16 @@ def gauss_deriv(r, h):
     L.check(L.load().sph_gauss_deriv(r.numel(), r.data_ptr(), h.data_ptr(), out.data_ptr(), current_stream()),
             "sph_gauss_deriv")
     return out
+
+
+def on_device(pA, op, fields, as_fluid=False):
+    """Run op(dp) on a device copy of the particle array pA and copy the
+    listed fields back into pA (the reference's functions return the array
+    they were given, modified)."""
+    dp = DeviceParticles.from_array(pA)
+    if as_fluid:
+        dp.label.zero_()
+    op(dp)
+    for f in fields:
+        pA[f] = dp.fields[f].cpu().numpy()
+    return pA

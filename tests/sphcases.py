@@ -70,7 +70,10 @@ def compare_state(got, want, fields, tol):
     """Return {field: rel_err} for fields whose error exceeds tol."""
     bad = {}
     for k in fields:
-        g = got[k] if isinstance(got, dict) else getattr(got, k)
+        if isinstance(got, dict) or (isinstance(got, np.ndarray) and got.dtype.names):
+            g = got[k]
+        else:
+            g = getattr(got, k)
         e = rel_err(g, want[k])
         if not (e <= tol):
             bad[k] = e

@@ -1,0 +1,184 @@
+"""The drop-in classes (sph.Solver, WCSPH, CubicSpline, Gaussian, PEC, Euler,
+NNLinkedList, TimeStep) used the way the reference's own tests use its
+classes (test/test_kernels_cubic.py, test/test_kernels_Gaussian.py,
+test/test_integrators_pec.py, test/test_integrators_euler.py,
+test/test_linked_list.py), plus Solver runs against the oracle."""
+import numpy as np
+import pytest
+
+import sphcases as SC
+
+pytestmark = pytest.mark.gpu
+
+
+@pytest.fixture(scope="module")
+def sph():
+    import torch
+    if not torch.cuda.is_available():
+        pytest.skip("no CUDA device")
+    import sph as pkg
+    from sph import build
+    build.build()
+    return pkg
+
+
+def test_cubic_known_answers(sph):
+    """test/test_kernels_cubic.py:11-72"""
+    k = sph.CubicSpline()
+    fac = lambda h: 10 / (7 * np.pi * h * h)
+    r = np.array([1.0])
+    for q, h, want in [(0.5, 2.0, fac(2.0) * (1 - 1.5 * 0.25 * 0.75)), (1.0, 1.0, fac(1.0) * (1 - 1.5 * 0.5)),
+                       (1.5, 2 / 3, fac(2 / 3) * 0.25 * 0.5 ** 3), (2.0, 0.5, 0.0), (3.0, 1 / 3, 0.0)]:
+        assert k.evaluate(r, np.array([h]))[0] == pytest.approx(want, abs=1e-7)
+    r, x = np.array([2.0]), np.array([3.0])
+    for q, h, dwdq in [(0.5, 4.0, fac(4.0) * -3.0 * 0.5 * (1 - 0.375)), (1.0, 2.0, fac(2.0) * -0.75),
+                       (2.0, 1.0, 0.0)]:
+        assert k.gradient(x, r, np.array([h]))[0] == pytest.approx(dwdq / (h * 2.0) * 3.0, abs=1e-7)
+    assert k.gradient(x, r, np.array([2 / 3]))[0] == 0.0
+
+
+def test_gaussian_matches_reference(sph):
+    z = SC.load("kernels")
+    g = sph.Gaussian()
+    assert SC.rel_err(g.evaluate(z["r"], z["h"]), z["gauss_w"]) <= 1e-14
+    assert SC.rel_err(g.derivative(z["r"], z["h"]), z["gauss_deriv"]) <= 1e-14
+    assert SC.rel_err(g.gradient(z["x"], z["r"], z["h"]), z["gauss_grad"]) <= 1e-14
+
+
+def _particle(sph, label):
+    p = np.zeros(1, dtype=sph.particle_dtype)
+    p["label"] = label
+    p["vx"], p["vy"], p["ax"], p["ay"], p["drho"] = 1.0, 3.0, 5.0, 0.0, 10.0
+    return 2.0, p
+
+
+def test_pec_known_answers(sph):
+    """test/test_integrators_pec.py:13-76 (dt = 2)."""
+    i = sph.PEC(useXSPH=False)
+    dt, p = _particle(sph, sph.ParticleType.Fluid)
+    p = i.predict(dt, p, 0)
+    assert p["x"][0] == pytest.approx(dt * 0.5) and p["y"][0] == pytest.approx(dt * 0.5 * 3.0)
+    assert p["rho"][0] == pytest.approx(dt * 0.5 * 10.0)
+    p = i.correct(dt, p, 0)
+    assert p["x"][0] == pytest.approx(dt * 1.0 + 0.5 * 5 * 2 * 2) and p["y"][0] == pytest.approx(dt * 3.0)
+    assert p["rho"][0] == pytest.approx(10 * dt)
+    # PEC equals Euler when the forces are not re-evaluated
+    _, pi = _particle(sph, sph.ParticleType.Fluid)
+    _, pe = _particle(sph, sph.ParticleType.Fluid)
+    pi = i.correct(dt, i.predict(dt, pi, 0), 0)
+    pe = sph.Euler().correct(dt, sph.Euler().predict(dt, pe, 0), 0)
+    for k in ("x", "y", "vx", "vy", "rho"):
+        assert pi[k][0] == pytest.approx(pe[k][0])
+
+
+def test_integrators_match_reference(sph):
+    z = SC.load("eos_integrators")
+    base = np.zeros(len(z["in_x"]), dtype=sph.particle_dtype)
+    for k in base.dtype.names:
+        if "in_" + k in z.files:
+            base[k] = z["in_" + k]
+    for xs in (0, 1):
+        for strict in (0, 1):
+            for d in (0, 5):
+                it = sph.PEC(useXSPH=bool(xs), strict=bool(strict))
+                a = it.predict(0.003, base.copy(), d / 100.0)
+                tag = "pec_x%d_s%d_d%d" % (xs, strict, d)
+                for k in ("x", "y", "vx", "vy", "rho", "x0", "y0", "vx0", "vy0", "rho0"):
+                    assert SC.rel_err(a[k], z[tag + "_pred_" + k]) <= 1e-13, (tag, k)
+                a = it.correct(0.003, a, d / 100.0)
+                for k in ("x", "y", "vx", "vy", "rho"):
+                    assert SC.rel_err(a[k], z[tag + "_corr_" + k]) <= 1e-13, (tag, k)
+    e = sph.Euler().correct(0.003, base.copy(), 0.0)
+    for k in ("x", "y", "vx", "vy", "rho"):
+        assert SC.rel_err(e[k], z["euler_" + k]) <= 1e-13
+    np.testing.assert_allclose(sph.TimeStep().compute(len(base), base, 0.25, 0.25), z["ts"], rtol=1e-14)
+    np.testing.assert_allclose(sph.TimeStep().compute(len(base), base, 0.3, 0.25), z["ts_c03"], rtol=1e-14)
+
+
+def test_wcsph_pressure_and_initialize(sph):
+    z = SC.load("eos_integrators")
+    m = sph.WCSPH(height=2.0, r0=0.025, rho0=1000.0, useXSPH=False, Pb=0.0, useSummationDensity=False)
+    assert m.co == pytest.approx(float(z["co"]), rel=1e-15) and m.B == pytest.approx(float(z["B"]), rel=1e-15)
+    pa = np.zeros(len(z["rho"]), dtype=sph.particle_dtype)
+    pa["label"], pa["rho"], pa["y"] = z["label"], z["rho"], z["y"]
+    assert SC.rel_err(m.compute_pressure(pa), z["p"]) <= 1e-13
+    m2 = sph.WCSPH(height=3.0, r0=0.025, rho0=1000.0, useXSPH=False, Pb=101325.0)
+    assert SC.rel_err(m2.compute_pressure(pa), z["p_pb"]) <= 1e-13
+    out = m.initialize(pa.copy())
+    assert SC.rel_err(out["rho"], z["rho_height"]) <= 1e-13
+    with pytest.raises(NotImplementedError):
+        m.compute_acceleration(pa[0], None)
+
+
+def test_linked_list_matches_brute_force(sph):
+    """test/test_linked_list.py:12-94: 26 x 26 points 1 apart, h = 1, scale 3."""
+    xv = np.linspace(0, 25, 26)
+    gx, gy = np.meshgrid(xv, xv, indexing="ij")
+    pa = np.zeros(gx.size, dtype=sph.particle_dtype)
+    pa["x"], pa["y"], pa["h"] = gx.ravel(), gy.ravel(), 1.0
+    nn = sph.NNLinkedList(scale=3.0)
+    nn.update(pa)
+    hij, q, r, near0 = nn.near(0, pa)
+    assert {0, 1, 26, 27} <= set(near0.tolist())
+    d = np.hypot(pa["x"] - pa["x"][0], pa["y"] - pa["y"][0])
+    assert set(near0.tolist()) == set(np.nonzero(d <= 3.0)[0].tolist())
+    assert np.all(q <= 3.0)
+    z = SC.load("nn_grid26")
+    off, idx = nn.neighbour_sets()
+    for i in range(len(pa)):
+        assert set(idx[off[i]:off[i + 1]].tolist()) == set(z["idx"][z["offsets"][i]:z["offsets"][i + 1]].tolist())
+
+
+def _tank(sph, dx=0.025):
+    from sph import scenarios as S
+    return S.dam_break(width=0.2, height=0.4, dx=dx, tank_width=0.8, tank_height=0.6)
+
+
+def test_solver_steps_match_oracle(sph):
+    import oracle
+    dx = 0.025
+    pa = _tank(sph, dx)
+    solver = sph.Solver(sph.WCSPH(0.4, dx, 1000.0, False, 0.0), sph.PEC(False, True), sph.CubicSpline(), 1.0,
+                        h=1.3 * dx, incrementalWriteout=False)
+    solver.addParticles(pa.copy())
+    solver.setup()
+    P = oracle.Particles(arrays={k: pa[k] for k in pa.dtype.names if k != "deleted"})
+    par = oracle.wcsph_params(0.4, dx, 1000.0)
+    oracle.setup(P, par, 0.4, 1.3 * dx)
+    hist = solver.step(5)
+    dts = oracle.run(par, oracle.NN(2.0), P, 5, h_fixed=1.3 * dx)
+    np.testing.assert_allclose(hist, dts, rtol=1e-12)
+    solver._download()
+    bad = SC.compare_state(solver.particleArray, P.as_dict(), SC.STATE_FIELDS, 1e-9)
+    assert not bad, bad
+
+
+def test_solver_run_settles_and_advances(sph, tmp_path):
+    from sph.Common import ParticleType
+    dx = 0.025
+    pa = _tank(sph, dx)
+    # a temporary wall that the end of settling removes (DamBreak.py:31)
+    tmp = np.zeros(12, dtype=sph.particle_dtype)
+    tmp["label"] = ParticleType.TempBoundary
+    tmp["x"] = 0.21 + 0.0125
+    tmp["y"] = (np.arange(12) + 0.5) * 0.0125 * 2
+    pa = np.concatenate((pa, tmp))
+    solver = sph.Solver(sph.WCSPH(0.4, dx, 1000.0, False, 0.0), sph.PEC(False, True), sph.CubicSpline(),
+                        duration=2e-3, h=1.3 * dx, maxSettle=5, incrementalWriteout=False,
+                        exportProperties=["x", "y", "p"])
+    solver.addParticles(pa)
+    solver.setup()
+    solver.run()
+    assert solver.settled and solver.t >= 2e-3
+    assert solver.t_step == len(solver.dt_a) == len(solver.export["x"])
+    assert np.all(solver.particleArray["deleted"][solver.particleArray["label"] == ParticleType.TempBoundary])
+    assert np.all(solver.particleArray["p"][solver.particleArray["label"] == ParticleType.TempBoundary] == -1e15)
+    assert solver.settleTime == pytest.approx(sum(solver.dt_a[:6]))
+    assert np.all(np.isfinite(solver.particleArray["x"]))
+    path = str(tmp_path / "out.hdf5")
+    solver.save(path, printLocation=False)
+    s2 = sph.Solver(sph.WCSPH(0.4, dx, 1000.0, False, 0.0), sph.PEC(False, True), sph.CubicSpline())
+    import os
+    s2.load(path if os.path.exists(path) else path + ".npz")
+    np.testing.assert_array_equal(s2.particleArray["x"], solver.particleArray["x"])
+    assert len(s2.dt_a) == len(solver.dt_a)
