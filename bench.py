@@ -1,13 +1,16 @@
 #!/usr/bin/env python
 """WCSPH throughput benchmark (particle-steps/s) on one or more GB300s.
 
-Workload (default ``lattice1m``): the 1M-particle lattice of the single
-derivative evaluation configuration -- 1000 x 1000 fluid particles at
-dx = 0.01, jitter U(+-0.05 dx), v ~ N(0, 0.1), rho = 1000 (1 + U(+-0.01)),
-h = 1.3 dx, cubic spline, no boundaries -- advanced by full PEC time steps.
-One step = TimeStep (Courant/force dt) -> PEC predict -> neighbour build ->
-h reset + Tait EOS + continuity + momentum (one fused pair kernel) -> PEC
-correct, all on the device.  ``dambreak2m`` is the 2M-fluid dam break.
+Workload (default ``dambreak1m``): a 1M-fluid 2D dam break -- the 1:2 column
+of the 3200-particle case at 707 x 1414 particles, dx = 0.01, in a tank 4x its
+width and 1.5x its height with 2 wall layers at dx/2 (28k boundary particles),
+rho0 = 1000, H = 14.14 m, h = 1.3 dx, cubic spline, alpha = 0.01, Courant 0.3,
+hydrostatic start -- advanced by full PEC time steps.  One step = TimeStep
+(Courant/force dt) -> PEC predict -> neighbour build -> h reset + Tait EOS +
+continuity + momentum + boundary force (the fused pair kernels) -> PEC
+correct, all on the device.  Also: ``lattice1m`` / ``lattice1m_gauss`` (the
+1000 x 1000 jittered lattice, cubic / Gaussian), ``dambreak2m`` (10 x 20 m
+column, 2M fluid), ``dambreak3200``.
 
 Metric: particle-steps/s = fluid particles x steps / device time of the
 timed steps (whole job: summed over ranks; N > 1 runs independent replicas).
@@ -35,10 +38,19 @@ METRIC = "WCSPH particle-steps/s"
 UNIT = "particle-steps/s"
 PAIR_BYTES = 81     # algorithmic bytes of the pair evaluation per particle (x,y,vx,vy,rho,m,h,label in; drho,ax,ay out)
 STEP_BYTES = 385    # algorithmic bytes of one PEC step per particle (dt 32 + predict 144 + build 24 + pair 81 + correct 104)
+# DRAM bytes (read + write) per particle of one pair launch, from the ncu
+# captures summarised in profiles/ (dram__bytes_read.sum + dram__bytes_write.sum
+# of k_pair_tiles over its particle count)
+TRAFFIC_PER_PARTICLE = {("dambreak1m", "mixed"): 77.0,  # profiles/k_pair_tiles_dambreak1m.md
+                        ("lattice1m", "mixed"): 76.5}
 
 
 def workload(name):
     from sph import scenarios as S
+    if name == "dambreak1m":
+        return dict(pa=S.cfg_dam_break_1m(), height=14.14, r0=0.01, h=0.013, kernel=0, gamma_c=0.3, setup=True,
+                    desc="1M-fluid dam break: 7.07x14.14 m column at dx=0.01 (707x1414 fluid) in a 28.3x21.2 m "
+                         "tank, 2 wall layers at dx/2, cubic, PEC, Courant 0.3")
     if name == "lattice1m":
         pa = S.jittered_lattice(1000, 1000, 0.01, seed=0)
         return dict(pa=pa, height=10.0, r0=0.01, h=0.013, kernel=0, gamma_c=0.25, setup=False,
@@ -59,10 +71,33 @@ def workload(name):
     raise SystemExit("unknown workload " + name)
 
 
-def lattice_sample(n_side, seed=0):
-    """The same lattice recipe at n_side x n_side (CPU baseline sample)."""
+def sample(wl_name, wl, size):
+    """A smaller case of the same recipe for the CPU timings: a size x size
+    lattice, or a dam break whose column is size x 2 size particles at the
+    workload's dx (same H scaling: H = column height).  Returns (particles,
+    height, description)."""
     from sph import scenarios as S
-    return S.jittered_lattice(n_side, n_side, 0.01, seed=seed)
+    if wl_name.startswith("lattice"):
+        return (S.jittered_lattice(size, size, 0.01, seed=0), wl["height"],
+                "%dx%d lattice of the same recipe" % (size, size))
+    dx = wl["r0"]
+    w, h = size * dx, 2 * size * dx
+    return (S.dam_break(w, h, dx, 4.0 * w, 1.5 * h), h,
+            "dam break of the same recipe, %dx%d fluid column" % (size, 2 * size))
+
+
+def oracle_particles(wl, pa, height):
+    import oracle
+    par = oracle.wcsph_params(height, wl["r0"], 1000.0, kernel=wl["kernel"])
+    d = {k: pa[k] for k in pa.dtype.names if k != "deleted"}
+    P = oracle.Particles(arrays=d)
+    if wl["setup"]:
+        oracle.setup(P, par, height, wl["h"])
+    else:
+        P.h[P.label == 0] = wl["h"]
+        P.p[:] = oracle.eos(P.label, P.rho, par)
+        P.c[:] = par.co
+    return P, par
 
 
 # ---------------------------------------------------------------------------
@@ -185,19 +220,13 @@ def e2e_steps(core, dp, wc, cfg, ws, k, pa):
     return s.elapsed_time(e) / 1e3, h2d, d2h
 
 
-def cpu_baseline(wl, budget_s=10.0):
-    """The oracle (C restatement of the reference's step) on a bounded sample:
-    a 200 x 200 lattice of the same recipe, PEC steps, all host threads."""
+def cpu_baseline(wl_name, wl, budget_s=10.0):
+    """The oracle (C restatement of the reference's step) on a bounded sample
+    of the same recipe, PEC steps, all host threads."""
     import oracle
     threads = oracle.max_threads()
-    side = 200
-    pa = lattice_sample(side)
-    d = {k: pa[k] for k in pa.dtype.names if k != "deleted"}
-    d["h"][:] = wl["h"]
-    par = oracle.wcsph_params(wl["height"], wl["r0"], 1000.0, kernel=wl["kernel"])
-    d["p"] = oracle.eos(d["label"], d["rho"], par)
-    d["c"][:] = par.co
-    P = oracle.Particles(arrays=d)
+    pa, height, what = sample(wl_name, wl, 200 if wl_name.startswith("lattice") else 141)
+    P, par = oracle_particles(wl, pa, height)
     nn = oracle.NN(2.0)
     oracle.run(par, nn, P, 1, h_fixed=wl["h"], gamma_c=wl["gamma_c"], nthreads=threads)
     steps, t0 = 0, time.perf_counter()
@@ -209,13 +238,13 @@ def cpu_baseline(wl, budget_s=10.0):
             break
     nf = int(np.sum(P.label == 0))
     return {"value": nf * steps / el, "unit": UNIT, "cores": threads, "kind": "port",
-            "sample": "%dx%d lattice of the same recipe (%d fluid), %d PEC steps, OpenMP over particles"
-                      % (side, side, nf, steps)}
+            "sample": "%s (%d fluid), %d PEC steps, OpenMP over particles" % (what, nf, steps)}
 
 
 def run_reference(args, wl_name):
     """--impl reference: the CPU reference implementation of the step (the C
-    restatement in oracle/, all host threads) on a bounded sample."""
+    restatement in oracle/, all host threads) on a bounded sample of the same
+    workload, sized so that warmup + steps take about a minute."""
     import oracle
     rank = int(os.environ.get("RANK", "0"))
     if rank != 0:
@@ -223,34 +252,26 @@ def run_reference(args, wl_name):
     oracle.build()
     wl = workload(wl_name)
     threads = oracle.max_threads()
-    # size the per-step sample so that warmup + steps take about a minute
-    side = 1000 if wl_name.startswith("lattice") else None
-    par = oracle.wcsph_params(wl["height"], wl["r0"], 1000.0, kernel=wl["kernel"])
-
-    def make(side_):
-        if side_ is None:
-            pa = wl["pa"]
-        else:
-            pa = lattice_sample(side_)
-        d = {k: pa[k] for k in pa.dtype.names if k != "deleted"}
-        P = oracle.Particles(arrays=d)
-        if wl["setup"]:
-            oracle.setup(P, par, wl["height"], wl["h"])
-        else:
-            P.h[P.label == 0] = wl["h"]
-            P.p[:] = oracle.eos(P.label, P.rho, par)
-            P.c[:] = par.co
-        return P
-
-    P = make(side)
-    nn = oracle.NN(2.0)
-    t0 = time.perf_counter()
-    oracle.run(par, nn, P, 1, h_fixed=wl["h"], gamma_c=wl["gamma_c"], nthreads=threads)
-    per_step = time.perf_counter() - t0
+    # start small and grow: the reference's cost per step grows faster than
+    # linearly for dam breaks (walls have h = 0, so its cells are 1 m wide)
+    lattice = wl_name.startswith("lattice")
+    size, size_max = (100, 1000) if lattice else (60, 707)
     total = args.steps + args.warmup
-    if side is not None and per_step * total > 60.0:
-        side = max(100, int(side * (60.0 / (per_step * total)) ** 0.5))
-        P = make(side)
+    target = 60.0 / total
+    nn = oracle.NN(2.0)
+    for _ in range(5):
+        pa, height, what = sample(wl_name, wl, size)
+        P, par = oracle_particles(wl, pa, height)
+        t0 = time.perf_counter()
+        oracle.run(par, nn, P, 1, h_fixed=wl["h"], gamma_c=wl["gamma_c"], nthreads=threads)
+        per_step = time.perf_counter() - t0
+        ratio = target / max(per_step, 1e-9)
+        if 0.5 <= ratio <= 2.0:
+            break
+        new = int(min(size_max, max(20, size * ratio ** (0.5 if lattice else 0.25))))
+        if new == size:
+            break
+        size = new
     for _ in range(args.warmup):
         oracle.run(par, nn, P, 1, h_fixed=wl["h"], gamma_c=wl["gamma_c"], nthreads=threads)
     t0 = time.perf_counter()
@@ -258,13 +279,12 @@ def run_reference(args, wl_name):
     el = time.perf_counter() - t0
     nf = int(np.sum(P.label == 0))
     v = nf * args.steps / el
-    sample = ("%s: %s" % (wl_name, "%dx%d lattice sample (%d fluid)" % (side, side, nf) if side else
-                          "full workload (%d fluid)" % nf)) + ", PEC steps, OpenMP over particles"
+    smp = "%s: %s (%d fluid), PEC steps, OpenMP over particles" % (wl_name, what, nf)
     out = {"impl": "reference", "metric": METRIC, "value": v, "unit": UNIT, "n_gpus": args.gpus,
            "steps": args.steps, "warmup": args.warmup, "ms_per_step": el / args.steps * 1e3,
            "higher_is_better": True, "scaling": "weak", "vs_baseline": None, "dtype": "f64", "data": "synthetic",
-           "config": {"workload": wl["desc"], "sample": sample},
-           "cpu_baseline": {"value": v, "unit": UNIT, "cores": threads, "kind": "port", "sample": sample},
+           "config": {"workload": wl_name + ": " + wl["desc"], "sample": smp},
+           "cpu_baseline": {"value": v, "unit": UNIT, "cores": threads, "kind": "port", "sample": smp},
            "e2e": {"value": v, "unit": UNIT, "h2d_bytes_per_step": 0, "d2h_bytes_per_step": 0}}
     print(json.dumps(out))
 
@@ -275,7 +295,7 @@ def main():
     ap.add_argument("--steps", type=int, default=2000)
     ap.add_argument("--warmup", type=int, default=10)
     ap.add_argument("--impl", default="ours", choices=["ours", "reference"])
-    ap.add_argument("--workload", default="lattice1m")
+    ap.add_argument("--workload", default="dambreak1m")
     ap.add_argument("--precision", default="mixed", choices=["mixed", "fp64"])
     ap.add_argument("--no-extras", action="store_true", help="skip the FP64 / e2e / CPU / profile passes")
     args = ap.parse_args()
@@ -320,7 +340,9 @@ def main():
         dist.all_reduce(t, op=dist.ReduceOp.MAX)
     el = float(t.item())
     value = world * nfluid * args.steps / el
-    launches_per_step = 11
+    # per step: bounds/predict, grid, keys, 3 scan passes, scatter, cellsort,
+    # records, pair tiles, pair fallback list (mixed) or one FP64 pair kernel
+    launches_per_step = 11 if args.precision == "mixed" else 10
     out = {"metric": METRIC, "value": value, "unit": UNIT, "n_gpus": world, "steps": args.steps,
            "warmup": args.warmup, "ms_per_step": el / args.steps * 1e3, "higher_is_better": True,
            "scaling": "weak", "vs_baseline": None,
@@ -340,9 +362,11 @@ def main():
         step_s = sum(stages.values()) / 1e3 / kprof
         ach = dp.n * PAIR_BYTES / pair_s / 1e9
         out["stages_ms_per_step"] = {k: v / kprof for k, v in stages.items()}
-        out["roofline"] = {"bound": "hbm", "kernel": "k_pair32" if args.precision == "mixed" else "k_pair64",
+        traffic = TRAFFIC_PER_PARTICLE.get((args.workload, args.precision))
+        out["roofline"] = {"bound": "hbm",
+                           "kernel": "k_pair_tiles + k_pair_list" if args.precision == "mixed" else "k_pair (FP64)",
                            "achieved": ach, "peak": hbm, "unit": "GB/s", "frac": ach / hbm,
-                           "peak_kind": peak_kind, "traffic": None,
+                           "peak_kind": peak_kind, "traffic": traffic * dp.n if traffic else None,
                            "algorithmic_bytes_per_launch": dp.n * PAIR_BYTES,
                            "step_achieved_gbs": dp.n * STEP_BYTES / step_s / 1e9}
         # the GPU's own FP64 path on the same workload
@@ -361,7 +385,7 @@ def main():
         el_e, h2d, d2h = e2e_steps(core, dp, wc, cfg, ws, ke, wl["pa"])
         out["e2e"] = {"value": nfluid * ke / el_e, "unit": UNIT, "h2d_bytes_per_step": h2d,
                       "d2h_bytes_per_step": d2h, "steps": ke}
-        out["cpu_baseline"] = cpu_baseline(wl)
+        out["cpu_baseline"] = cpu_baseline(args.workload, wl)
     if rank == 0:
         print(json.dumps(out))
     if world > 1:

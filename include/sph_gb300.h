@@ -220,7 +220,7 @@ int sph_compute(sph_particles_t *pa, const sph_wcsph_t *w, const sph_config_t *c
  *    this call (asynchronously, on the stream). */
 #define SPH_STATIC_MAX_PARTICLES 32768
 #define SPH_STATIC_MAX_CELLS 131072
-#define SPH_STATIC_WS_BYTES 6291456
+#define SPH_STATIC_WS_BYTES 8388608
 int sph_compute_static(sph_particles_t *pa, const sph_wcsph_t *w, const sph_config_t *cfg, uint32_t *status,
                        sph_stream_t stream);
 

@@ -36,6 +36,11 @@ WsLayout make_layout(long long n_cap, long long max_cells) {
   L.rec2 = take(n * 16);
   L.rec64a = take(n * 32);
   L.rec64b = take(n * 32);
+  // one entry per query slot, per 128-slot chunk and per tile bounds every
+  // list the tile pair kernel can write
+  L.fb_cap = (long long)(n + n / 128 + mc + 2);
+  L.fb = take((size_t)L.fb_cap * 8);
+  L.tiles = take((mc + 1) * 4);
   L.total = off;
   return L;
 }
@@ -60,6 +65,9 @@ WsPtrs ws_ptrs(const sph_workspace_t *ws) {
   p.rec2 = (float4 *)(b + L.rec2);
   p.rec64a = (double4_32a *)(b + L.rec64a);
   p.rec64b = (double4_32a *)(b + L.rec64b);
+  p.fb = (int2 *)(b + L.fb);
+  p.tiles = (int *)(b + L.tiles);
+  p.fb_cap = L.fb_cap;
   p.n_cap = L.n_cap;
   p.max_cells = L.max_cells;
   p.n_parts = L.n_parts;

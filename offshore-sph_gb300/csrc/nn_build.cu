@@ -204,6 +204,7 @@ __global__ void k_grid(DevCtrl *ctrl, DevGrid *g, GridParams gp) {
   ctrl->xmin = kEncMinId; ctrl->xmax = kEncMaxId; ctrl->ymin = kEncMinId; ctrl->ymax = kEncMaxId;
   ctrl->hmin_all = kEncMinId; ctrl->hmax_new = kEncMaxId;
   ctrl->alias_count = 0;
+  ctrl->tl_count = 0;
   unsigned status = 0;
   bool fin = isfinite(xmin) && isfinite(xmax) && isfinite(ymin) && isfinite(ymax) && isfinite(hmin) &&
              isfinite(hmax);
@@ -228,6 +229,8 @@ __global__ void k_grid(DevCtrl *ctrl, DevGrid *g, GridParams gp) {
   g->ncx = ncx; g->ncy = ncy; g->ncells_ref = ncx * ncy;
   g->xminf = (float)xmin; g->yminf = (float)ymin; g->inv_csf = (float)cs1;
   g->hmax = hmax;
+  // the mixed records compute h in FP32 (a few ulp from the FP64 value)
+  g->hmaxf = __double2float_ru(hmax) * 1.00001f;
   // interaction radius: the kernel support (cubic 2h, Gaussian 3h) and the
   // Lennard-Jones reach min(r0, 3h)
   const bool cubic = gp.kernel == SPH_KERNEL_CUBIC;
@@ -482,15 +485,22 @@ __global__ void __launch_bounds__(kBlock) k_scatter(const int *__restrict__ keys
   keys_sorted[slot] = key;
 }
 
+// In-cell order by particle index (deterministic); the first particle of each
+// non-empty tile also lists its tile for the tile pair kernel.
 __global__ void __launch_bounds__(kBlock) k_cellsort(const int *__restrict__ perm_tmp,
                                                      const int *__restrict__ keys_sorted,
                                                      const unsigned int *__restrict__ cstart,
                                                      const int2 *__restrict__ refcell, long long n,
-                                                     int *__restrict__ perm, int2 *__restrict__ meta) {
+                                                     const DevGrid *__restrict__ gp, DevCtrl *ctrl,
+                                                     int *__restrict__ perm, int2 *__restrict__ meta,
+                                                     int *__restrict__ tiles) {
   long long k = (long long)blockIdx.x * blockDim.x + threadIdx.x;
   if (k >= n) return;
   int key = keys_sorted[k];
   unsigned int s = cstart[key], e = cstart[key + 1];
+  const int ts2 = 2 * gp->ts;
+  if (key < gp->ncells && (unsigned)k == __ldg(&cstart[(key >> ts2) << ts2]))
+    tiles[atomicAdd(&ctrl->tl_count, 1u)] = key >> ts2;
   int v = perm_tmp[k];
   unsigned int rank = 0;
   for (unsigned int t = s; t < e; t++) rank += (unsigned)(perm_tmp[t] < v);
@@ -512,7 +522,8 @@ void launch_build(const StepArgs &a, const WsPtrs &w, const sph_config_t &cfg, c
   k_scan_top<<<1, 1024, 0, st>>>(w.scan_part, (int)w.n_parts);
   k_scan_apply<<<(unsigned)w.n_parts, kScanThreads, 0, st>>>(w.counts, w.grid, w.scan_part, w.cstart);
   k_scatter<<<nb, kBlock, 0, st>>>(w.keys, a.n, w.counts, w.cstart, w.perm_tmp, w.keys_sorted);
-  k_cellsort<<<nb, kBlock, 0, st>>>(w.perm_tmp, w.keys_sorted, w.cstart, w.refcell, a.n, w.perm, w.meta);
+  k_cellsort<<<nb, kBlock, 0, st>>>(w.perm_tmp, w.keys_sorted, w.cstart, w.refcell, a.n, w.grid, w.ctrl, w.perm,
+                                    w.meta, w.tiles);
 }
 
 // ---------------------------------------------------------------------------

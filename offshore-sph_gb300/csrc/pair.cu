@@ -207,6 +207,115 @@ __device__ __forceinline__ double accel2(double ax, double ay) {
   return __dadd_rn(__dmul_rn(ax, ax), __dmul_rn(ay, ay));
 }
 
+// ---------------------------------------------------------------------------
+// Mixed-form pair physics, shared by the tile kernel and the global-path
+// kernel so that both give bit-identical sums for the same candidate order.
+// ---------------------------------------------------------------------------
+struct MixedAcc {
+  float fd = 0.f, fax = 0.f, fay = 0.f, fbx = 0.f, fby = 0.f, fsx = 0.f, fsy = 0.f;
+};
+
+struct MixedConsts {
+  float KC, r02f, co, alpha, beta, eps, D;
+};
+
+template <int KERNEL>
+__device__ __forceinline__ MixedConsts mixed_consts(const PairParams &pp) {
+  MixedConsts c;
+  c.KC = KERNEL == SPH_KERNEL_CUBIC ? 4.0f : 9.0f;  // (support / h)^2
+  const float r0f = (float)pp.r0;
+  c.r02f = r0f * r0f;
+  c.co = (float)pp.co;
+  c.alpha = (float)pp.alpha;
+  c.beta = (float)pp.beta;
+  c.eps = (float)pp.eps;
+  c.D = (float)pp.D;
+  return c;
+}
+
+// One candidate j of query i: the exact support test, then continuity,
+// momentum with artificial viscosity, the Lennard-Jones boundary force and
+// XSPH.  Qi/qj: x_hi, y_hi, h (sign bit: non-fluid), m; Ri/rj: x_lo, y_lo,
+// rho, p / rho^2; Vi and *vjp: vx_hi, vy_hi, vx_lo, vy_lo (read only when the
+// pair is inside the support).
+template <int KERNEL, bool XSPH, bool SUMDENS>
+__device__ __forceinline__ void mixed_pair(MixedAcc &acc, const MixedConsts &c, float4 Qi, float4 Ri, float4 Vi,
+                                           float4 qj, float4 rj, const float4 *vjp) {
+  const float hif = Qi.z;
+  const float dx = (Qi.x - qj.x) + (Ri.x - rj.x);
+  const float dy = (Qi.y - qj.y) + (Ri.y - rj.y);
+  const float d2 = dx * dx + dy * dy;
+  const float hij = 0.5f * (hif + fabsf(qj.z));
+  const float h2 = hij * hij;
+  const bool jf = !signbit(qj.z);
+  float lim = c.KC * h2;
+  if (!jf) lim = fmaxf(lim, fminf(c.r02f, 9.0f * h2));
+  if (d2 > lim) return;
+  const float4 vj = *vjp;
+  const float inv_h = __fdividef(1.0f, hij);
+  const float inv_r = d2 > 0.f ? rsqrtf(d2) : 0.f;
+  const float r = d2 * inv_r;
+  const float q = r * inv_h;
+  const float vxij = (Vi.x - vj.x) + (Vi.z - vj.z);
+  const float vyij = (Vi.y - vj.y) + (Vi.w - vj.w);
+  float w, coef;
+  if (KERNEL == SPH_KERNEL_CUBIC) {
+    const float al = (float)kCubicFac * inv_h * inv_h;
+    const float t2 = fmaxf(2.0f - q, 0.f);
+    const bool outer = q > 1.0f;
+    w = outer ? al * 0.25f * (t2 * t2 * t2) : al * (1.0f - 1.5f * (q * q) * (1.0f - 0.5f * q));
+    const float gq = outer ? -0.75f * (t2 * t2) : -3.0f * q * (1.0f - 0.75f * q);
+    coef = r >= 1e-10f ? al * gq * inv_h * inv_r : 0.f;
+  } else {
+    const float ac = (float)kInvPi * inv_h * inv_h;
+    const float e = __expf(-q * q);
+    w = ac * e;
+    coef = r * hij > 1e-12f ? -2.0f * ac * e * inv_h * inv_h : 0.f;
+  }
+  const float dwx = coef * dx, dwy = coef * dy;
+  const float mj = qj.w;
+  if (jf) {
+    if (!SUMDENS) acc.fd = fmaf(mj, vxij * dwx + vyij * dwy, acc.fd);
+    const float dot = vxij * dx + vyij * dy;
+    const float hb = 0.5f * (hif + hij);
+    const float mu = hb * dot * __fdividef(1.0f, d2 + 0.01f * hb * hb);
+    const float PI = dot < 0.f ? mu * (c.beta * mu - c.alpha * 0.5f * c.co) * __fdividef(2.0f, Ri.z + rj.z) : 0.f;
+    const float fac = mj * (Ri.w + rj.w + PI);
+    acc.fax = fmaf(-fac, dwx, acc.fax);
+    acc.fay = fmaf(-fac, dwy, acc.fay);
+  } else if (d2 <= c.r02f && d2 > 1e-24f) {
+    const float ir2 = __fdividef(1.0f, d2);
+    const float f2 = c.r02f * ir2;
+    const float fac = c.D * (f2 * f2 - f2) * ir2;
+    acc.fbx = fmaf(fac, dx, acc.fbx);
+    acc.fby = fmaf(fac, dy, acc.fby);
+  }
+  if (XSPH) {
+    const float fac = -c.eps * mj * w * __fdividef(2.0f, Ri.z + rj.z);
+    acc.fsx = fmaf(fac, vxij, acc.fsx);
+    acc.fsy = fmaf(fac, vyij, acc.fsy);
+  }
+}
+
+// Writes the derivatives of particle i (gravity on y) and returns its encoded
+// a^2 for the TimeStep reduction.
+template <bool XSPH, bool SUMDENS>
+__device__ __forceinline__ unsigned long long mixed_store(const MixedAcc &acc, const StepArgs &a, int i) {
+  const float axs = acc.fax + acc.fbx, ays = acc.fay + acc.fby;
+  a.ax[i] = f2d(axs);
+  a.ay[i] = f2d(ays) - 9.81;
+  a.drho[i] = SUMDENS ? 0.0 : f2d(acc.fd);
+  if (XSPH) {
+    a.xsphx[i] = a.vx[i] + f2d(acc.fsx);
+    a.xsphy[i] = a.vy[i] + f2d(acc.fsy);
+  } else {
+    a.xsphx[i] = 0.0;
+    a.xsphy[i] = 0.0;
+  }
+  const float ayg = ays - 9.81f;
+  return enc_d(f2d(axs * axs + ayg * ayg));
+}
+
 struct PairPtrs {
   const float4 *rec0, *rec1, *rec2;
   const double4_32a *r64a, *r64b;
@@ -224,21 +333,20 @@ struct PairOcc {
   static constexpr int blocks = MIXED ? SPH_PAIR_MIXED_BLOCKS : 4;
 };
 
+// Global-path evaluation of query slot k (all candidate records read from
+// global memory); returns the encoded a^2 of a fluid query, else the max
+// identity.  lists: the block's per-thread candidate lists.
 template <int KERNEL, bool XSPH, bool SUMDENS, bool MIXED>
-__global__ void __launch_bounds__(kPairBlock, PairOcc<MIXED>::blocks)
-    k_pair(StepArgs a, PairPtrs P, PairParams pp, double *dt_out, double *dt_hist) {
+__device__ __forceinline__ unsigned long long pair_query(const StepArgs &a, const PairPtrs &P, const PairParams &pp,
+                                                         const DevGrid &g, bool filter, long long k,
+                                                         unsigned int (*lists)[kPairBlock]) {
   constexpr int kListCap = ListCap<KERNEL>::value;
-  __shared__ unsigned int lists[kListCap][kPairBlock];
-  const DevGrid g = *P.grid;
-  const bool filter = g.mode == 1 && (g.need_filter || P.ctrl->alias_count > 0);
-  const long long k = (long long)blockIdx.x * blockDim.x + threadIdx.x;
   const int tid = threadIdx.x;
   unsigned long long ea = kEncMaxId;
-  const float KC = KERNEL == SPH_KERNEL_CUBIC ? 4.0f : 9.0f;               // (support / h)^2
   const float SK = (KERNEL == SPH_KERNEL_CUBIC ? 2.0f : 3.0f) * 1.000002f;  // support / h, padded
-  const float r0f = (float)pp.r0, r02f = r0f * r0f;
+  const float r0f = (float)pp.r0;
   const float pad = g.pad_e;
-  if (k < pp.n) {
+  {
     const float4 Qi = P.rec0[k];  // x_hi, y_hi, h (signed), m
     const float hif = Qi.z;
     if (!signbit(hif)) {
@@ -259,71 +367,16 @@ __global__ void __launch_bounds__(kPairBlock, PairOcc<MIXED>::blocks)
         rhoi = B.y; slf = B.z; hi = B.w;
       }
       // accumulators: FP32 (mixed) or FP64
-      float fd = 0.f, fax = 0.f, fay = 0.f, fbx = 0.f, fby = 0.f, fsx = 0.f, fsy = 0.f;
+      MixedAcc acc;
+      const MixedConsts mc = mixed_consts<KERNEL>(pp);
       double dd = 0.0, dax = 0.0, day = 0.0, dbx = 0.0, dby = 0.0, dsx = 0.0, dsy = 0.0;
-      const float co = (float)pp.co, alpha = (float)pp.alpha, beta = (float)pp.beta, eps = (float)pp.eps;
-      const float D = (float)pp.D;
 
       // ---- phase 2: pair physics over the list
       auto physics = [&](int cnt) {
         for (int t = 0; t < cnt; t++) {
           const unsigned int j = lists[t][tid];
           if (MIXED) {
-            const float4 qj = P.rec0[j];
-            const float4 rj = P.rec1[j];
-            const float dx = (Qi.x - qj.x) + (Ri.x - rj.x);
-            const float dy = (Qi.y - qj.y) + (Ri.y - rj.y);
-            const float d2 = dx * dx + dy * dy;
-            const float hij = 0.5f * (hif + fabsf(qj.z));
-            const float h2 = hij * hij;
-            const bool jf = !signbit(qj.z);
-            float lim = KC * h2;
-            if (!jf) lim = fmaxf(lim, fminf(r02f, 9.0f * h2));
-            if (d2 > lim) continue;
-            const float4 vj = P.rec2[j];
-            const float inv_h = __fdividef(1.0f, hij);
-            const float inv_r = d2 > 0.f ? rsqrtf(d2) : 0.f;
-            const float r = d2 * inv_r;
-            const float q = r * inv_h;
-            const float vxij = (Vi.x - vj.x) + (Vi.z - vj.z);
-            const float vyij = (Vi.y - vj.y) + (Vi.w - vj.w);
-            float w, coef;
-            if (KERNEL == SPH_KERNEL_CUBIC) {
-              const float al = (float)kCubicFac * inv_h * inv_h;
-              const float t2 = fmaxf(2.0f - q, 0.f);
-              const bool outer = q > 1.0f;
-              w = outer ? al * 0.25f * (t2 * t2 * t2) : al * (1.0f - 1.5f * (q * q) * (1.0f - 0.5f * q));
-              const float gq = outer ? -0.75f * (t2 * t2) : -3.0f * q * (1.0f - 0.75f * q);
-              coef = r >= 1e-10f ? al * gq * inv_h * inv_r : 0.f;
-            } else {
-              const float ac = (float)kInvPi * inv_h * inv_h;
-              const float e = __expf(-q * q);
-              w = ac * e;
-              coef = r * hij > 1e-12f ? -2.0f * ac * e * inv_h * inv_h : 0.f;
-            }
-            const float dwx = coef * dx, dwy = coef * dy;
-            const float mj = qj.w;
-            if (jf) {
-              if (!SUMDENS) fd = fmaf(mj, vxij * dwx + vyij * dwy, fd);
-              const float dot = vxij * dx + vyij * dy;
-              const float hb = 0.5f * (hif + hij);
-              const float mu = hb * dot * __fdividef(1.0f, d2 + 0.01f * hb * hb);
-              const float PI = dot < 0.f ? mu * (beta * mu - alpha * 0.5f * co) * __fdividef(2.0f, Ri.z + rj.z) : 0.f;
-              const float fac = mj * (Ri.w + rj.w + PI);
-              fax = fmaf(-fac, dwx, fax);
-              fay = fmaf(-fac, dwy, fay);
-            } else if (d2 <= r02f && d2 > 1e-24f) {
-              const float ir2 = __fdividef(1.0f, d2);
-              const float f2 = r02f * ir2;
-              const float fac = D * (f2 * f2 - f2) * ir2;
-              fbx = fmaf(fac, dx, fbx);
-              fby = fmaf(fac, dy, fby);
-            }
-            if (XSPH) {
-              const float fac = -eps * mj * w * __fdividef(2.0f, Ri.z + rj.z);
-              fsx = fmaf(fac, vxij, fsx);
-              fsy = fmaf(fac, vyij, fsy);
-            }
+            mixed_pair<KERNEL, XSPH, SUMDENS>(acc, mc, Qi, Ri, Vi, P.rec0[j], P.rec1[j], P.rec2 + j);
           } else {
             const double4_32a A = P.r64a[j], B = P.r64b[j];
             const double dx = xi - A.x, dy = yi - A.y;
@@ -426,34 +479,66 @@ __global__ void __launch_bounds__(kPairBlock, PairOcc<MIXED>::blocks)
         any = exact_count(a, P.perm, g, qref, qkey, W, g.mode == 1, P.meta, P.cstart, xi, yi, hi) > 0;
       }
       if (any) {
-        double axf, ayf;
         if (MIXED) {
-          const float axs = fax + fbx, ays = fay + fby;
-          axf = f2d(axs);
-          ayf = f2d(ays) - 9.81;
-          a.drho[i] = SUMDENS ? 0.0 : f2d(fd);
-          if (XSPH) {
-            a.xsphx[i] = a.vx[i] + f2d(fsx);
-            a.xsphy[i] = a.vy[i] + f2d(fsy);
-          } else {
-            a.xsphx[i] = 0.0;
-            a.xsphy[i] = 0.0;
-          }
-          const float ayg = ays - 9.81f;
-          ea = enc_d(f2d(axs * axs + ayg * ayg));
+          ea = mixed_store<XSPH, SUMDENS>(acc, a, i);
         } else {
-          axf = dax + dbx;
-          ayf = (day - 9.81) + dby;
+          const double axf = dax + dbx;
+          const double ayf = (day - 9.81) + dby;
           a.drho[i] = SUMDENS ? 0.0 : dd;
           a.xsphx[i] = XSPH ? vxi + dsx : 0.0;
           a.xsphy[i] = XSPH ? vyi + dsy : 0.0;
           ea = enc_d(accel2(axf, ayf));
+          a.ax[i] = axf;
+          a.ay[i] = ayf;
         }
-        a.ax[i] = axf;
-        a.ay[i] = ayf;
       } else {
         ea = enc_d(accel2(a.ax[i], a.ay[i]));  // keeps its previous values (SolverTools.py:150-153)
       }
+    }
+  }
+  return ea;
+}
+
+template <int KERNEL, bool XSPH, bool SUMDENS, bool MIXED>
+__global__ void __launch_bounds__(kPairBlock, PairOcc<MIXED>::blocks)
+    k_pair(StepArgs a, PairPtrs P, PairParams pp, double *dt_out, double *dt_hist) {
+  __shared__ unsigned int lists[ListCap<KERNEL>::value][kPairBlock];
+  const DevGrid g = *P.grid;
+  const bool filter = g.mode == 1 && (g.need_filter || P.ctrl->alias_count > 0);
+  const long long k = (long long)blockIdx.x * blockDim.x + threadIdx.x;
+  unsigned long long ea = kEncMaxId;
+  if (k < pp.n) ea = pair_query<KERNEL, XSPH, SUMDENS, MIXED>(a, P, pp, g, filter, k, lists);
+  if (pp.do_dt) timestep_epilogue(P.ctrl, ea, pp.co, pp.cfl_c, pp.cfl_f, dt_out, dt_hist);
+}
+
+// The queries the tile kernel left over (slot ranges of at most kPairBlock
+// slots), on the global path; the last block resets the list and, when asked,
+// finishes the TimeStep reduction.
+constexpr int kListBlocks = 6;
+template <int KERNEL, bool XSPH, bool SUMDENS>
+__global__ void __launch_bounds__(kPairBlock, kListBlocks)
+    k_pair_list(StepArgs a, PairPtrs P, PairParams pp, const int2 *__restrict__ fb, double *dt_out,
+                double *dt_hist) {
+  __shared__ unsigned int lists[ListCap<KERNEL>::value][kPairBlock];
+  __shared__ bool last;
+  const DevGrid g = *P.grid;
+  const bool filter = g.mode == 1 && (g.need_filter || P.ctrl->alias_count > 0);
+  const unsigned int cnt = *(volatile unsigned int *)&P.ctrl->fb_count;
+  unsigned long long ea = kEncMaxId;
+  for (unsigned int e = blockIdx.x; e < cnt; e += gridDim.x) {
+    const int2 r = fb[e];
+    if ((int)threadIdx.x < r.y) {
+      const unsigned long long q = pair_query<KERNEL, XSPH, SUMDENS, true>(a, P, pp, g, filter, r.x + threadIdx.x, lists);
+      ea = q > ea ? q : ea;
+    }
+  }
+  __syncthreads();
+  if (threadIdx.x == 0) {
+    __threadfence();
+    last = atomicAdd(&P.ctrl->fb_done, 1u) == gridDim.x - 1;
+    if (last) {
+      P.ctrl->fb_count = 0;
+      P.ctrl->fb_done = 0;
     }
   }
   if (pp.do_dt) timestep_epilogue(P.ctrl, ea, pp.co, pp.cfl_c, pp.cfl_f, dt_out, dt_hist);
@@ -575,6 +660,230 @@ __global__ void __launch_bounds__(kPairBlock)
 }
 
 // ---------------------------------------------------------------------------
+// Tile kernel (mixed form).  A block takes one tile of 2^ts x 2^ts cells at a
+// time and stages the records of the tile and its W-cell halo in shared
+// memory: a table of the (2^ts + 2W)^2 halo cells (counts -> exclusive scan ->
+// shared-memory offsets, cells row-major, so each stencil row of a query is
+// one contiguous shared-memory range), then one copy per cell.  Its queries
+// walk their stencils in shared memory, with 16-bit list entries.  The
+// candidate order (rows, then cells by x, then slot) is the global path's, so
+// both give bit-identical sums.
+// Left to the global path, through the fallback list: tiles whose halo does
+// not fit, queries whose own cell is not in their stencil or whose h is not
+// positive, and every query when candidates need the reference-stencil filter
+// or the halo table does not fit (wide stencils).
+// Blocks are persistent and claim one tile at a time from the list of
+// non-empty tiles the neighbour build writes, the next claim overlapping the
+// current tile.
+// ---------------------------------------------------------------------------
+constexpr int kHaloCellsMax = 144;  // (8 + 2 * 2)^2: 8x8 tiles with a 5x5 stencil
+constexpr int kHaloScanPer = (kHaloCellsMax + 31) / 32;
+#ifndef SPH_TILE_BLOCKS
+#define SPH_TILE_BLOCKS 7
+#endif
+#ifndef SPH_HALO_CAP
+#define SPH_HALO_CAP 384
+#endif
+#ifndef SPH_TILE_UNROLL_PAIRS
+#define SPH_TILE_UNROLL_PAIRS 1
+#endif
+#ifndef SPH_TILE_UNROLL_CANDS
+#define SPH_TILE_UNROLL_CANDS 1
+#endif
+constexpr int kTileBlocks = SPH_TILE_BLOCKS;
+constexpr int kTileUnrollPairs = SPH_TILE_UNROLL_PAIRS;  // ILP over list entries
+constexpr int kTileUnrollCands = SPH_TILE_UNROLL_CANDS;  // ILP over stencil candidates
+constexpr int kHaloCap = SPH_HALO_CAP;  // particles of one halo in shared memory
+static_assert(kHaloCap <= 65535, "list entries are 16-bit");
+
+__device__ __forceinline__ void fb_push(DevCtrl *ctrl, int2 *fb, unsigned int fb_cap, unsigned int s,
+                                        unsigned int len) {
+  const unsigned int e = atomicAdd(&ctrl->fb_count, 1u);
+  if (e < fb_cap) fb[e] = make_int2((int)s, (int)len);
+}
+
+template <int KERNEL, bool XSPH, bool SUMDENS>
+__global__ void __launch_bounds__(kPairBlock, kTileBlocks)
+    k_pair_tiles(StepArgs a, PairPtrs P, PairParams pp, const int *__restrict__ tiles, int2 *__restrict__ fb,
+                 unsigned int fb_cap) {
+  constexpr int kListCap = ListCap<KERNEL>::value;
+  __shared__ float4 h0[kHaloCap], h1[kHaloCap], h2[kHaloCap];  // rec0, rec1, rec2 of the halo
+  __shared__ unsigned short lists[kListCap][kPairBlock];
+  __shared__ unsigned int hoff[kHaloCellsMax + 1];  // shared-memory offset of each halo cell, then the total
+  __shared__ unsigned int hgs[kHaloCellsMax];       // its first sorted slot
+  __shared__ int s_tile[2];                         // this and the next claimed tile (-1: none left)
+  __shared__ unsigned long long red[kPairBlock / 32];
+  const int tid = threadIdx.x;
+  DevCtrl *ctrl = P.ctrl;
+  const DevGrid *gp = P.grid;
+  const int mode = gp->mode, ts = gp->ts, ntlx = gp->ntlx, ntx = gp->ntx, nty = gp->nty;
+  const long long ncx = gp->ncx;
+  const int W = mode == 0 ? 1 : gp->wt;
+  const int T = 1 << ts, HW = T + 2 * W, HC = HW * HW;
+  const bool filter = mode == 1 && (gp->need_filter || ctrl->alias_count > 0);
+  // per-query candidate radius: the padded reach of the largest pair h
+  // (every |h| <= hmaxf), so that one compare per candidate suffices
+  const float SK = (KERNEL == SPH_KERNEL_CUBIC ? 2.0f : 3.0f) * 1.000002f;  // support / h, padded
+  const float r0f = (float)pp.r0;
+  const float pad = gp->pad_e, hmaxf = gp->hmaxf;
+  const MixedConsts mc = mixed_consts<KERNEL>(pp);
+  unsigned long long ea = kEncMaxId;
+
+  if (filter || HC > kHaloCellsMax) {
+    // everything on the global path, in 128-slot chunks
+    if (tid == 0) {
+      const long long nch = (pp.n + kPairBlock - 1) / kPairBlock;
+      for (long long c = blockIdx.x; c < nch; c += gridDim.x)
+        fb_push(ctrl, fb, fb_cap, (unsigned)(c * kPairBlock), (unsigned)min((long long)kPairBlock, pp.n - c * kPairBlock));
+    }
+  } else {
+    const unsigned int ntl = ctrl->tl_count;
+    if (tid == 0) {
+      if (blockIdx.x == 0) {  // the dump cell (reference-OOB particles) is in no tile
+        const unsigned int d0 = __ldg(&P.cstart[gp->ncells]), d1 = __ldg(&P.cstart[gp->ncells + 1]);
+        for (unsigned int s = d0; s < d1; s += kPairBlock) fb_push(ctrl, fb, fb_cap, s, min((unsigned)kPairBlock, d1 - s));
+      }
+      const unsigned int c = atomicAdd(&ctrl->tile_next, 1u);
+      s_tile[0] = c < ntl ? tiles[c] : -1;
+    }
+    __syncthreads();
+    for (int it = 0;; it++) {
+      const int t = s_tile[it & 1];
+      if (t < 0) break;
+      if (tid == 0) {  // claim the next tile while this one runs
+        const unsigned int c = atomicAdd(&ctrl->tile_next, 1u);
+        s_tile[(it + 1) & 1] = c < ntl ? tiles[c] : -1;
+      }
+      const unsigned int qs = __ldg(&P.cstart[t << (2 * ts)]), qe = __ldg(&P.cstart[(t + 1) << (2 * ts)]);
+      const int ox = (t % ntlx) * T - W, oy = (t / ntlx) * T - W;
+      // halo table: counts and first slots
+      for (int c = tid; c < HC; c += kPairBlock) {
+        const int x = ox + c % HW, y = oy + c / HW;
+        unsigned int gs = 0, cnt = 0;
+        if (x >= 0 && x < ntx && y >= 0 && y < nty) {
+          const int key = tiled_key(x, y, ts, ntlx);
+          gs = __ldg(&P.cstart[key]);
+          cnt = __ldg(&P.cstart[key + 1]) - gs;
+        }
+        hgs[c] = gs;
+        hoff[c] = cnt;
+      }
+      __syncthreads();
+      if (tid < 32) {  // exclusive scan of the counts, kHaloScanPer cells per lane
+        const int c0 = tid * kHaloScanPer;
+        unsigned int v[kHaloScanPer], sum = 0;
+#pragma unroll
+        for (int u = 0; u < kHaloScanPer; u++) {
+          v[u] = c0 + u < HC ? hoff[c0 + u] : 0u;
+          sum += v[u];
+        }
+        unsigned int inc = sum;
+#pragma unroll
+        for (int d = 1; d < 32; d <<= 1) {
+          const unsigned int o = __shfl_up_sync(0xffffffffu, inc, d);
+          if (tid >= d) inc += o;
+        }
+        unsigned int run = inc - sum;
+#pragma unroll
+        for (int u = 0; u < kHaloScanPer; u++) {
+          if (c0 + u < HC) hoff[c0 + u] = run;
+          run += v[u];
+        }
+        if (tid == 31) hoff[HC] = inc;
+      }
+      __syncthreads();
+      const unsigned int total = hoff[HC];
+      if (total > (unsigned)kHaloCap) {  // halo does not fit: global path
+        if (tid == 0)
+          for (unsigned int s = qs; s < qe; s += kPairBlock) fb_push(ctrl, fb, fb_cap, s, min((unsigned)kPairBlock, qe - s));
+        __syncthreads();
+        continue;
+      }
+      // stage the halo's records: slot s belongs to the last cell whose offset is <= s
+      for (unsigned int s = tid; s < total; s += kPairBlock) {
+        int lo = 0, hi = HC;
+        while (hi - lo > 1) {
+          const int mid = (lo + hi) >> 1;
+          if (hoff[mid] <= s) lo = mid;
+          else hi = mid;
+        }
+        const unsigned int gsl = hgs[lo] + (s - hoff[lo]);
+        h0[s] = P.rec0[gsl];
+        h1[s] = P.rec1[gsl];
+        h2[s] = P.rec2[gsl];
+      }
+      __syncthreads();
+      for (unsigned int k = qs + tid; k < qe; k += kPairBlock) {
+        int cx, cy;
+        tiled_cell(P.keys_sorted[k], ts, ntlx, cx, cy);
+        const int hx = cx - ox, hy = cy - oy, hc = hy * HW + hx;
+        const unsigned int sq = hoff[hc] + (k - hgs[hc]);  // the query's own shared-memory slot
+        const float4 Qi = h0[sq];
+        const float hif = Qi.z;
+        if (signbit(hif)) continue;  // queries are fluid
+        if (P.meta[k].x >= ncx || !(hif > 0.f)) {  // aliased query or h <= 0
+          fb_push(ctrl, fb, fb_cap, k, 1u);
+          continue;
+        }
+        const float4 Ri = h1[sq], Vi = h2[sq];
+        const int i = P.perm[k];
+        MixedAcc acc;
+        auto physics = [&](int cnt) {
+#pragma unroll kTileUnrollPairs
+          for (int u = 0; u < cnt; u++) {
+            const unsigned int j = lists[u][tid];
+            mixed_pair<KERNEL, XSPH, SUMDENS>(acc, mc, Qi, Ri, Vi, h0[j], h1[j], h2 + j);
+          }
+        };
+        const float hq = 0.5f * (hif + hmaxf);
+        const float rq = fmaxf(SK * hq, fminf(r0f, 3.0f * hq) * 1.000002f) + pad;
+        const float rq2 = rq * rq;
+        int nl = 0;
+        for (int r = -W; r <= W; r++) {
+          const unsigned int *row = hoff + (hy + r) * HW + hx;
+          const unsigned int s1 = row[W + 1];
+#pragma unroll kTileUnrollCands
+          for (unsigned int j = row[-W]; j < s1; j++) {
+            const float4 qj = h0[j];
+            const float dx = Qi.x - qj.x, dy = Qi.y - qj.y;
+            if (fmaf(dx, dx, dy * dy) <= rq2 && j != sq) {  // j == sq: the particle itself contributes zero
+              lists[nl][tid] = (unsigned short)j;
+              if (++nl == kListCap) {
+                physics(nl);
+                nl = 0;
+              }
+            }
+          }
+        }
+        physics(nl);
+        const unsigned long long q = mixed_store<XSPH, SUMDENS>(acc, a, i);
+        ea = q > ea ? q : ea;
+      }
+      __syncthreads();
+    }
+  }
+  // this block's max a^2 (the list kernel finishes the TimeStep reduction);
+  // the last block resets the tile counter
+  if (pp.do_dt) {
+    const unsigned long long wm = warp_max_u64(ea);
+    if ((tid & 31) == 0) red[tid >> 5] = wm;
+  }
+  __syncthreads();
+  if (tid == 0) {
+    if (pp.do_dt) {
+      unsigned long long ba = kEncMaxId;
+      for (int w = 0; w < kPairBlock / 32; w++) ba = red[w] > ba ? red[w] : ba;
+      if (ba != kEncMaxId) atomicMax(&ctrl->pd_a2max, ba);
+    }
+    __threadfence();
+    if (atomicAdd(&ctrl->tile_done, 1u) == gridDim.x - 1) {
+      ctrl->tile_next = 0;
+      ctrl->tile_done = 0;
+    }
+  }
+}
+
+// ---------------------------------------------------------------------------
 // Launchers
 // ---------------------------------------------------------------------------
 static PairPtrs pair_ptrs(const WsPtrs &w) {
@@ -596,14 +905,34 @@ static PairParams pair_params(const StepArgs &a, const sph_config_t &cfg, const 
   return pp;
 }
 
+// SMs of the current device (cached per device)
+static int sm_count() {
+  static int cache[64] = {0};
+  int dev = 0;
+  cudaGetDevice(&dev);
+  if (dev < 0 || dev >= 64) return 152;
+  if (!cache[dev]) {
+    int v = 0;
+    cudaDeviceGetAttribute(&v, cudaDevAttrMultiProcessorCount, dev);
+    cache[dev] = v > 0 ? v : 152;
+  }
+  return cache[dev];
+}
+
 template <int KERNEL, bool XSPH, bool SUMDENS>
 static void pair_dispatch(const StepArgs &a, const WsPtrs &w, const sph_config_t &cfg, const PairParams &pp,
                           double *dt_out, double *dt_hist, cudaStream_t st) {
-  const unsigned nb = nblocks(a.n, kPairBlock);
-  if (cfg.precision == SPH_PREC_MIXED)
-    k_pair<KERNEL, XSPH, SUMDENS, true><<<nb, kPairBlock, 0, st>>>(a, pair_ptrs(w), pp, dt_out, dt_hist);
-  else
-    k_pair<KERNEL, XSPH, SUMDENS, false><<<nb, kPairBlock, 0, st>>>(a, pair_ptrs(w), pp, dt_out, dt_hist);
+  if (cfg.precision == SPH_PREC_MIXED) {
+    // persistent tile kernel, then the global path over what it left
+    const int sms = sm_count();
+    k_pair_tiles<KERNEL, XSPH, SUMDENS><<<sms * kTileBlocks, kPairBlock, 0, st>>>(a, pair_ptrs(w), pp, w.tiles,
+                                                                                   w.fb, (unsigned)w.fb_cap);
+    k_pair_list<KERNEL, XSPH, SUMDENS><<<sms * kListBlocks, kPairBlock, 0, st>>>(a, pair_ptrs(w), pp, w.fb,
+                                                                                          dt_out, dt_hist);
+  } else {
+    k_pair<KERNEL, XSPH, SUMDENS, false><<<nblocks(a.n, kPairBlock), kPairBlock, 0, st>>>(a, pair_ptrs(w), pp, dt_out,
+                                                                                          dt_hist);
+  }
 }
 
 void launch_pair(const StepArgs &a, const WsPtrs &w, const sph_config_t &cfg, const sph_wcsph_t &wc,

@@ -145,7 +145,11 @@ struct DevCtrl {
   unsigned int status;  // sticky SPH_STATUS_* bits
   unsigned int alias_count;
   unsigned int initialised;
-  unsigned int pad;
+  // pair-kernel scheduling: next tile chunk and finished blocks of the tile
+  // kernel; entries and finished blocks of the fallback list
+  unsigned int tile_next, tile_done;
+  unsigned int fb_count, fb_done;
+  unsigned int tl_count;  // non-empty tiles listed by the build
   double dt_ring[2][3];  // {dt, dt_c, dt_f} of the step with that parity
 };
 
@@ -154,7 +158,8 @@ struct DevGrid {
   // reference grid (src/Tools/NNLinkedList.py:86-127)
   double xmin, xmax, ymin, ymax, cs, inv_cs;
   long long ncx, ncy, ncells_ref;
-  float xminf, yminf, inv_csf, pad0;  // FP32 fast path of the reference binning
+  float xminf, yminf, inv_csf;  // FP32 fast path of the reference binning
+  float hmaxf;  // FP32 bound on every record's |h| (hmax rounded up, with margin)
   // traversal grid
   int mode;    // 0: the reference cells with their 3x3 stencil; 1: own grid
   int ntx, nty;  // traversal cells per axis
@@ -175,8 +180,8 @@ struct DevGrid {
 // Byte offsets of the workspace regions (computed on the host).
 struct WsLayout {
   size_t ctrl, grid, keys, refcell, perm_tmp, keys_sorted, perm, meta, counts, cstart, scan_part, rec0, rec1,
-      rec2, rec64a, rec64b, total;
-  long long n_cap, max_cells, n_parts;
+      rec2, rec64a, rec64b, fb, tiles, total;
+  long long n_cap, max_cells, n_parts, fb_cap;
 };
 
 WsLayout make_layout(long long n_cap, long long max_cells);
@@ -203,7 +208,9 @@ struct WsPtrs {
   unsigned int *scan_part;
   float4 *rec0, *rec1, *rec2;
   double4_32a *rec64a, *rec64b;
-  long long n_cap, max_cells, n_parts;
+  int2 *fb;  // fallback list of the tile pair kernel: (first slot, count <= 128)
+  int *tiles;  // non-empty tiles of the current build, in no particular order
+  long long n_cap, max_cells, n_parts, fb_cap;
 };
 
 WsPtrs ws_ptrs(const sph_workspace_t *ws);

@@ -120,6 +120,14 @@ def cfg_dam_break_large(scale_dx=0.01):
     return dam_break(10.0, 20.0, scale_dx, 40.0, 30.0)
 
 
+def cfg_dam_break_1m(dx=0.01):
+    """1M-fluid dam break: the 1:2 column of the 3200-particle case at 707 x 1414
+    particles (7.07 x 14.14 m at dx = 0.01) in a tank 4x its width and 1.5x its
+    height, 2 wall layers at dx/2."""
+    w, h = 707 * dx, 1414 * dx
+    return dam_break(w, h, dx, 4.0 * w, 1.5 * h)
+
+
 def cfg_adjoint():
     """20k-fluid dam break: 1.0 x 2.0 m column at dx = 0.01 in the 4 x 3 m tank."""
     return dam_break(1.0, 2.0, 0.01, 4.0, 3.0)
