@@ -289,6 +289,64 @@ def run_reference(args, wl_name):
     print(json.dumps(out))
 
 
+def replica_value(el, nfluid, steps, world, device):
+    """Whole-job throughput of N independent replicas: the slowest rank's
+    elapsed time (max over ranks) and the fluid particle-steps of all ranks
+    over it."""
+    import torch
+    import torch.distributed as dist
+    t = torch.tensor([el], dtype=torch.float64, device=device)
+    if world > 1:
+        dist.all_reduce(t, op=dist.ReduceOp.MAX)
+    el = float(t.item())
+    return el, world * nfluid * steps / el
+
+
+def accuracy(names):
+    """Mixed form against the GPU's own FP64 path (the oracle for the mixed
+    form) from identical states: the per-step derivative error of one
+    evaluation (drho, ax, ay: norm-wise relative error over fluid) and the
+    trajectory error (x, y, vx, vy, rho) after 1, 10 and 100 PEC steps.  One
+    JSON line per workload."""
+    import torch
+    from sph import build as sph_build
+    sph_build.build()
+    from sph import core
+
+    def rel(a, b):
+        a = a.double()
+        b = b.double()
+        n = torch.linalg.norm(b).item()
+        d = torch.linalg.norm(a - b).item()
+        return d / n if n > 0 else d
+
+    for name in names:
+        wl = workload(name)
+        f = torch.from_numpy(wl["pa"]["label"] == 0).cuda()
+        out = {"workload": name + ": " + wl["desc"], "n_fluid": int(f.sum().item())}
+        st = {}
+        for prec in ("fp64", "mixed"):
+            dp, wc, cfg, ws = prepare(wl, prec)
+            core.compute(dp, wc, cfg, ws)
+            ws.check()
+            st[prec] = (dp, wc, cfg, ws)
+        d64, dmx = st["fp64"][0], st["mixed"][0]
+        out["derivative"] = {k: rel(dmx.fields[k][f], d64.fields[k][f]) for k in ("drho", "ax", "ay")}
+        traj = {}
+        done = 0
+        for s in (1, 10, 100):
+            for prec in ("fp64", "mixed"):
+                dp, wc, cfg, ws = st[prec]
+                core.run(dp, wc, cfg, ws, s - done)
+                ws.check()
+            done = s
+            traj[str(s)] = {k: rel(dmx.fields[k][f], d64.fields[k][f]) for k in ("x", "y", "vx", "vy", "rho")}
+        out["trajectory"] = traj
+        print(json.dumps(out), flush=True)
+        del st, d64, dmx
+        torch.cuda.empty_cache()
+
+
 def main():
     ap = argparse.ArgumentParser()
     ap.add_argument("--gpus", type=int, default=1)
@@ -298,7 +356,12 @@ def main():
     ap.add_argument("--workload", default="dambreak1m")
     ap.add_argument("--precision", default="mixed", choices=["mixed", "fp64"])
     ap.add_argument("--no-extras", action="store_true", help="skip the FP64 / e2e / CPU / profile passes")
+    ap.add_argument("--accuracy", default=None,
+                    help="comma-separated workloads: mixed vs FP64 derivative and trajectory errors, then exit")
     args = ap.parse_args()
+    if args.accuracy:
+        accuracy(args.accuracy.split(","))
+        return
     if args.warmup < 3:
         raise SystemExit("--warmup must be >= 3")
     if args.impl == "reference":
@@ -335,11 +398,7 @@ def main():
     barrier()
     clk = clocks.stop()
     ws.check()
-    t = torch.tensor([el], dtype=torch.float64, device="cuda")
-    if world > 1:
-        dist.all_reduce(t, op=dist.ReduceOp.MAX)
-    el = float(t.item())
-    value = world * nfluid * args.steps / el
+    el, value = replica_value(el, nfluid, args.steps, world, "cuda")
     # per step: bounds/predict, grid, keys, 3 scan passes, scatter, cellsort,
     # records, pair tiles, pair fallback list (mixed) or one FP64 pair kernel
     launches_per_step = 11 if args.precision == "mixed" else 10
