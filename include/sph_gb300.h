@@ -260,6 +260,40 @@ enum {
 int sph_run_profiled(sph_particles_t *pa, const sph_wcsph_t *w, const sph_config_t *cfg, const sph_workspace_t *ws,
                      int64_t nsteps, double *stage_ms, sph_stream_t stream);
 
+/* ------------------------------------------------------------------------
+ * Differentiation form.  The reference has no derivatives; these entry
+ * points differentiate its step (fixed dt, src/Solver.py:370-372; PEC,
+ * src/Integrators/PEC.py:32-89; fixed h; FP64 form; no XSPH, no summation
+ * density) for losses built from a wall load: the x component of the
+ * Lennard-Jones boundary force (src/Equations/BoundaryForce.py:6-42) that
+ * the boundary particles at x >= wall_x exert on the fluid, with the sign of
+ * the load on the wall: load = -sum_i m_i b_x,i.
+ * ------------------------------------------------------------------------ */
+
+/* sph_run (fixed dt) that also writes load_hist[s] = the wall load of step
+ * s's evaluation (device doubles, nsteps of them), summed in a fixed order.
+ * fr: device scratch, n doubles. */
+int sph_run_wall_load(sph_particles_t *pa, const sph_wcsph_t *w, const sph_config_t *cfg, const sph_workspace_t *ws,
+                      int64_t nsteps, double wall_x, double *fr, double *load_hist, sph_stream_t stream);
+
+/* Adjoint of one step.  On entry xb .. drhob hold d loss / d S' for the
+ * state after the step (fluid particles; caller order), on exit d loss / d S
+ * for the state before it; S is pa's x, y, vx, vy, rho, ax, ay, drho (the
+ * state before the step, as sph_run leaves it).  alphab[i] accumulates the
+ * step's d loss / d alpha contribution of particle i (sum it for the
+ * gradient).  omega: the weight of this step's wall load in the loss (dt for
+ * a time integral).  The remaining pointers are device scratch of n doubles
+ * each; half is a scratch particle set of n particles (all fields). */
+typedef struct sph_adjoint {
+  double *xb, *yb, *vxb, *vyb, *rhob, *axb, *ayb, *drhob;
+  double *alphab;
+  double *lax, *lay, *lad, *xhb, *yhb, *vxhb, *vyhb, *rhohb, *alb;
+  double omega;
+  double wall_x;
+} sph_adjoint_t;
+int sph_adjoint_step(const sph_particles_t *pa, sph_particles_t *half, const sph_wcsph_t *w, const sph_config_t *cfg,
+                     const sph_workspace_t *ws, const sph_adjoint_t *adj, sph_stream_t stream);
+
 #ifdef __cplusplus
 }
 #endif

@@ -1,0 +1,338 @@
+// adjoint.cu -- reverse mode of the WCSPH step (FP64 form).
+//
+// The forward step with a fixed dt (src/Solver.py:370-372 timeStep path) and
+// the PEC integrator (src/Integrators/PEC.py:32-89, damping 0) maps the state
+// S = (x, v, rho, a, drho) of the fluid particles to S':
+//   half:    x_h = x + dt/2 v,  v_h = v + dt/2 a,  rho_h = rho + dt/2 drho
+//   compute: (A, D) = F(x_h, v_h, rho_h; alpha)   (src/Tools/SolverTools.py:120-175)
+//   correct: x' = x + dt v_h,  v' = v + dt A,  rho' = rho + dt D,  a' = A,  drho' = D
+// and adds omega * (wall load of the evaluation) to the loss.  The adjoint
+// step maps the adjoint of S' back to the adjoint of S:
+//   lambda_A = dt vb' + ab',  lambda_D = dt rhob' + drhob'       (k_adj_pre)
+//   (xb_h, vb_h, rhob_h, alphab) = VJP of F and of the wall load  (k_pair_adjoint)
+//   vb_h += dt xb';  xb = xb' + xb_h;  vb = vb' + dt/2 xb_h + vb_h;
+//   ab = dt/2 vb_h;  rhob = rhob' + rhob_h;  drhob = dt/2 rhob_h  (k_adj_post)
+//
+// k_pair_adjoint is the hand-written vector-Jacobian product of the fused
+// pair evaluation: continuity (src/Equations/Continuity.py), momentum with
+// artificial viscosity (src/Equations/Momentum.py), the Tait EOS inside
+// p/rho^2 (src/Equations/TaitEOS.py) and the Lennard-Jones boundary force
+// (src/Equations/BoundaryForce.py).  For a fluid pair (k, j) the outputs of
+// both particles enter one scalar
+//   phi = lQ . (S dW) + lC (v_kj . dW),
+//   lQ = -m_j lambdaA_k + m_k lambdaA_j,  lC = m_j lambdaD_k + m_k lambdaD_j,
+//   S = p_k/rho_k^2 + p_j/rho_j^2 + Pi_kj,
+// which is the same for (k, j) and (j, k); each thread differentiates it with
+// respect to its own position, velocity and density, so the product is a
+// gather over the neighbour set with no atomics.  The alpha adjoint takes
+// each thread's own outputs only, so each pair counts once.
+#include <math.h>
+
+#include "sph_internal.cuh"
+
+namespace sph {
+
+constexpr int kAdjBlock = 128;
+
+struct AdjParams {
+  double alpha, beta, co, r0, D, p1, p2, gamma, B, inv_rho0;
+  int lj_42;
+  double omega, wall_x, dt;
+  long long n;
+};
+
+// d(p/rho^2)/drho of a fluid particle from its rho and p/rho^2
+// (p = B ((rho/rho0)^gamma - 1) + Pb, src/Equations/TaitEOS.py:6-31)
+__device__ __forceinline__ double dothr_drho(double rho, double othr, const AdjParams &ap) {
+  if (!(rho > 0.0)) return 0.0;
+  const double t = rho * ap.inv_rho0;
+  double tg1;  // t^(gamma - 1)
+  if (ap.gamma == 7.0) {
+    const double t2 = t * t, t3 = t2 * t;
+    tg1 = t3 * t3;
+  } else {
+    tg1 = pow(t, ap.gamma - 1.0);
+  }
+  const double dp = ap.B * ap.gamma * ap.inv_rho0 * tg1;
+  return (dp - 2.0 * othr * rho) / (rho * rho);
+}
+
+// kernel gradient factor coef(r) (dW = coef * u) and its r-derivative, with
+// the reference's guards (CubicSpline.py:40-70, Gaussian.py:42-59)
+template <int KERNEL>
+__device__ __forceinline__ void grad_coef(double r, double h, double &coef, double &dcoef) {
+  coef = 0.0;
+  dcoef = 0.0;
+  const double q = r / h;
+  if (KERNEL == SPH_KERNEL_CUBIC) {
+    if (q > 2.0 || r < 1e-10) return;
+    const double al = kCubicFac / (h * h);
+    double g, gp;
+    if (q > 1.0) {
+      const double t = 2.0 - q;
+      g = -0.75 * t * t;
+      gp = 1.5 * t;
+    } else {
+      g = -3.0 * q * (1.0 - 0.75 * q);
+      gp = -3.0 + 4.5 * q;
+    }
+    coef = al * g / (h * r);
+    dcoef = al / (h * r) * (gp / h - g / r);
+  } else {
+    if (!(q <= 3.0) || !(r * h > 1e-12)) return;
+    const double ac = kInvPi / (h * h);
+    const double e = exp(-q * q);
+    coef = -2.0 * ac * e / (h * h);
+    dcoef = coef * (-2.0 * r / (h * h));
+  }
+}
+
+struct AdjPtrs {
+  const double4_32a *r64a, *r64b;
+  const int *perm, *keys_sorted;
+  const int2 *meta;
+  const unsigned int *cstart;
+  const DevGrid *grid;
+  DevCtrl *ctrl;
+  const double *lax, *lay, *lad;                  // lambda_A, lambda_D (caller order)
+  double *xhb, *yhb, *vxhb, *vyhb, *rhohb, *alb;  // outputs (caller order)
+};
+
+template <int KERNEL>
+__global__ void __launch_bounds__(kAdjBlock) k_pair_adjoint(AdjPtrs P, AdjParams ap) {
+  const long long k = (long long)blockIdx.x * blockDim.x + threadIdx.x;
+  if (k >= ap.n) return;
+  const DevGrid &g = *P.grid;
+  const double4_32a Ak = P.r64a[k], Bk = P.r64b[k];
+  const int i = P.perm[k];
+  if (signbit(Bk.w)) {  // not fluid: no outputs, its adjoint is not used
+    P.xhb[i] = P.yhb[i] = P.vxhb[i] = P.vyhb[i] = P.rhohb[i] = P.alb[i] = 0.0;
+    return;
+  }
+  const double xk = Ak.x, yk = Ak.y, vxk = Ak.z, vyk = Ak.w;
+  const double mk = Bk.x, rhok = Bk.y, othrk = Bk.z, hk = Bk.w;
+  const double lAxk = P.lax[i], lAyk = P.lay[i], lDk = P.lad[i];
+  const double dothk = dothr_drho(rhok, othrk, ap);
+  const double cbar = 0.5 * ap.co;
+  const int2 qref = P.meta[k];
+  const int qkey = P.keys_sorted[k];
+  const bool slow = qref.x >= g.ncx || !(hk > 0.0);
+  const int W = g.mode == 0 ? 1 : (slow ? g.wide : g.wt);
+  const bool filter = g.mode == 1 && (g.need_filter || P.ctrl->alias_count > 0);
+  double gx = 0.0, gy = 0.0, gvx = 0.0, gvy = 0.0, grho = 0.0, gal = 0.0;
+  const Stencil sten(g, qref, qkey, W);
+  for_stencil(sten, P.cstart, [&](unsigned int j) {
+    if (j == (unsigned int)k) return;
+    if (filter && !in_ref_stencil(P.meta, j, g, qref)) return;
+    const double4_32a Aj = P.r64a[j], Bj = P.r64b[j];
+    const double dx = xk - Aj.x, dy = yk - Aj.y;
+    const double r = __dsqrt_rn(__dadd_rn(__dmul_rn(dx, dx), __dmul_rn(dy, dy)));
+    const double hij = __dmul_rn(0.5, __dadd_rn(hk, fabs(Bj.w)));
+    if (!(__ddiv_rn(r, hij) <= 3.0)) return;  // the forward's neighbour test (NNLinkedList.py:74)
+    if (!signbit(Bj.w)) {
+      // fluid pair: continuity + momentum with artificial viscosity
+      const double mj = Bj.x, rhoj = Bj.y, othrj = Bj.z;
+      const double vxij = vxk - Aj.z, vyij = vyk - Aj.w;
+      double coef, dcoef;
+      grad_coef<KERNEL>(r, hij, coef, dcoef);
+      if (coef == 0.0 && dcoef == 0.0) return;
+      const double dWx = coef * dx, dWy = coef * dy;
+      const double dot = vxij * dx + vyij * dy;
+      double Pi = 0.0, dPi_dmu = 0.0, mu = 0.0, den = 1.0, hb = 0.0;
+      const double rbar = 0.5 * (rhok + rhoj);
+      if (dot < 0.0) {
+        hb = 0.5 * (hk + hij);
+        den = r * r + 0.01 * hb * hb;
+        mu = hb * dot / den;
+        Pi = mu * (ap.beta * mu - ap.alpha * cbar) / rbar;
+        dPi_dmu = (2.0 * ap.beta * mu - ap.alpha * cbar) / rbar;
+      }
+      const double S = othrk + othrj + Pi;
+      const int pj = P.perm[j];
+      const double lAxj = P.lax[pj], lAyj = P.lay[pj], lDj = P.lad[pj];
+      const double lQx = -mj * lAxk + mk * lAxj, lQy = -mj * lAyk + mk * lAyj;
+      const double lC = mj * lDk + mk * lDj;
+      const double lQdW = lQx * dWx + lQy * dWy;
+      // (d dW / d u)^T z = coef z + dcoef (u . z) u / r
+      const double uq = dx * lQx + dy * lQy;
+      const double ir = 1.0 / r;
+      gx += S * (coef * lQx + dcoef * uq * dx * ir) + lC * (coef * vxij + dcoef * dot * dx * ir);
+      gy += S * (coef * lQy + dcoef * uq * dy * ir) + lC * (coef * vyij + dcoef * dot * dy * ir);
+      gvx += lC * dWx;
+      gvy += lC * dWy;
+      if (dot < 0.0) {
+        const double f = lQdW * dPi_dmu * hb;
+        const double id2 = 1.0 / (den * den);
+        gx += f * (vxij / den - 2.0 * dot * dx * id2);
+        gy += f * (vyij / den - 2.0 * dot * dy * id2);
+        gvx += f * dx / den;
+        gvy += f * dy / den;
+        gal += -mj * (lAxk * dWx + lAyk * dWy) * (-mu * cbar / rbar);
+      }
+      grho += lQdW * (dothk - 0.5 * Pi / rbar);
+    } else if (r <= ap.r0 && r > 1e-12) {
+      // boundary pair: Lennard-Jones force b = D phi(r) u, phi = ((r0/r)^p1 - (r0/r)^p2) / r^2,
+      // and the wall load -m_k b.x when j is on the loaded wall
+      const double s = ap.r0 / r;
+      double sp1, sp2;
+      if (ap.lj_42) {
+        sp2 = s * s;
+        sp1 = sp2 * sp2;
+      } else {
+        sp1 = pow(s, ap.p1);
+        sp2 = pow(s, ap.p2);
+      }
+      const double r2 = r * r;
+      const double phi = (sp1 - sp2) / r2;
+      const double dphi = ((-ap.p1 - 2.0) * sp1 + (ap.p2 + 2.0) * sp2) / (r2 * r);
+      const double zx = lAxk - ((ap.omega != 0.0 && Aj.x >= ap.wall_x) ? ap.omega * mk : 0.0), zy = lAyk;
+      const double uz = dx * zx + dy * zy;
+      gx += ap.D * (phi * zx + dphi * uz * dx / r);
+      gy += ap.D * (phi * zy + dphi * uz * dy / r);
+    }
+  });
+  P.xhb[i] = gx;
+  P.yhb[i] = gy;
+  P.vxhb[i] = gvx;
+  P.vyhb[i] = gvy;
+  P.rhohb[i] = grho;
+  P.alb[i] = gal;
+}
+
+// lambda_A = dt vb' + ab', lambda_D = dt rhob' + drhob' (zero for non-fluid)
+__global__ void k_adj_pre(const int8_t *__restrict__ label, long long n, double dt, const double *vxb,
+                          const double *vyb, const double *rhob, const double *axb, const double *ayb,
+                          const double *drhob, double *lax, double *lay, double *lad) {
+  const long long i = (long long)blockIdx.x * blockDim.x + threadIdx.x;
+  if (i >= n) return;
+  if (!is_fluid(label[i])) {
+    lax[i] = lay[i] = lad[i] = 0.0;
+    return;
+  }
+  lax[i] = dt * vxb[i] + axb[i];
+  lay[i] = dt * vyb[i] + ayb[i];
+  lad[i] = dt * rhob[i] + drhob[i];
+}
+
+// the half state of step S (PEC.predict's update, src/Integrators/PEC.py:32-60)
+// into the scratch particle set; m, h and label are copied
+__global__ void k_adj_half(StepArgs s, StepArgs h, double dt) {
+  const long long i = (long long)blockIdx.x * blockDim.x + threadIdx.x;
+  if (i >= s.n) return;
+  const int8_t lab = s.label[i];
+  const_cast<int8_t *>(h.label)[i] = lab;  // the scratch set is writable
+  h.m[i] = s.m[i];
+  h.h[i] = s.h[i];
+  const double hdt = 0.5 * dt;
+  if (is_fluid(lab)) {
+    h.x[i] = s.x[i] + hdt * s.vx[i];
+    h.y[i] = s.y[i] + hdt * s.vy[i];
+    h.vx[i] = s.vx[i] + hdt * s.ax[i];
+    h.vy[i] = s.vy[i] + hdt * s.ay[i];
+    double rho = s.rho[i] + hdt * s.drho[i];
+    h.rho[i] = rho;
+  } else {
+    h.x[i] = s.x[i];
+    h.y[i] = s.y[i];
+    h.vx[i] = s.vx[i];
+    h.vy[i] = s.vy[i];
+    h.rho[i] = s.rho[i];
+  }
+}
+
+// state adjoint update of the step (see the top of the file); the *b arrays
+// hold the adjoint of S' on entry and that of S on exit; alphab accumulates
+__global__ void k_adj_post(const int8_t *__restrict__ label, long long n, double dt, double *xb, double *yb,
+                           double *vxb, double *vyb, double *rhob, double *axb, double *ayb, double *drhob,
+                           const double *xhb, const double *yhb, const double *vxhb, const double *vyhb,
+                           const double *rhohb, const double *alb, double *alphab) {
+  const long long i = (long long)blockIdx.x * blockDim.x + threadIdx.x;
+  if (i >= n) return;
+  alphab[i] += alb[i];
+  if (!is_fluid(label[i])) return;
+  const double hdt = 0.5 * dt;
+  const double vhx = vxhb[i] + dt * xb[i], vhy = vyhb[i] + dt * yb[i];
+  xb[i] += xhb[i];
+  yb[i] += yhb[i];
+  vxb[i] += hdt * xhb[i] + vhx;
+  vyb[i] += hdt * yhb[i] + vhy;
+  axb[i] = hdt * vhx;
+  ayb[i] = hdt * vhy;
+  rhob[i] += rhohb[i];
+  drhob[i] = hdt * rhohb[i];
+}
+
+// sum of v[0 .. n) in a fixed order (one block): deterministic
+__global__ void k_sum_fixed(const double *__restrict__ v, long long n, double *out) {
+  __shared__ double red[1024];
+  double s = 0.0;
+  for (long long i = threadIdx.x; i < n; i += blockDim.x) s += v[i];
+  red[threadIdx.x] = s;
+  __syncthreads();
+  for (int w = blockDim.x / 2; w > 0; w >>= 1) {
+    if ((int)threadIdx.x < w) red[threadIdx.x] += red[threadIdx.x + w];
+    __syncthreads();
+  }
+  if (threadIdx.x == 0) *out = red[0];
+}
+
+void launch_sum_fixed(const double *v, long long n, double *out, cudaStream_t st) {
+  k_sum_fixed<<<1, 1024, 0, st>>>(v, n, out);
+}
+
+void launch_adjoint_step(const StepArgs &s, const StepArgs &h, const WsPtrs &w, const sph_config_t &cfg,
+                         const sph_wcsph_t &wc, const sph_adjoint_t &adj, cudaStream_t st) {
+  const long long n = s.n;
+  const double dt = cfg.dt_fixed;
+  const unsigned nb = nblocks(n);
+  k_adj_pre<<<nb, kBlock, 0, st>>>(s.label, n, dt, adj.vxb, adj.vyb, adj.rhob, adj.axb, adj.ayb, adj.drhob, adj.lax,
+                                   adj.lay, adj.lad);
+  k_adj_half<<<nb, kBlock, 0, st>>>(s, h, dt);
+  // neighbour build and FP64 records of the half state (the forward's own passes)
+  launch_bounds(h, w, cfg, kStageNone, true, nullptr, nullptr, st);
+  launch_build(h, w, cfg, wc, st);
+  sph_config_t c64 = cfg;
+  c64.precision = SPH_PREC_FP64;
+  launch_records(h, w, c64, wc, true, false, false, st);
+  AdjPtrs P;
+  P.r64a = w.rec64a;
+  P.r64b = w.rec64b;
+  P.perm = w.perm;
+  P.keys_sorted = w.keys_sorted;
+  P.meta = w.meta;
+  P.cstart = w.cstart;
+  P.grid = w.grid;
+  P.ctrl = w.ctrl;
+  P.lax = adj.lax;
+  P.lay = adj.lay;
+  P.lad = adj.lad;
+  P.xhb = adj.xhb;
+  P.yhb = adj.yhb;
+  P.vxhb = adj.vxhb;
+  P.vyhb = adj.vyhb;
+  P.rhohb = adj.rhohb;
+  P.alb = adj.alb;
+  AdjParams ap;
+  ap.alpha = wc.alpha;
+  ap.beta = wc.beta;
+  ap.co = wc.co;
+  ap.r0 = wc.r0;
+  ap.D = wc.D;
+  ap.p1 = wc.p1;
+  ap.p2 = wc.p2;
+  ap.lj_42 = (wc.p1 == 4.0 && wc.p2 == 2.0) ? 1 : 0;
+  ap.gamma = wc.gamma;
+  ap.B = wc.B;
+  ap.inv_rho0 = 1.0 / wc.rho0;
+  ap.omega = adj.omega;
+  ap.wall_x = adj.wall_x;
+  ap.dt = dt;
+  ap.n = n;
+  const unsigned nbp = nblocks(n, kAdjBlock);
+  if (cfg.kernel == SPH_KERNEL_CUBIC) k_pair_adjoint<SPH_KERNEL_CUBIC><<<nbp, kAdjBlock, 0, st>>>(P, ap);
+  else k_pair_adjoint<SPH_KERNEL_GAUSSIAN><<<nbp, kAdjBlock, 0, st>>>(P, ap);
+  k_adj_post<<<nb, kBlock, 0, st>>>(s.label, n, dt, adj.xb, adj.yb, adj.vxb, adj.vyb, adj.rhob, adj.axb, adj.ayb,
+                                    adj.drhob, adj.xhb, adj.yhb, adj.vxhb, adj.vyhb, adj.rhohb, adj.alb, adj.alphab);
+}
+
+}  // namespace sph

@@ -263,7 +263,7 @@ int sph_nn_export(const sph_particles_t *pa, const sph_config_t *cfg, const sph_
 }
 
 static void compute_body(const StepArgs &a, const WsPtrs &w, const sph_wcsph_t &wc, const sph_config_t &cfg,
-                         double *dt_out, double *dt_hist, cudaStream_t st) {
+                         double *dt_out, double *dt_hist, cudaStream_t st, const WallLoad *wall = nullptr) {
   const bool do_dt = dt_out != nullptr || dt_hist != nullptr;
   launch_build(a, w, cfg, wc, st);
   launch_records(a, w, cfg, wc, true, false, do_dt, st);
@@ -271,7 +271,7 @@ static void compute_body(const StepArgs &a, const WsPtrs &w, const sph_wcsph_t &
     launch_sumdens(a, w, cfg, wc, st);
     launch_records(a, w, cfg, wc, false, true, false, st);
   }
-  launch_pair(a, w, cfg, wc, dt_out, dt_hist, st);
+  launch_pair(a, w, cfg, wc, dt_out, dt_hist, st, wall);
 }
 
 int sph_compute(sph_particles_t *pa, const sph_wcsph_t *w, const sph_config_t *cfg, const sph_workspace_t *ws,
@@ -338,6 +338,58 @@ int sph_run(sph_particles_t *pa, const sph_wcsph_t *w, const sph_config_t *cfg, 
     compute_body(a, wp, *w, *cfg, fixed ? nullptr : nxt, hist_next, st);
   }
   launch_correct(a, *cfg, ring + 3 * ((nsteps - 1) & 1), cfg->dt_fixed, st);
+  return check_launch();
+}
+
+// the differentiation form's constraints: fixed dt and h, PEC, FP64, no XSPH
+// or summation density
+static bool adjoint_config_ok(const sph_wcsph_t *w, const sph_config_t *cfg) {
+  return cfg->dt_fixed > 0.0 && cfg->h_fixed > 0.0 && cfg->integrator == SPH_INTEGRATOR_PEC &&
+         cfg->precision == SPH_PREC_FP64 && !w->use_xsph && !w->use_summation_density && !cfg->pec_use_xsph &&
+         cfg->damping == 0.0;
+}
+
+int sph_run_wall_load(sph_particles_t *pa, const sph_wcsph_t *w, const sph_config_t *cfg, const sph_workspace_t *ws,
+                      int64_t nsteps, double wall_x, double *fr, double *load_hist, sph_stream_t stream) {
+  if (!particles_ok(pa) || !w || !config_ok(cfg) || nsteps < 0 || !fr || !load_hist) return SPH_ERR_INVALID_ARGUMENT;
+  if (!adjoint_config_ok(w, cfg)) return SPH_ERR_INVALID_ARGUMENT;
+  int e = ws_ok(ws, pa->n);
+  if (e) return e;
+  if (pa->n == 0 || nsteps == 0) return SPH_OK;
+  cudaStream_t st = (cudaStream_t)stream;
+  StepArgs a = step_args(pa);
+  WsPtrs wp = ws_ptrs(ws);
+  double *ring = &wp.ctrl->dt_ring[0][0];
+  WallLoad wall;
+  wall.wall_x = wall_x;
+  wall.fr = fr;
+  if (cudaMemsetAsync(fr, 0, (size_t)pa->n * sizeof(double), st) != cudaSuccess) return SPH_ERR_CUDA;
+  for (int64_t s = 0; s < nsteps; s++) {
+    double *prev = ring + 3 * ((s + 1) & 1);
+    double *cur = ring + 3 * (s & 1);
+    launch_bounds(a, wp, *cfg, s == 0 ? kStagePredict : kStageCorrectPredict, true, prev, cur, st);
+    compute_body(a, wp, *w, *cfg, nullptr, nullptr, st, &wall);
+    launch_sum_fixed(fr, a.n, load_hist + s, st);
+  }
+  launch_correct(a, *cfg, ring + 3 * ((nsteps - 1) & 1), cfg->dt_fixed, st);
+  return check_launch();
+}
+
+int sph_adjoint_step(const sph_particles_t *pa, sph_particles_t *half, const sph_wcsph_t *w, const sph_config_t *cfg,
+                     const sph_workspace_t *ws, const sph_adjoint_t *adj, sph_stream_t stream) {
+  if (!particles_ok(pa) || !particles_ok(half) || half->n != pa->n || !w || !config_ok(cfg) || !adj)
+    return SPH_ERR_INVALID_ARGUMENT;
+  if (!adjoint_config_ok(w, cfg)) return SPH_ERR_INVALID_ARGUMENT;
+  const double *need[] = {adj->xb, adj->yb, adj->vxb, adj->vyb, adj->rhob, adj->axb, adj->ayb, adj->drhob,
+                          adj->alphab, adj->lax, adj->lay, adj->lad, adj->xhb, adj->yhb, adj->vxhb, adj->vyhb,
+                          adj->rhohb, adj->alb};
+  for (const double *q : need)
+    if (!q) return SPH_ERR_INVALID_ARGUMENT;
+  int e = ws_ok(ws, pa->n);
+  if (e) return e;
+  if (pa->n == 0) return SPH_OK;
+  cudaStream_t st = (cudaStream_t)stream;
+  launch_adjoint_step(step_args(const_cast<sph_particles_t *>(pa)), step_args(half), ws_ptrs(ws), *cfg, *w, *adj, st);
   return check_launch();
 }
 

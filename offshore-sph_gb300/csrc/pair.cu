@@ -46,94 +46,11 @@ struct PairParams {
   double cfl_c, cfl_f;
   int do_dt;
   long long n;
+  // wall load (FP64 form): fr[i] = -m_i x (x part of the Lennard-Jones
+  // acceleration from boundary neighbours at x >= wall_x), when fr != nullptr
+  double wall_x;
+  double *fr;
 };
-
-// Stencil of one query.  Mode 0: the reference's 3x3 cells around the
-// query's raw cell (validity as NNLinkedList._get_valid_cell_index); mode 1:
-// the own grid.  Cell ids are tiled (tiled_key), so the cells of one stencil
-// row are one contiguous range of sorted slots per tile they touch.  The key
-// of (x, y) splits into a row part and a column part; the column parts of the
-// segment bounds are the same for every row and are computed once.
-struct Stencil {
-  int y0, y1;          // rows, clipped (empty when y0 > y1)
-  int x0, x1;          // columns, clipped
-  int ca, cb, cc, cd;  // column parts: first segment [ca, cb), second [cc, cd)
-  int ts, ntlx;
-  bool multi;          // columns span more than two tiles
-  __device__ __forceinline__ static int colpart(int x, int ts) {
-    return ((x >> ts) << (2 * ts)) + (x & ((1 << ts) - 1));
-  }
-  __device__ __forceinline__ int rowpart(int y) const {
-    return (((y >> ts) * ntlx) << (2 * ts)) + ((y & ((1 << ts) - 1)) << ts);
-  }
-  __device__ __forceinline__ Stencil(const DevGrid &g, int2 qref, int qkey, int W) {
-    ts = g.ts;
-    ntlx = g.ntlx;
-    int cx, cy;
-    bool ok = true;
-    if (g.mode == 0) {
-      cx = qref.x;
-      cy = qref.y;
-    } else {
-      ok = qkey < g.ncells;
-      tiled_cell(qkey, ts, ntlx, cx, cy);
-    }
-    x0 = max(cx - W, 0);
-    x1 = min(cx + W, g.ntx - 1);
-    y0 = max(cy - W, 0);
-    y1 = min(cy + W, g.nty - 1);
-    if (!ok || x0 > x1) y1 = y0 - 1;
-    multi = (x1 >> ts) - (x0 >> ts) > 1;
-    const int xs = ((x0 >> ts) + 1) << ts;  // first column of the next tile
-    ca = colpart(x0, ts);
-    if (xs <= x1) {
-      cb = colpart(xs - 1, ts) + 1;
-      cc = colpart(xs, ts);
-      cd = colpart(x1, ts) + 1;
-    } else {
-      cb = colpart(x1, ts) + 1;
-      cc = cd = cb;
-    }
-  }
-};
-
-// visit(j) for every slot j of the stencil.  Each row is one loop over its
-// (at most two) segments, with the four bounds loaded up front, so that the
-// threads of a warp -- whose split points differ -- stay converged.  Columns
-// spanning more than two tiles (tiles narrower than the stencil) walk the
-// tiles one by one.
-template <class F>
-__device__ __forceinline__ void for_stencil(const Stencil &sten, const unsigned int *__restrict__ cstart,
-                                            F &&visit) {
-  if (!sten.multi) {
-    for (int yy = sten.y0; yy <= sten.y1; yy++) {
-      const unsigned int *c = cstart + sten.rowpart(yy);
-      const unsigned int s0 = __ldg(c + sten.ca), e0 = __ldg(c + sten.cb);
-      const unsigned int s1 = __ldg(c + sten.cc), e1 = __ldg(c + sten.cd);
-      // slots [s0, e0) then [s1, e1) as one uniform index range
-      const unsigned int jump = s1 - e0, jend = e0 + (e1 - s1);
-      for (unsigned int j = s0; j < jend; j++) visit(j >= e0 ? j + jump : j);
-    }
-  } else {
-    const int m = (1 << sten.ts) - 1;
-    for (int yy = sten.y0; yy <= sten.y1; yy++) {
-      const unsigned int *c = cstart + sten.rowpart(yy);
-      for (int xs = sten.x0; xs <= sten.x1; xs = (xs | m) + 1) {
-        const int xe = min(sten.x1, xs | m);
-        const unsigned int e = __ldg(c + Stencil::colpart(xe, sten.ts) + 1);
-        for (unsigned int j = __ldg(c + Stencil::colpart(xs, sten.ts)); j < e; j++) visit(j);
-      }
-    }
-  }
-}
-
-__device__ __forceinline__ bool in_ref_stencil(const int2 *__restrict__ meta, unsigned int j, const DevGrid &g,
-                                               int2 qref) {
-  const int2 mj = __ldg(&meta[j]);
-  int sx, sy;
-  storage_cell(mj.x, mj.y, g.ncx, sx, sy);
-  return abs(sx - qref.x) <= 1 && abs(sy - qref.y) <= 1;
-}
 
 // Exact size of the reference's neighbour set of a query whose own cell is
 // not in its stencil (x-overflow alias) or whose h is not positive; those are
@@ -369,7 +286,7 @@ __device__ __forceinline__ unsigned long long pair_query(const StepArgs &a, cons
       // accumulators: FP32 (mixed) or FP64
       MixedAcc acc;
       const MixedConsts mc = mixed_consts<KERNEL>(pp);
-      double dd = 0.0, dax = 0.0, day = 0.0, dbx = 0.0, dby = 0.0, dsx = 0.0, dsy = 0.0;
+      double dd = 0.0, dax = 0.0, day = 0.0, dbx = 0.0, dby = 0.0, dsx = 0.0, dsy = 0.0, dfr = 0.0;
 
       // ---- phase 2: pair physics over the list
       auto physics = [&](int cnt) {
@@ -434,6 +351,7 @@ __device__ __forceinline__ unsigned long long pair_query(const StepArgs &a, cons
               const double r2 = r * r;
               dbx += fac * dx / r2;
               dby += fac * dy / r2;
+              if (pp.fr && A.x >= pp.wall_x) dfr += fac * dx / r2;
             }
             if (XSPH) {
               const double fac = -pp.eps * mj * w / (0.5 * (rhoi + rhoj));
@@ -490,9 +408,11 @@ __device__ __forceinline__ unsigned long long pair_query(const StepArgs &a, cons
           ea = enc_d(accel2(axf, ayf));
           a.ax[i] = axf;
           a.ay[i] = ayf;
+          if (pp.fr) pp.fr[i] = -P.r64b[k].x * dfr;
         }
       } else {
         ea = enc_d(accel2(a.ax[i], a.ay[i]));  // keeps its previous values (SolverTools.py:150-153)
+        if (!MIXED && pp.fr) pp.fr[i] = 0.0;
       }
     }
   }
@@ -896,6 +816,8 @@ static PairPtrs pair_ptrs(const WsPtrs &w) {
 
 static PairParams pair_params(const StepArgs &a, const sph_config_t &cfg, const sph_wcsph_t &wc, bool do_dt) {
   PairParams pp;
+  pp.wall_x = 0.0;
+  pp.fr = nullptr;
   pp.alpha = wc.alpha; pp.beta = wc.beta; pp.co = wc.co; pp.eps = wc.epsilon;
   pp.r0 = wc.r0; pp.D = wc.D; pp.p1 = wc.p1; pp.p2 = wc.p2;
   pp.lj_42 = (wc.p1 == 4.0 && wc.p2 == 2.0) ? 1 : 0;
@@ -936,8 +858,12 @@ static void pair_dispatch(const StepArgs &a, const WsPtrs &w, const sph_config_t
 }
 
 void launch_pair(const StepArgs &a, const WsPtrs &w, const sph_config_t &cfg, const sph_wcsph_t &wc,
-                 double *dt_out, double *dt_hist, cudaStream_t st) {
+                 double *dt_out, double *dt_hist, cudaStream_t st, const WallLoad *wall) {
   PairParams pp = pair_params(a, cfg, wc, dt_out != nullptr || dt_hist != nullptr);
+  if (wall) {
+    pp.wall_x = wall->wall_x;
+    pp.fr = wall->fr;
+  }
   const bool xs = wc.use_xsph != 0, sd = wc.use_summation_density != 0;
   if (cfg.kernel == SPH_KERNEL_CUBIC) {
     if (xs) sd ? pair_dispatch<SPH_KERNEL_CUBIC, true, true>(a, w, cfg, pp, dt_out, dt_hist, st)

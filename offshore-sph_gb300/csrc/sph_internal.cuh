@@ -309,6 +309,93 @@ __device__ __forceinline__ void storage_cell(int cx, int cy, long long ncx, int 
   }
 }
 
+// Stencil of one query.  Mode 0: the reference's 3x3 cells around the
+// query's raw cell (validity as NNLinkedList._get_valid_cell_index); mode 1:
+// the own grid.  Cell ids are tiled (tiled_key), so the cells of one stencil
+// row are one contiguous range of sorted slots per tile they touch.  The key
+// of (x, y) splits into a row part and a column part; the column parts of the
+// segment bounds are the same for every row and are computed once.
+struct Stencil {
+  int y0, y1;          // rows, clipped (empty when y0 > y1)
+  int x0, x1;          // columns, clipped
+  int ca, cb, cc, cd;  // column parts: first segment [ca, cb), second [cc, cd)
+  int ts, ntlx;
+  bool multi;          // columns span more than two tiles
+  __device__ __forceinline__ static int colpart(int x, int ts) {
+    return ((x >> ts) << (2 * ts)) + (x & ((1 << ts) - 1));
+  }
+  __device__ __forceinline__ int rowpart(int y) const {
+    return (((y >> ts) * ntlx) << (2 * ts)) + ((y & ((1 << ts) - 1)) << ts);
+  }
+  __device__ __forceinline__ Stencil(const DevGrid &g, int2 qref, int qkey, int W) {
+    ts = g.ts;
+    ntlx = g.ntlx;
+    int cx, cy;
+    bool ok = true;
+    if (g.mode == 0) {
+      cx = qref.x;
+      cy = qref.y;
+    } else {
+      ok = qkey < g.ncells;
+      tiled_cell(qkey, ts, ntlx, cx, cy);
+    }
+    x0 = max(cx - W, 0);
+    x1 = min(cx + W, g.ntx - 1);
+    y0 = max(cy - W, 0);
+    y1 = min(cy + W, g.nty - 1);
+    if (!ok || x0 > x1) y1 = y0 - 1;
+    multi = (x1 >> ts) - (x0 >> ts) > 1;
+    const int xs = ((x0 >> ts) + 1) << ts;  // first column of the next tile
+    ca = colpart(x0, ts);
+    if (xs <= x1) {
+      cb = colpart(xs - 1, ts) + 1;
+      cc = colpart(xs, ts);
+      cd = colpart(x1, ts) + 1;
+    } else {
+      cb = colpart(x1, ts) + 1;
+      cc = cd = cb;
+    }
+  }
+};
+
+// visit(j) for every slot j of the stencil.  Each row is one loop over its
+// (at most two) segments, with the four bounds loaded up front, so that the
+// threads of a warp -- whose split points differ -- stay converged.  Columns
+// spanning more than two tiles (tiles narrower than the stencil) walk the
+// tiles one by one.
+template <class F>
+__device__ __forceinline__ void for_stencil(const Stencil &sten, const unsigned int *__restrict__ cstart,
+                                            F &&visit) {
+  if (!sten.multi) {
+    for (int yy = sten.y0; yy <= sten.y1; yy++) {
+      const unsigned int *c = cstart + sten.rowpart(yy);
+      const unsigned int s0 = __ldg(c + sten.ca), e0 = __ldg(c + sten.cb);
+      const unsigned int s1 = __ldg(c + sten.cc), e1 = __ldg(c + sten.cd);
+      // slots [s0, e0) then [s1, e1) as one uniform index range
+      const unsigned int jump = s1 - e0, jend = e0 + (e1 - s1);
+      for (unsigned int j = s0; j < jend; j++) visit(j >= e0 ? j + jump : j);
+    }
+  } else {
+    const int m = (1 << sten.ts) - 1;
+    for (int yy = sten.y0; yy <= sten.y1; yy++) {
+      const unsigned int *c = cstart + sten.rowpart(yy);
+      for (int xs = sten.x0; xs <= sten.x1; xs = (xs | m) + 1) {
+        const int xe = min(sten.x1, xs | m);
+        const unsigned int e = __ldg(c + Stencil::colpart(xe, sten.ts) + 1);
+        for (unsigned int j = __ldg(c + Stencil::colpart(xs, sten.ts)); j < e; j++) visit(j);
+      }
+    }
+  }
+}
+
+__device__ __forceinline__ bool in_ref_stencil(const int2 *__restrict__ meta, unsigned int j, const DevGrid &g,
+                                               int2 qref) {
+  const int2 mj = __ldg(&meta[j]);
+  int sx, sy;
+  storage_cell(mj.x, mj.y, g.ncx, sx, sy);
+  return abs(sx - qref.x) <= 1 && abs(sy - qref.y) <= 1;
+}
+
 // Tait EOS of one particle (TaitEOS.py:6-31) plus the background pressure
 // (WCSPH.py:131-149), FP64.  gamma == 7 uses repeated products.
 __device__ __forceinline__ double tait_p(double rho, int8_t label, double gamma, double B, double inv_rho0,
@@ -477,8 +564,17 @@ void launch_build(const StepArgs &a, const WsPtrs &w, const sph_config_t &cfg, c
 void launch_records(const StepArgs &a, const WsPtrs &w, const sph_config_t &cfg, const sph_wcsph_t &wc,
                     bool write_state, bool p_from_state, bool reduce_h, cudaStream_t st);
 // fused pair interaction; dt_out (ring slot) receives the next TimeStep
+// optional per-particle wall load of the FP64 pair kernel
+struct WallLoad {
+  double wall_x;  // boundary particles at x >= wall_x form the wall
+  double *fr;     // fr[i] = -m_i (Lennard-Jones acceleration of i from the wall).x
+};
 void launch_pair(const StepArgs &a, const WsPtrs &w, const sph_config_t &cfg, const sph_wcsph_t &wc,
-                 double *dt_out, double *dt_hist, cudaStream_t st);
+                 double *dt_out, double *dt_hist, cudaStream_t st,
+                 const WallLoad *wall = nullptr);
+void launch_sum_fixed(const double *v, long long n, double *out, cudaStream_t st);
+void launch_adjoint_step(const StepArgs &s, const StepArgs &h, const WsPtrs &w, const sph_config_t &cfg,
+                         const sph_wcsph_t &wc, const sph_adjoint_t &adj, cudaStream_t st);
 void launch_sumdens(const StepArgs &a, const WsPtrs &w, const sph_config_t &cfg, const sph_wcsph_t &wc,
                     cudaStream_t st);
 void launch_nn_count(const StepArgs &a, const WsPtrs &w, int64_t *counts, const int64_t *offsets, int64_t *idx,

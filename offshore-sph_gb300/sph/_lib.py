@@ -51,12 +51,20 @@ class Workspace(C.Structure):
     _fields_ = [("ptr", C.c_void_p), ("bytes", C.c_size_t), ("n_cap", C.c_int64), ("max_cells", C.c_int64)]
 
 
+ADJOINT_ARRAYS = ("xb", "yb", "vxb", "vyb", "rhob", "axb", "ayb", "drhob", "alphab",
+                  "lax", "lay", "lad", "xhb", "yhb", "vxhb", "vyhb", "rhohb", "alb")
+
+
+class Adjoint(C.Structure):
+    _fields_ = [(k, C.c_void_p) for k in ADJOINT_ARRAYS] + [("omega", C.c_double), ("wall_x", C.c_double)]
+
+
 #: every function include/sph_gb300.h declares
 EXPORTS = ("sph_abi_version", "sph_workspace_size", "sph_default_max_cells", "sph_workspace_init",
            "sph_get_status", "sph_status_string", "sph_initialize", "sph_eos", "sph_nn_update",
            "sph_nn_count", "sph_nn_export", "sph_compute", "sph_timestep", "sph_predict", "sph_correct",
            "sph_run", "sph_kernel_eval", "sph_kernel_grad", "sph_gauss_deriv", "sph_run_profiled",
-           "sph_compute_static")
+           "sph_compute_static", "sph_run_wall_load", "sph_adjoint_step")
 SPH_ERR_STATIC_LIMIT = 5
 STATIC_MAX_PARTICLES = 32768
 
@@ -101,6 +109,8 @@ def load():
         "sph_gauss_deriv": (C.c_int, [C.c_int64, vp, vp, vp, vp]),
         "sph_run_profiled": (C.c_int, [PP, WP, CP, WS, C.c_int64, C.POINTER(C.c_double), vp]),
         "sph_compute_static": (C.c_int, [PP, WP, CP, vp, vp]),
+        "sph_run_wall_load": (C.c_int, [PP, WP, CP, WS, C.c_int64, C.c_double, vp, vp, vp]),
+        "sph_adjoint_step": (C.c_int, [PP, PP, WP, CP, WS, C.POINTER(Adjoint), vp]),
     }
     for name, (res, args) in sig.items():
         f = getattr(L, name)

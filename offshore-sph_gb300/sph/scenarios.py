@@ -33,11 +33,12 @@ def _wall_rows(xs, ys, label):
 
 
 def dam_break(width=1.0, height=2.0, dx=0.025, tank_width=4.0, tank_height=3.0, rho0=1000.0,
-              layers=2, boundary_spacing=None):
+              layers=2, boundary_spacing=None, side="left"):
     """Fluid column ``width x height`` at lattice spacing ``dx`` (points at
     ((i+1/2) dx, (j+1/2) dx)), in a tank ``tank_width x tank_height`` with a
     floor and two side walls of ``layers`` boundary rows at ``dx/2`` spacing,
-    offset (k+1/2) dx/2 outside the fluid domain.
+    offset (k+1/2) dx/2 outside the fluid domain.  ``side="right"`` stands the
+    column against the right wall instead of the left one.
 
     Returns the particle array (fluid first, then floor, left, right wall).
     Fluid mass is rho0 dx^2; boundary m = rho = h = 0.
@@ -47,6 +48,8 @@ def dam_break(width=1.0, height=2.0, dx=0.025, tank_width=4.0, tank_height=3.0, 
     nfy = int(round(height / dx))
     fx = (np.arange(nfx) + 0.5) * dx
     fy = (np.arange(nfy) + 0.5) * dx
+    if side == "right":
+        fx = tank_width - width + fx
     fluid = _wall_rows(fx, fy, ParticleType.Fluid)
     fluid["m"] = rho0 * dx * dx
     fluid["rho"] = rho0
@@ -128,9 +131,11 @@ def cfg_dam_break_1m(dx=0.01):
     return dam_break(w, h, dx, 4.0 * w, 1.5 * h)
 
 
-def cfg_adjoint():
-    """20k-fluid dam break: 1.0 x 2.0 m column at dx = 0.01 in the 4 x 3 m tank."""
-    return dam_break(1.0, 2.0, 0.01, 4.0, 3.0)
+def cfg_adjoint(dx=0.01, width=1.0, height=2.0, tank_width=4.0, tank_height=3.0):
+    """20k-fluid dam break for the differentiation form: a 1.0 x 2.0 m column
+    at dx = 0.01 in the 4 x 3 m tank, standing against the RIGHT wall so that
+    the right wall carries a load from the first step."""
+    return dam_break(width, height, dx, tank_width, tank_height, side="right")
 
 
 def isclose_int(v):
