@@ -302,6 +302,82 @@ def replica_value(el, nfluid, steps, world, device):
     return el, world * nfluid * steps / el
 
 
+def adjoint_case(nsteps=200):
+    """The differentiation form's case: a 1.0 x 2.0 m column at dx = 0.01
+    (20k fluid) against the right wall of the 4 x 3 m tank, 200 PEC steps,
+    checkpoints every 20; loss = time integral of the load on the right wall.
+    Fixed dt = 5e-5 s: at 1e-4 s (Courant number 0.48 with co = 62.6 m/s and
+    h = 0.013) this configuration diverges after about 40 steps, on the GPU
+    and in the CPU restatement alike; the reference's own TimeStep would take
+    5.2e-5 s here."""
+    from sph import adjoint, scenarios
+    pa = scenarios.cfg_adjoint()
+    return adjoint.WallLoadCase(pa, height=2.0, r0=0.01, h=0.013, dt=5e-5, nsteps=nsteps, wall_x=4.0,
+                                checkpoint=20 if nsteps >= 100 else 10)
+
+
+def adjoint_cost(reps=3):
+    """Forward pass (loss only) and backward pass (replay + adjoint) of the
+    differentiation form, CUDA-event timed; gradient checks against central
+    differences (eps = 1e-6, FP64) along alpha and one random direction each
+    for the initial positions and velocities."""
+    import torch
+    from sph import adjoint
+    case = adjoint_case()
+    # a small seeded initial velocity field, N(0, 0.01 m/s) per component:
+    # at rest every pair sits on the kink of the artificial-viscosity switch
+    # (v_ij . x_ij = 0), where the loss has only one-sided derivatives
+    torch.manual_seed(3)
+    pos = case.positions()
+    vel = case.velocities() + 0.01 * torch.randn_like(pos)
+    a = torch.tensor(0.01, dtype=torch.float64, device="cuda", requires_grad=True)
+    p = pos.clone().requires_grad_(True)
+    v = vel.clone().requires_grad_(True)
+    torch.autograd.grad(adjoint.WallLoadLoss.apply(a, p, v, case), (a, p, v))  # warm-up
+    case.loss(0.01, pos, vel)
+    ev = [torch.cuda.Event(enable_timing=True) for _ in range(5)]
+    fwd, fwd_ckpt, bwd = [], [], []
+    for _ in range(reps):
+        torch.cuda.synchronize()
+        ev[0].record()
+        case.loss(0.01, pos, vel)
+        ev[1].record()
+        loss = adjoint.WallLoadLoss.apply(a, p, v, case)
+        ev[2].record()
+        ga, gp, gv = torch.autograd.grad(loss, (a, p, v))
+        ev[3].record()
+        torch.cuda.synchronize()
+        fwd.append(ev[0].elapsed_time(ev[1]))
+        fwd_ckpt.append(ev[1].elapsed_time(ev[2]))
+        bwd.append(ev[2].elapsed_time(ev[3]))
+    f, fc, b = float(np.median(fwd)), float(np.median(fwd_ckpt)), float(np.median(bwd))
+    torch.manual_seed(2)
+    dpos = torch.randn_like(pos)
+    dpos /= torch.linalg.norm(dpos)
+    dvel = torch.randn_like(vel)
+    dvel /= torch.linalg.norm(dvel)
+    checks = {"alpha": (ga.item(), adjoint.central_difference(case, 0.01, pos, vel, d_alpha=1.0)),
+              "v0_direction": ((gv * dvel).sum().item(),
+                               adjoint.central_difference(case, 0.01, pos, vel, d_vel=dvel)),
+              "x0_direction": ((gp * dpos).sum().item(),
+                               adjoint.central_difference(case, 0.01, pos, vel, d_pos=dpos))}
+    # over 200 steps the loss is kinked in x0 (pairs crossing the
+    # Lennard-Jones cutoff), so the x0 difference does not converge in eps;
+    # the same check over the first 50 steps does
+    short = adjoint_case(nsteps=50)
+    _, ga50, gp50, gv50 = adjoint.gradients(short, 0.01, pos, vel)
+    checks["x0_direction_50_steps"] = ((gp50 * dpos).sum().item(),
+                                       adjoint.central_difference(short, 0.01, pos, vel, d_pos=dpos))
+    checks["v0_direction_50_steps"] = ((gv50 * dvel).sum().item(),
+                                       adjoint.central_difference(short, 0.01, pos, vel, eps=1e-5, d_vel=dvel))
+    return {"case": "20k-fluid dam break against the right wall, v0 ~ N(0, 0.01 m/s), 200 PEC steps, dt=5e-5, "
+                    "FP64, checkpoints every 20",
+            "n_fluid": case.nf, "loss": loss.item(), "forward_ms": f, "forward_with_checkpoints_ms": fc,
+            "backward_ms": b, "backward_over_forward": b / f, "forward_plus_backward_over_forward": (fc + b) / f,
+            "fd_rel_err": {k: abs(g - d) / abs(d) for k, (g, d) in checks.items()},
+            "grad_vs_fd": {k: [g, d] for k, (g, d) in checks.items()}}
+
+
 def accuracy(names):
     """Mixed form against the GPU's own FP64 path (the oracle for the mixed
     form) from identical states: the per-step derivative error of one
@@ -358,9 +434,16 @@ def main():
     ap.add_argument("--no-extras", action="store_true", help="skip the FP64 / e2e / CPU / profile passes")
     ap.add_argument("--accuracy", default=None,
                     help="comma-separated workloads: mixed vs FP64 derivative and trajectory errors, then exit")
+    ap.add_argument("--adjoint", action="store_true",
+                    help="differentiation form only: adjoint/forward cost and finite-difference checks, then exit")
     args = ap.parse_args()
     if args.accuracy:
         accuracy(args.accuracy.split(","))
+        return
+    if args.adjoint:
+        from sph import build as sph_build
+        sph_build.build()
+        print(json.dumps(adjoint_cost()))
         return
     if args.warmup < 3:
         raise SystemExit("--warmup must be >= 3")
@@ -445,6 +528,9 @@ def main():
         out["e2e"] = {"value": nfluid * ke / el_e, "unit": UNIT, "h2d_bytes_per_step": h2d,
                       "d2h_bytes_per_step": d2h, "steps": ke}
         out["cpu_baseline"] = cpu_baseline(args.workload, wl)
+        del dp, ws
+        torch.cuda.empty_cache()
+        out["adjoint"] = adjoint_cost()
     if rank == 0:
         print(json.dumps(out))
     if world > 1:

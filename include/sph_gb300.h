@@ -150,8 +150,11 @@ int sph_workspace_init(sph_workspace_t *ws, sph_stream_t stream);
  * Synchronises the stream. */
 int sph_get_status(const sph_workspace_t *ws, uint32_t *status, sph_stream_t stream);
 
-/* Human-readable name of a return code or a single status bit. */
+/* Human-readable name of a return code (SPH_OK, SPH_ERR_*). */
 const char *sph_status_string(int code);
+
+/* Human-readable name of a single device status bit (SPH_STATUS_*). */
+const char *sph_status_bit_string(uint32_t bit);
 
 /* WCSPH.initialize + the fluid part of Solver.setup
  * (src/Methods/WCSPH.py:82-108, src/Solver.py:184-196): for fluid particles
@@ -283,11 +286,17 @@ int sph_run_wall_load(sph_particles_t *pa, const sph_wcsph_t *w, const sph_confi
  * step's d loss / d alpha contribution of particle i (sum it for the
  * gradient).  omega: the weight of this step's wall load in the loss (dt for
  * a time integral).  The remaining pointers are device scratch of n doubles
- * each; half is a scratch particle set of n particles (all fields). */
+ * each; half is a scratch particle set of n particles (all fields).
+ * reuse_build != 0: ws already holds the neighbour build and FP64 records
+ * of this step's evaluation (a copy of the workspace as sph_run_wall_load
+ * left it after running this one step); the step then skips its own build
+ * and does not touch half. */
 typedef struct sph_adjoint {
   double *xb, *yb, *vxb, *vyb, *rhob, *axb, *ayb, *drhob;
   double *alphab;
   double *lax, *lay, *lad, *xhb, *yhb, *vxhb, *vyhb, *rhohb, *alb;
+  int32_t reuse_build;
+  int32_t pad0;
   double omega;
   double wall_x;
 } sph_adjoint_t;

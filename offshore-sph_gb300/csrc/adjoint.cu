@@ -33,6 +33,7 @@
 namespace sph {
 
 constexpr int kAdjBlock = 128;
+constexpr int kAdjSplit = 1;  // lanes per query
 
 struct AdjParams {
   double alpha, beta, co, r0, D, p1, p2, gamma, B, inv_rho0;
@@ -57,16 +58,40 @@ __device__ __forceinline__ double dothr_drho(double rho, double othr, const AdjP
   return (dp - 2.0 * othr * rho) / (rho * rho);
 }
 
+// The adjoint needs about 1e-12 relative accuracy, not correct rounding, so
+// its reciprocals and square roots start from the FP32 hardware estimate
+// (reached through the integer-pipe truncating conversion) and take two
+// Newton-Raphson steps in FP64, each squaring the relative error:
+//   1/x:        y <- y + y (1 - x y)
+//   1/sqrt(x):  y <- y + y (1 - x y^2) / 2
+// (the FP64 pipe of GB300 issues few instructions per cycle; a correctly
+// rounded FP64 division or square root costs several times more).
+__device__ __forceinline__ double rcp_nr(double x) {
+  double y = f2d(__frcp_rn(d2f_trunc(x)));
+  double e = fma(-x, y, 1.0);
+  y = fma(y, e, y);
+  e = fma(-x, y, 1.0);
+  return fma(y, e, y);
+}
+__device__ __forceinline__ double rsqrt_nr(double x) {
+  double y = f2d(rsqrtf(d2f_trunc(x)));
+  double e = fma(-x * y, y, 1.0);
+  y = fma(0.5 * y, e, y);
+  e = fma(-x * y, y, 1.0);
+  return fma(0.5 * y, e, y);
+}
+
 // kernel gradient factor coef(r) (dW = coef * u) and its r-derivative, with
 // the reference's guards (CubicSpline.py:40-70, Gaussian.py:42-59)
+// (q = r / h, ih = 1 / h, ir = 1 / r; one reciprocal each per pair)
 template <int KERNEL>
-__device__ __forceinline__ void grad_coef(double r, double h, double &coef, double &dcoef) {
+__device__ __forceinline__ void grad_coef(double r, double q, double ih, double ir, double &coef, double &dcoef) {
   coef = 0.0;
   dcoef = 0.0;
-  const double q = r / h;
+  const double ih2 = ih * ih;
   if (KERNEL == SPH_KERNEL_CUBIC) {
     if (q > 2.0 || r < 1e-10) return;
-    const double al = kCubicFac / (h * h);
+    const double al = kCubicFac * ih2;
     double g, gp;
     if (q > 1.0) {
       const double t = 2.0 - q;
@@ -76,18 +101,18 @@ __device__ __forceinline__ void grad_coef(double r, double h, double &coef, doub
       g = -3.0 * q * (1.0 - 0.75 * q);
       gp = -3.0 + 4.5 * q;
     }
-    coef = al * g / (h * r);
-    dcoef = al / (h * r) * (gp / h - g / r);
+    const double a = al * ih * ir;
+    coef = a * g;
+    dcoef = a * (gp * ih - g * ir);
   } else {
-    if (!(q <= 3.0) || !(r * h > 1e-12)) return;
-    const double ac = kInvPi / (h * h);
-    const double e = exp(-q * q);
-    coef = -2.0 * ac * e / (h * h);
-    dcoef = coef * (-2.0 * r / (h * h));
+    if (!(q <= 3.0) || !(r > 1e-12 * ih)) return;
+    coef = -2.0 * kInvPi * ih2 * exp(-q * q) * ih2;
+    dcoef = coef * (-2.0 * r * ih2);
   }
 }
 
 struct AdjPtrs {
+  const float4 *rec0;  // FP32 positions and signed h (prefilter)
   const double4_32a *r64a, *r64b;
   const int *perm, *keys_sorted;
   const int2 *meta;
@@ -98,54 +123,80 @@ struct AdjPtrs {
   double *xhb, *yhb, *vxhb, *vyhb, *rhohb, *alb;  // outputs (caller order)
 };
 
+// the candidates of fluid query slot k that fall to lane `part`
 template <int KERNEL>
-__global__ void __launch_bounds__(kAdjBlock) k_pair_adjoint(AdjPtrs P, AdjParams ap) {
-  const long long k = (long long)blockIdx.x * blockDim.x + threadIdx.x;
-  if (k >= ap.n) return;
+__device__ __forceinline__ void adjoint_query(const AdjPtrs &P, const AdjParams &ap, long long k, int i,
+                                              unsigned int part, double &gx, double &gy, double &gvx, double &gvy,
+                                              double &grho, double &gal) {
   const DevGrid &g = *P.grid;
   const double4_32a Ak = P.r64a[k], Bk = P.r64b[k];
-  const int i = P.perm[k];
-  if (signbit(Bk.w)) {  // not fluid: no outputs, its adjoint is not used
-    P.xhb[i] = P.yhb[i] = P.vxhb[i] = P.vyhb[i] = P.rhohb[i] = P.alb[i] = 0.0;
-    return;
-  }
   const double xk = Ak.x, yk = Ak.y, vxk = Ak.z, vyk = Ak.w;
   const double mk = Bk.x, rhok = Bk.y, othrk = Bk.z, hk = Bk.w;
   const double lAxk = P.lax[i], lAyk = P.lay[i], lDk = P.lad[i];
   const double dothk = dothr_drho(rhok, othrk, ap);
+  const double ihk = 1.0 / hk;  // 1 / h_ij of pairs with h_j == h_k
   const double cbar = 0.5 * ap.co;
   const int2 qref = P.meta[k];
   const int qkey = P.keys_sorted[k];
   const bool slow = qref.x >= g.ncx || !(hk > 0.0);
   const int W = g.mode == 0 ? 1 : (slow ? g.wide : g.wt);
   const bool filter = g.mode == 1 && (g.need_filter || P.ctrl->alias_count > 0);
-  double gx = 0.0, gy = 0.0, gvx = 0.0, gvy = 0.0, grho = 0.0, gal = 0.0;
+  unsigned int cnt = 0;
+  // the forward's padded FP32 reach test: a candidate outside it contributes
+  // nothing (kernel support for fluid, min(r0, 3 h_ij) for boundary)
+  const float4 Qi = P.rec0[k];
+  const float hif = Qi.z, r0f = (float)ap.r0, pad = g.pad_e;
+  const float SK = (KERNEL == SPH_KERNEL_CUBIC ? 2.0f : 3.0f) * 1.000002f;
   const Stencil sten(g, qref, qkey, W);
   for_stencil(sten, P.cstart, [&](unsigned int j) {
+    if ((cnt++ % kAdjSplit) != part) return;
     if (j == (unsigned int)k) return;
     if (filter && !in_ref_stencil(P.meta, j, g, qref)) return;
+    {
+      const float4 qj = P.rec0[j];
+      const float fx = Qi.x - qj.x, fy = Qi.y - qj.y;
+      const float hijf = 0.5f * (hif + fabsf(qj.z));
+      float reach = SK * hijf;
+      if (signbit(qj.z)) reach = fmaxf(reach, fminf(r0f, 3.0f * hijf) * 1.000002f);
+      const float rp = reach + pad;
+      if (fx * fx + fy * fy > rp * rp) return;
+    }
     const double4_32a Aj = P.r64a[j], Bj = P.r64b[j];
     const double dx = xk - Aj.x, dy = yk - Aj.y;
-    const double r = __dsqrt_rn(__dadd_rn(__dmul_rn(dx, dx), __dmul_rn(dy, dy)));
-    const double hij = __dmul_rn(0.5, __dadd_rn(hk, fabs(Bj.w)));
-    if (!(__ddiv_rn(r, hij) <= 3.0)) return;  // the forward's neighbour test (NNLinkedList.py:74)
+    const double d2 = __dadd_rn(__dmul_rn(dx, dx), __dmul_rn(dy, dy));
+    if (!(d2 > 1e-24)) return;  // coincident: no kernel gradient, no boundary force
+    const double ir = rsqrt_nr(d2);
+    double r = d2 * ir;
+    const double hj = fabs(Bj.w);
+    const double hij = __dmul_rn(0.5, __dadd_rn(hk, hj));
+    // h_j == h_k (fluid pairs at a fixed h) and h_j == 0 (boundary) are exact
+    const double ih = hj == hk ? ihk : (hj == 0.0 ? 2.0 * ihk : rcp_nr(hij));
+    double q = r * ih;
+    // the forward's neighbour test q = r / h_ij <= 3 (NNLinkedList.py:74),
+    // redone with its correctly rounded operations where the estimate could
+    // decide differently
+    if (fabs(q - 3.0) < 1e-9) {
+      r = __dsqrt_rn(d2);
+      q = __ddiv_rn(r, hij);
+    }
+    if (!(q <= 3.0)) return;
     if (!signbit(Bj.w)) {
       // fluid pair: continuity + momentum with artificial viscosity
       const double mj = Bj.x, rhoj = Bj.y, othrj = Bj.z;
       const double vxij = vxk - Aj.z, vyij = vyk - Aj.w;
       double coef, dcoef;
-      grad_coef<KERNEL>(r, hij, coef, dcoef);
+      grad_coef<KERNEL>(r, q, ih, ir, coef, dcoef);
       if (coef == 0.0 && dcoef == 0.0) return;
       const double dWx = coef * dx, dWy = coef * dy;
       const double dot = vxij * dx + vyij * dy;
-      double Pi = 0.0, dPi_dmu = 0.0, mu = 0.0, den = 1.0, hb = 0.0;
-      const double rbar = 0.5 * (rhok + rhoj);
+      const double irbar = 2.0 * rcp_nr(rhok + rhoj);
+      double Pi = 0.0, dPi_dmu = 0.0, mu = 0.0, iden = 0.0, hb = 0.0;
       if (dot < 0.0) {
         hb = 0.5 * (hk + hij);
-        den = r * r + 0.01 * hb * hb;
-        mu = hb * dot / den;
-        Pi = mu * (ap.beta * mu - ap.alpha * cbar) / rbar;
-        dPi_dmu = (2.0 * ap.beta * mu - ap.alpha * cbar) / rbar;
+        iden = rcp_nr(d2 + 0.01 * hb * hb);
+        mu = hb * dot * iden;
+        Pi = mu * (ap.beta * mu - ap.alpha * cbar) * irbar;
+        dPi_dmu = (2.0 * ap.beta * mu - ap.alpha * cbar) * irbar;
       }
       const double S = othrk + othrj + Pi;
       const int pj = P.perm[j];
@@ -154,26 +205,25 @@ __global__ void __launch_bounds__(kAdjBlock) k_pair_adjoint(AdjPtrs P, AdjParams
       const double lC = mj * lDk + mk * lDj;
       const double lQdW = lQx * dWx + lQy * dWy;
       // (d dW / d u)^T z = coef z + dcoef (u . z) u / r
-      const double uq = dx * lQx + dy * lQy;
-      const double ir = 1.0 / r;
-      gx += S * (coef * lQx + dcoef * uq * dx * ir) + lC * (coef * vxij + dcoef * dot * dx * ir);
-      gy += S * (coef * lQy + dcoef * uq * dy * ir) + lC * (coef * vyij + dcoef * dot * dy * ir);
+      const double cq = S * dcoef * (dx * lQx + dy * lQy) * ir + lC * dcoef * dot * ir;
+      gx += S * coef * lQx + lC * coef * vxij + cq * dx;
+      gy += S * coef * lQy + lC * coef * vyij + cq * dy;
       gvx += lC * dWx;
       gvy += lC * dWy;
       if (dot < 0.0) {
-        const double f = lQdW * dPi_dmu * hb;
-        const double id2 = 1.0 / (den * den);
-        gx += f * (vxij / den - 2.0 * dot * dx * id2);
-        gy += f * (vyij / den - 2.0 * dot * dy * id2);
-        gvx += f * dx / den;
-        gvy += f * dy / den;
-        gal += -mj * (lAxk * dWx + lAyk * dWy) * (-mu * cbar / rbar);
+        const double f = lQdW * dPi_dmu * hb * iden;
+        const double c2 = 2.0 * dot * iden;
+        gx += f * (vxij - c2 * dx);
+        gy += f * (vyij - c2 * dy);
+        gvx += f * dx;
+        gvy += f * dy;
+        gal += mj * (lAxk * dWx + lAyk * dWy) * (mu * cbar * irbar);
       }
-      grho += lQdW * (dothk - 0.5 * Pi / rbar);
+      grho += lQdW * (dothk - 0.5 * Pi * irbar);  // d rbar / d rho_k = 1/2
     } else if (r <= ap.r0 && r > 1e-12) {
       // boundary pair: Lennard-Jones force b = D phi(r) u, phi = ((r0/r)^p1 - (r0/r)^p2) / r^2,
       // and the wall load -m_k b.x when j is on the loaded wall
-      const double s = ap.r0 / r;
+      const double s = ap.r0 * ir;
       double sp1, sp2;
       if (ap.lj_42) {
         sp2 = s * s;
@@ -182,21 +232,47 @@ __global__ void __launch_bounds__(kAdjBlock) k_pair_adjoint(AdjPtrs P, AdjParams
         sp1 = pow(s, ap.p1);
         sp2 = pow(s, ap.p2);
       }
-      const double r2 = r * r;
-      const double phi = (sp1 - sp2) / r2;
-      const double dphi = ((-ap.p1 - 2.0) * sp1 + (ap.p2 + 2.0) * sp2) / (r2 * r);
+      const double ir2 = ir * ir;
+      const double phi = (sp1 - sp2) * ir2;
+      const double dphi = ((-ap.p1 - 2.0) * sp1 + (ap.p2 + 2.0) * sp2) * ir2 * ir;
       const double zx = lAxk - ((ap.omega != 0.0 && Aj.x >= ap.wall_x) ? ap.omega * mk : 0.0), zy = lAyk;
-      const double uz = dx * zx + dy * zy;
-      gx += ap.D * (phi * zx + dphi * uz * dx / r);
-      gy += ap.D * (phi * zy + dphi * uz * dy / r);
+      const double c = dphi * (dx * zx + dy * zy) * ir;
+      gx += ap.D * (phi * zx + c * dx);
+      gy += ap.D * (phi * zy + c * dy);
     }
   });
-  P.xhb[i] = gx;
-  P.yhb[i] = gy;
-  P.vxhb[i] = gvx;
-  P.vyhb[i] = gvy;
-  P.rhohb[i] = grho;
-  P.alb[i] = gal;
+}
+
+template <int KERNEL>
+__global__ void __launch_bounds__(kAdjBlock, 2) k_pair_adjoint(AdjPtrs P, AdjParams ap) {
+  // kAdjSplit adjacent lanes share a query and take every kAdjSplit-th
+  // candidate of its stencil; their sums are combined with shuffles
+  const long long t = (long long)blockIdx.x * blockDim.x + threadIdx.x;
+  const long long k = t / kAdjSplit;
+  const unsigned int part = (unsigned int)(t % kAdjSplit);
+  double gx = 0.0, gy = 0.0, gvx = 0.0, gvy = 0.0, grho = 0.0, gal = 0.0;
+  int i = -1;
+  if (k < ap.n) {
+    i = P.perm[k];
+    if (!signbit(P.r64b[k].w)) adjoint_query<KERNEL>(P, ap, k, i, part, gx, gy, gvx, gvy, grho, gal);
+  }
+#pragma unroll
+  for (int o = 1; o < kAdjSplit; o <<= 1) {
+    gx += __shfl_xor_sync(0xffffffffu, gx, o);
+    gy += __shfl_xor_sync(0xffffffffu, gy, o);
+    gvx += __shfl_xor_sync(0xffffffffu, gvx, o);
+    gvy += __shfl_xor_sync(0xffffffffu, gvy, o);
+    grho += __shfl_xor_sync(0xffffffffu, grho, o);
+    gal += __shfl_xor_sync(0xffffffffu, gal, o);
+  }
+  if (i >= 0 && part == 0) {  // non-fluid particles get zeros: no outputs, their adjoint is not used
+    P.xhb[i] = gx;
+    P.yhb[i] = gy;
+    P.vxhb[i] = gvx;
+    P.vyhb[i] = gvy;
+    P.rhohb[i] = grho;
+    P.alb[i] = gal;
+  }
 }
 
 // lambda_A = dt vb' + ab', lambda_D = dt rhob' + drhob' (zero for non-fluid)
@@ -287,14 +363,17 @@ void launch_adjoint_step(const StepArgs &s, const StepArgs &h, const WsPtrs &w, 
   const unsigned nb = nblocks(n);
   k_adj_pre<<<nb, kBlock, 0, st>>>(s.label, n, dt, adj.vxb, adj.vyb, adj.rhob, adj.axb, adj.ayb, adj.drhob, adj.lax,
                                    adj.lay, adj.lad);
-  k_adj_half<<<nb, kBlock, 0, st>>>(s, h, dt);
-  // neighbour build and FP64 records of the half state (the forward's own passes)
-  launch_bounds(h, w, cfg, kStageNone, true, nullptr, nullptr, st);
-  launch_build(h, w, cfg, wc, st);
-  sph_config_t c64 = cfg;
-  c64.precision = SPH_PREC_FP64;
-  launch_records(h, w, c64, wc, true, false, false, st);
+  if (!adj.reuse_build) {
+    k_adj_half<<<nb, kBlock, 0, st>>>(s, h, dt);
+    // neighbour build and FP64 records of the half state (the forward's own passes)
+    launch_bounds(h, w, cfg, kStageNone, true, nullptr, nullptr, st);
+    launch_build(h, w, cfg, wc, st);
+    sph_config_t c64 = cfg;
+    c64.precision = SPH_PREC_FP64;
+    launch_records(h, w, c64, wc, true, false, false, st);
+  }
   AdjPtrs P;
+  P.rec0 = w.rec0;
   P.r64a = w.rec64a;
   P.r64b = w.rec64b;
   P.perm = w.perm;
@@ -328,7 +407,7 @@ void launch_adjoint_step(const StepArgs &s, const StepArgs &h, const WsPtrs &w, 
   ap.wall_x = adj.wall_x;
   ap.dt = dt;
   ap.n = n;
-  const unsigned nbp = nblocks(n, kAdjBlock);
+  const unsigned nbp = nblocks(n * kAdjSplit, kAdjBlock);
   if (cfg.kernel == SPH_KERNEL_CUBIC) k_pair_adjoint<SPH_KERNEL_CUBIC><<<nbp, kAdjBlock, 0, st>>>(P, ap);
   else k_pair_adjoint<SPH_KERNEL_GAUSSIAN><<<nbp, kAdjBlock, 0, st>>>(P, ap);
   k_adj_post<<<nb, kBlock, 0, st>>>(s.label, n, dt, adj.xb, adj.yb, adj.vxb, adj.vyb, adj.rhob, adj.axb, adj.ayb,

@@ -175,9 +175,12 @@ const char *sph_status_string(int code) {
     case SPH_ERR_CUDA: return "CUDA error";
     case SPH_ERR_NOT_INITIALISED: return "workspace not initialised";
     case SPH_ERR_STATIC_LIMIT: return "more particles than the static scratch of sph_compute_static holds";
-    default: break;
+    default: return "unknown";
   }
-  switch ((unsigned)code) {
+}
+
+const char *sph_status_bit_string(uint32_t bit) {
+  switch (bit) {
     case SPH_STATUS_CELL_OVERFLOW: return "cell id past the reference grid (reference writes out of bounds)";
     case SPH_STATUS_GRID_COARSENED: return "search grid coarsened to fit the cell capacity";
     case SPH_STATUS_NONFINITE: return "non-finite position or h";

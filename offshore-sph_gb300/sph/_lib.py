@@ -56,12 +56,13 @@ ADJOINT_ARRAYS = ("xb", "yb", "vxb", "vyb", "rhob", "axb", "ayb", "drhob", "alph
 
 
 class Adjoint(C.Structure):
-    _fields_ = [(k, C.c_void_p) for k in ADJOINT_ARRAYS] + [("omega", C.c_double), ("wall_x", C.c_double)]
+    _fields_ = [(k, C.c_void_p) for k in ADJOINT_ARRAYS] + [("reuse_build", C.c_int32), ("pad0", C.c_int32),
+                                                            ("omega", C.c_double), ("wall_x", C.c_double)]
 
 
 #: every function include/sph_gb300.h declares
 EXPORTS = ("sph_abi_version", "sph_workspace_size", "sph_default_max_cells", "sph_workspace_init",
-           "sph_get_status", "sph_status_string", "sph_initialize", "sph_eos", "sph_nn_update",
+           "sph_get_status", "sph_status_string", "sph_status_bit_string", "sph_initialize", "sph_eos", "sph_nn_update",
            "sph_nn_count", "sph_nn_export", "sph_compute", "sph_timestep", "sph_predict", "sph_correct",
            "sph_run", "sph_kernel_eval", "sph_kernel_grad", "sph_gauss_deriv", "sph_run_profiled",
            "sph_compute_static", "sph_run_wall_load", "sph_adjoint_step")
@@ -94,6 +95,7 @@ def load():
         "sph_workspace_init": (C.c_int, [WS, vp]),
         "sph_get_status": (C.c_int, [WS, C.POINTER(C.c_uint32), vp]),
         "sph_status_string": (C.c_char_p, [C.c_int]),
+        "sph_status_bit_string": (C.c_char_p, [C.c_uint32]),
         "sph_initialize": (C.c_int, [PP, WP, CP, vp]),
         "sph_eos": (C.c_int, [PP, WP, vp]),
         "sph_nn_update": (C.c_int, [PP, CP, WS, vp]),
@@ -130,4 +132,4 @@ def check(code, what="sph call"):
 
 def status_names(bits):
     L = load()
-    return [L.sph_status_string(1 << b).decode() for b in range(32) if bits & (1 << b)]
+    return [L.sph_status_bit_string(1 << b).decode() for b in range(32) if bits & (1 << b)]

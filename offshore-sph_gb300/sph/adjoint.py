@@ -14,9 +14,11 @@ horizontal force the fluid exerts on that wall.
 
 The forward pass runs the device step (``sph_run_wall_load``) and keeps a
 checkpoint of the state every ``checkpoint`` steps.  The backward pass
-replays each segment from its checkpoint, keeping the segment's states, and
-walks it in reverse with the hand-written adjoint step (``sph_adjoint_step``:
-the vector-Jacobian product of the fused pair evaluation and of PEC).
+replays each segment from its checkpoint, keeping a copy of the workspace
+after every replayed step (its neighbour build and FP64 records), and walks
+the segment in reverse with the hand-written adjoint step
+(``sph_adjoint_step``: the vector-Jacobian product of the fused pair
+evaluation and of PEC), which reuses those builds.
 The initial density is an input held fixed (it is not recomputed from
 perturbed positions), as are h and the boundary particles.
 """
@@ -27,17 +29,19 @@ import torch
 
 from . import _lib as L
 from . import core
+from .Common import FLOAT_FIELDS
 from .state import DeviceParticles, DeviceWorkspace, current_stream
 
 #: the state of a step: what sph_run leaves and the next step reads
 STATE_FIELDS = ("x", "y", "vx", "vy", "rho", "ax", "ay", "drho")
+_STATE_ROWS = [FLOAT_FIELDS.index(k) for k in STATE_FIELDS]
 
 
 class WallLoadCase:
     """A scenario for the differentiation form.
 
     pa: particle_dtype array (fluid and boundary); height, r0: WCSPH
-    constructor arguments; dx_h: the fixed h; dt: the fixed time step;
+    constructor arguments; h: the fixed h; dt: the fixed time step;
     wall_x: boundary particles at x >= wall_x form the loaded wall.
     """
 
@@ -61,6 +65,7 @@ class WallLoadCase:
         self.dp = DeviceParticles(self.n, device)
         self.half = DeviceParticles(self.n, device)
         self.fr = torch.zeros(self.n, dtype=torch.float64, device=device)
+        self._rows = torch.tensor(_STATE_ROWS, dtype=torch.int64, device=device)
 
     def wcsph(self, alpha):
         return core.wcsph_struct(self.height, self.r0, self.rho0, alpha=float(alpha))
@@ -101,11 +106,10 @@ class WallLoadCase:
             return self.dt * hist.sum()
 
     def snapshot(self, dp):
-        return torch.stack([dp.fields[k] for k in STATE_FIELDS]).clone()
+        return dp._buf[self._rows, :self.n]
 
     def restore(self, dp, snap):
-        for j, k in enumerate(STATE_FIELDS):
-            dp.fields[k].copy_(snap[j])
+        dp._buf[self._rows, :self.n] = snap
 
 
 class WallLoadLoss(torch.autograd.Function):
@@ -138,29 +142,29 @@ class WallLoadLoss(torch.autograd.Function):
         cs = L.Adjoint(**{k: A[k].data_ptr() for k in L.ADJOINT_ARRAYS})
         cs.omega = case.dt * float(g.item())
         cs.wall_x = case.wall_x
-        dp, st, half = case.dp, DeviceParticles(n, dev), case.half
-        st._buf.copy_(case.base._buf)
-        st.label.copy_(case.base.label)
-        scratch = torch.empty(case.checkpoint, dtype=torch.float64, device=dev)
+        cs.reuse_build = 1
+        dp, half = case.dp, case.half
         lib = L.load()
         K = case.checkpoint
+        w0 = case.ws.ws
         for seg in reversed(range(len(ctx.ckpts))):
             s0 = seg * K
             m = min(K, case.nsteps - s0)
-            # replay the segment, keeping the state in front of every step
+            # replay the segment; after each step the workspace holds that
+            # step's neighbour build and FP64 records, which its adjoint reuses
             dp._buf.copy_(case.base._buf)
             case.restore(dp, ctx.ckpts[seg])
-            states = []
+            builds = []
             for s in range(m):
-                states.append(case.snapshot(dp))
-                if s + 1 < m:
-                    case._run(dp, wc, 1, scratch)
+                # the same step without the wall-load output (the state is identical)
+                core.run(dp, wc, case.cfg, case.ws, 1)
+                builds.append(case.ws.buf.clone())
+            case.ws.check()
             for s in reversed(range(m)):
-                case.restore(st, states[s])
-                L.check(lib.sph_adjoint_step(core._P(st), core._P(half), C.byref(wc), C.byref(case.cfg),
-                                             C.byref(case.ws.ws), C.byref(cs), current_stream()),
-                        "sph_adjoint_step")
-        case.ws.check()
+                ws_s = L.Workspace(ptr=builds[s].data_ptr(), bytes=w0.bytes, n_cap=w0.n_cap, max_cells=w0.max_cells)
+                L.check(lib.sph_adjoint_step(core._P(case.base), core._P(half), C.byref(wc), C.byref(case.cfg),
+                                             C.byref(ws_s), C.byref(cs), current_stream()), "sph_adjoint_step")
+            del builds
         f = case.fluid
         galpha = A["alphab"].sum().reshape(())
         gpos = torch.stack((A["xb"][f], A["yb"][f]), 1)

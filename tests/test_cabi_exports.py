@@ -49,6 +49,8 @@ def test_host_only_calls(lib):
     assert lib.sph_workspace_size(-1, 0, C.byref(nbytes)) != 0
     assert lib.sph_default_max_cells(10) == 65536
     assert lib.sph_status_string(0) == b"ok"
+    assert b"non-finite" in lib.sph_status_bit_string(4)
+    assert b"coarsened" in lib.sph_status_bit_string(2)
     assert b"workspace" in lib.sph_status_string(2)
 
 

@@ -78,3 +78,62 @@ def test_adjoint_matches_central_differences(case):
         dvel /= torch.linalg.norm(dvel)
         fd = adjoint.central_difference(case, 0.01, pos, vel, eps=1e-6, d_vel=dvel)
         assert (gv * dvel).sum().item() == pytest.approx(fd, rel=1e-4)
+
+
+def test_full_size_case_against_torch_and_differences():
+    """The 20k-fluid case (1.0 x 2.0 m column at dx = 0.01 against the right
+    wall, 200 steps of 5e-5 s, checkpoints every 20): adjoint against torch
+    autograd (the unfused restatement holds ~30 GB of autograd state) and
+    against central differences along alpha."""
+    if not torch.cuda.is_available():
+        pytest.skip("no CUDA device")
+    import adjoint_ref
+    from sph import adjoint, build, scenarios
+    build.build()
+    big = adjoint.WallLoadCase(scenarios.cfg_adjoint(), height=2.0, r0=0.01, h=0.013, dt=5e-5, nsteps=200,
+                               wall_x=4.0, checkpoint=20)
+    # a small seeded velocity field keeps v_ij . x_ij away from 0, the kink of
+    # the artificial-viscosity switch (at rest every pair sits on it)
+    torch.manual_seed(3)
+    pos = big.positions()
+    vel = big.velocities() + 0.01 * torch.randn_like(pos)
+    loss, ga, gp, gv = adjoint.gradients(big, 0.01, pos, vel)
+    a = torch.tensor(0.01, dtype=torch.float64, device="cuda", requires_grad=True)
+    p = pos.clone().requires_grad_(True)
+    v = vel.clone().requires_grad_(True)
+    ref = adjoint_ref.reference_loss(big, a, p, v)
+    ra, rp, rv = torch.autograd.grad(ref, (a, p, v))
+    ref_value = ref.item()
+    del ref
+    torch.cuda.empty_cache()
+    assert loss.item() > 0.0
+    assert loss.item() == pytest.approx(ref_value, rel=1e-11)
+    # both are FP64 gradients of the same model; they differ by round-off
+    # (summation order, powers), which 200 steps of stiff wall contact
+    # amplify to ~1e-6 in the position gradient
+    assert _rel(ga, ra) <= 1e-8
+    assert _rel(gp, rp) <= 1e-5
+    assert _rel(gv, rv) <= 1e-5
+    fd = adjoint.central_difference(big, 0.01, pos, vel, eps=1e-6, d_alpha=1.0)
+    assert ga.item() == pytest.approx(fd, rel=1e-4)
+    torch.manual_seed(2)
+    dpos = torch.randn_like(pos)
+    dpos /= torch.linalg.norm(dpos)
+    dvel = torch.randn_like(vel)
+    dvel /= torch.linalg.norm(dvel)
+    fd = adjoint.central_difference(big, 0.01, pos, vel, eps=1e-6, d_vel=dvel)
+    assert (gv * dvel).sum().item() == pytest.approx(fd, rel=2e-4)
+    # over 200 steps the loss is kinked in the initial positions (pairs that
+    # cross the Lennard-Jones cutoff r0, where the force's slope jumps): the
+    # central difference scatters by ~1e-2 relative with eps (1e-4 .. 1e-8)
+    # and does not converge, so along positions it bounds the adjoint loosely
+    fd = adjoint.central_difference(big, 0.01, pos, vel, eps=1e-6, d_pos=dpos)
+    assert (gp * dpos).sum().item() == pytest.approx(fd, rel=5e-3)
+    # over 50 steps the differences converge: 1e-4 along both
+    short = adjoint.WallLoadCase(scenarios.cfg_adjoint(), height=2.0, r0=0.01, h=0.013, dt=5e-5, nsteps=50,
+                                 wall_x=4.0, checkpoint=10)
+    loss, ga, gp, gv = adjoint.gradients(short, 0.01, pos, vel)
+    fd = adjoint.central_difference(short, 0.01, pos, vel, eps=1e-6, d_pos=dpos)
+    assert (gp * dpos).sum().item() == pytest.approx(fd, rel=1e-4)
+    fd = adjoint.central_difference(short, 0.01, pos, vel, eps=1e-5, d_vel=dvel)
+    assert (gv * dvel).sum().item() == pytest.approx(fd, rel=1e-4)
