@@ -303,6 +303,41 @@ typedef struct sph_adjoint {
 int sph_adjoint_step(const sph_particles_t *pa, sph_particles_t *half, const sph_wcsph_t *w, const sph_config_t *cfg,
                      const sph_workspace_t *ws, const sph_adjoint_t *adj, sph_stream_t stream);
 
+/* ------------------------------------------------------------------------
+ * Batched form.  No reference counterpart (the reference runs one tank per
+ * Solver).  n_inst independent instances -- each a particle set the
+ * reference's Solver would run on its own, with its own WCSPH constants,
+ * fixed h and Courant dt -- live in one particle set, instance b in
+ * [offsets[b], offsets[b+1]).  Each step is one launch per stage over all
+ * instances (neighbour build, records, pair interaction, TimeStep, PEC), and
+ * instance b's results are those of a single-instance run of it with
+ * max_cells = sph_batch_instance_cells(...).  Mixed form, PEC, TimeStep dt,
+ * no XSPH or summation density.
+ * ------------------------------------------------------------------------ */
+
+/* Workspace bytes for n_total particles in n_inst instances (max_cells <= 0:
+ * a default of 8 cells per particle). */
+int sph_batch_workspace_size(int64_t n_total, int64_t n_inst, int64_t max_cells, size_t *bytes);
+
+/* Prepares ws (allocated with sph_batch_workspace_size and the same
+ * max_cells) for the instances: offsets (host, n_inst + 1), w and h_fixed
+ * (host, one per instance), cfg (shared settings).  tile_shift_max: the
+ * largest tile shift of the own-grid cell numbering (0..3; -1: default).
+ * Synchronises. */
+int sph_batch_setup(const sph_workspace_t *ws, int64_t n_inst, const int64_t *offsets, const sph_wcsph_t *w,
+                    const double *h_fixed, const sph_config_t *cfg, int32_t tile_shift_max, sph_stream_t stream);
+
+/* The cell capacity instance b gets inside ws (what a single-instance run
+ * of it must use to match the batched results bit for bit). */
+int64_t sph_batch_instance_cells(const sph_workspace_t *ws, int64_t n_inst, const int64_t *offsets, int64_t b);
+
+/* nsteps steps of every instance.  dt_hist (device, optional):
+ * nsteps x n_inst x 3 doubles {dt, dt_courant, dt_force}.  tile_blocks:
+ * resident blocks per SM of the pair tile kernel (<= 0: default).  No host
+ * synchronisation, so a sequence of calls can be captured in a CUDA graph. */
+int sph_batch_run(sph_particles_t *pa, const sph_config_t *cfg, const sph_workspace_t *ws, int64_t n_inst,
+                  int64_t nsteps, double *dt_hist, int32_t tile_blocks, sph_stream_t stream);
+
 #ifdef __cplusplus
 }
 #endif

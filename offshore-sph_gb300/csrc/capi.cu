@@ -82,6 +82,13 @@ __global__ void k_ctrl_init(DevCtrl *c) {
   c->initialised = 0x53504821u;
 }
 
+// zero cell counters, zero grid, control block at its identities
+void init_workspace(const WsPtrs &w, cudaStream_t st) {
+  cudaMemsetAsync(w.counts, 0, (size_t)(w.max_cells + 1) * 4, st);
+  cudaMemsetAsync(w.grid, 0, sizeof(DevGrid), st);
+  k_ctrl_init<<<1, 32, 0, st>>>(w.ctrl);
+}
+
 __global__ void k_fill_dt(double *dt_hist, long long nsteps, double dt) {
   long long s = (long long)blockIdx.x * blockDim.x + threadIdx.x;
   if (s >= nsteps) return;
@@ -144,11 +151,7 @@ int sph_workspace_init(sph_workspace_t *ws, sph_stream_t stream) {
   int e = ws_ok(ws, 0);
   if (e) return e;
   cudaStream_t st = (cudaStream_t)stream;
-  WsLayout L = make_layout(ws->n_cap, ws->max_cells);
-  WsPtrs p = ws_ptrs(ws);
-  if (cudaMemsetAsync(p.counts, 0, (size_t)(L.max_cells + 1) * 4, st) != cudaSuccess) return SPH_ERR_CUDA;
-  if (cudaMemsetAsync(p.grid, 0, sizeof(DevGrid), st) != cudaSuccess) return SPH_ERR_CUDA;
-  k_ctrl_init<<<1, 32, 0, st>>>(p.ctrl);
+  init_workspace(ws_ptrs(ws), st);
   if (check_launch()) return SPH_ERR_CUDA;
   return cudaStreamSynchronize(st) == cudaSuccess ? SPH_OK : SPH_ERR_CUDA;
 }

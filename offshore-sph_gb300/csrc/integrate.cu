@@ -43,9 +43,7 @@ __global__ void __launch_bounds__(kBlock) k_predict(StepArgs a, IntParams ip) {
 
 // PEC.correct (src/Integrators/PEC.py:61-89) or Euler.correct
 // (src/Integrators/Euler.py:17-27) on the fluid particles
-__global__ void __launch_bounds__(kBlock) k_correct(StepArgs a, IntParams ip) {
-  long long i = (long long)blockIdx.x * blockDim.x + threadIdx.x;
-  if (i >= a.n || !is_fluid(a.label[i])) return;
+__device__ __forceinline__ void correct_one(const StepArgs &a, long long i, const IntParams &ip) {
   const double dt = load_dt(ip);
   const double hdt = 0.5 * dt;
   const double ax = a.ax[i], ay = a.ay[i], drho = a.drho[i];
@@ -81,6 +79,12 @@ __global__ void __launch_bounds__(kBlock) k_correct(StepArgs a, IntParams ip) {
   if (ip.strict && rho < 0.0) rho = 0.0;
   a.rho[i] = rho;
   (void)hdt;
+}
+
+__global__ void __launch_bounds__(kBlock) k_correct(StepArgs a, IntParams ip) {
+  long long i = (long long)blockIdx.x * blockDim.x + threadIdx.x;
+  if (i >= a.n || !is_fluid(a.label[i])) return;
+  correct_one(a, i, ip);
 }
 
 static IntParams int_params(const sph_config_t &cfg, const double *dt, double dt_fixed) {
@@ -218,6 +222,98 @@ __global__ void __launch_bounds__(kBlock) k_kernel_map(int kernel, int what, lon
 void launch_kernel_map(int kernel, int what, long long n, const double *x, const double *r, const double *h,
                        double *out, cudaStream_t st) {
   k_kernel_map<<<nblocks(n), kBlock, 0, st>>>(kernel, what, n, x, r, h, out);
+}
+
+// ---------------------------------------------------------------------------
+// Batched form (see nn_build.cu): per-instance TimeStep and corrector.
+// ---------------------------------------------------------------------------
+// TimeStep's formulas (src/Equations/TimeStep.py:7-56) into dt3 = {dt, dt_c, dt_f};
+// returns status bits
+__device__ unsigned dt_from(double min_h, double max_c, double max_a2, unsigned int cnt, double cfl_c,
+                            double cfl_f, double *dt3) {
+  double dc = __ddiv_rn(__dmul_rn(cfl_c, min_h), max_c);
+  double df = max_a2 < 1e-12 ? 1e10 : __dmul_rn(cfl_f, __dsqrt_rn(__ddiv_rn(min_h, max_a2)));
+  double dt = (df < dc) ? df : dc;
+  unsigned st = 0;
+  if (cnt == 0) {
+    st |= SPH_STATUS_NO_FLUID;
+    dt = dc = df = nan("");
+  }
+  if (dt < 1e-6) st |= SPH_STATUS_SMALL_DT;
+  dt3[0] = dt;
+  dt3[1] = dc;
+  dt3[2] = df;
+  return st;
+}
+
+// the initial TimeStep's reductions per instance (min h, max c, max a^2 over fluid)
+__global__ void __launch_bounds__(kBlock) k_bt_timestep(StepArgs a, BatchPtrs B) {
+  const long long i = (long long)blockIdx.x * blockDim.x + threadIdx.x;
+  unsigned long long eh = kEncMinId, ec = kEncMinId, ea = kEncMinId;  // maxima as minima of the complement
+  unsigned int nf = 0;
+  int b = -1;
+  if (i < a.n) {
+    b = B.inst[i];
+    if (is_fluid(a.label[i])) {
+      const double ax = a.ax[i], ay = a.ay[i];
+      eh = enc_d(a.h[i]);
+      ec = ~enc_d(a.c[i]);
+      ea = ~enc_d(__dadd_rn(__dmul_rn(ax, ax), __dmul_rn(ay, ay)));
+      nf = 1;
+    }
+  }
+  InstSlots *sl = B.sl;
+  seg_min_u64(eh, b, [&](int q, unsigned long long m) { atomicMin(&sl[q].pd_hmin, m); });
+  seg_min_u64(ec, b, [&](int q, unsigned long long m) { atomicMax(&sl[q].ts_cmax, ~m); });
+  seg_min_u64(ea, b, [&](int q, unsigned long long m) { atomicMax(&sl[q].pd_a2max, ~m); });
+  seg_add_u32(nf, b, [&](int q, unsigned int c) { atomicAdd(&sl[q].pd_nfluid, c); });
+}
+
+// every instance's dt from its reductions into dt_ring[slot] (and dt_hist,
+// n_inst x 3, when given); the reductions return to their identities.
+// use_c: max c from the reduction (initial TimeStep), else co (the pair
+// pass's epilogue, where compute_speed_of_sound gives co to every particle)
+__global__ void k_bt_dt_finish(BatchPtrs B, DevCtrl *ctrl, int slot, double *dt_hist, int use_c) {
+  unsigned st = 0;
+  for (int b = threadIdx.x; b < B.n_inst; b += blockDim.x) {
+    InstSlots &s = B.sl[b];
+    const double min_h = dec_d(s.pd_hmin), max_a2 = dec_d(s.pd_a2max), max_c_r = dec_d(s.ts_cmax);
+    const unsigned int cnt = s.pd_nfluid;
+    s.pd_hmin = kEncMinId;
+    s.pd_a2max = kEncMaxId;
+    s.ts_cmax = kEncMaxId;
+    s.pd_nfluid = 0;
+    const InstParams &p = B.ip[b];
+    st |= dt_from(min_h, use_c ? max_c_r : p.pp.co, max_a2, cnt, p.cfl_c, p.cfl_f, s.dt_ring[slot]);
+    if (dt_hist) {
+      dt_hist[3 * b] = s.dt_ring[slot][0];
+      dt_hist[3 * b + 1] = s.dt_ring[slot][1];
+      dt_hist[3 * b + 2] = s.dt_ring[slot][2];
+    }
+  }
+  if (st) atomicOr(&ctrl->status, st);
+}
+
+__global__ void __launch_bounds__(kBlock) k_bt_correct(StepArgs a, BatchPtrs B, IntParams ip, int slot) {
+  const long long i = (long long)blockIdx.x * blockDim.x + threadIdx.x;
+  if (i >= a.n || !is_fluid(a.label[i])) return;
+  IntParams q = ip;
+  q.dt = B.sl[B.inst[i]].dt_ring[slot];
+  correct_one(a, i, q);
+}
+
+void launch_bt_timestep(const StepArgs &a, const WsPtrs &w, const BatchPtrs &B, int slot, double *dt_hist,
+                        cudaStream_t st) {
+  k_bt_timestep<<<nblocks(a.n), kBlock, 0, st>>>(a, B);
+  k_bt_dt_finish<<<1, 256, 0, st>>>(B, w.ctrl, slot, dt_hist, 1);
+}
+
+void launch_bt_dt_finish(const WsPtrs &w, const BatchPtrs &B, int slot, double *dt_hist, cudaStream_t st) {
+  k_bt_dt_finish<<<1, 256, 0, st>>>(B, w.ctrl, slot, dt_hist, 0);
+}
+
+void launch_bt_correct(const StepArgs &a, const BatchPtrs &B, const sph_config_t &cfg, int slot, cudaStream_t st) {
+  k_bt_correct<<<nblocks(a.n), kBlock, 0, st>>>(a, B, int_params(cfg, nullptr, 0.0), slot);
 }
 
 }  // namespace sph

@@ -114,13 +114,11 @@ __device__ __forceinline__ void integrate_front(const StepArgs &a, long long i, 
   a.rho[i] = rho;
 }
 
-__global__ void __launch_bounds__(kBlock) k_bounds(StepArgs a, DevCtrl *ctrl, BoundsParams bp) {
-  __shared__ unsigned long long red[kBlock / 32][6];
-  const long long i = (long long)blockIdx.x * blockDim.x + threadIdx.x;
-  // six minima; the maxima are taken as minima of the complement
-  unsigned long long v[6] = {kEncMinId, kEncMinId, kEncMinId, kEncMinId, kEncMinId, kEncMinId};
-  bool bad = false;
-  if (i < a.n) {
+// One particle's part of k_bounds: the integrator work in front of the build
+// and its six bound values (minima; maxima as minima of the complement).
+__device__ __forceinline__ void bounds_one(const StepArgs &a, long long i, const BoundsParams &bp,
+                                           unsigned long long (&v)[6], bool &bad) {
+  {
     const int8_t lab = a.label[i];
     double x = a.x[i], y = a.y[i];
     const double h = a.h[i];
@@ -144,6 +142,14 @@ __global__ void __launch_bounds__(kBlock) k_bounds(StepArgs a, DevCtrl *ctrl, Bo
       v[5] = ~enc_d(hn);
     }
   }
+}
+
+__global__ void __launch_bounds__(kBlock) k_bounds(StepArgs a, DevCtrl *ctrl, BoundsParams bp) {
+  __shared__ unsigned long long red[kBlock / 32][6];
+  const long long i = (long long)blockIdx.x * blockDim.x + threadIdx.x;
+  unsigned long long v[6] = {kEncMinId, kEncMinId, kEncMinId, kEncMinId, kEncMinId, kEncMinId};
+  bool bad = false;
+  if (i < a.n) bounds_one(a, i, bp, v, bad);
   if (__syncthreads_or(bad) && threadIdx.x == 0) atomicOr(&ctrl->status, (unsigned)SPH_STATUS_NONFINITE);
   const int lane = threadIdx.x & 31, wid = threadIdx.x >> 5;
 #pragma unroll
@@ -186,25 +192,14 @@ void launch_bounds(const StepArgs &a, const WsPtrs &w, const sph_config_t &cfg, 
   k_bounds<<<nblocks(a.n), kBlock, 0, st>>>(a, w.ctrl, bp);
 }
 
-struct GridParams {
-  double scale, r0;
-  int kernel;
-  long long max_cells;
-};
 
 // ---------------------------------------------------------------------------
 // Grid: the reference grid (NNLinkedList.py:86-127) and the traversal grid.
 // One thread; consumes and resets the bounds slots.
 // ---------------------------------------------------------------------------
-__global__ void k_grid(DevCtrl *ctrl, DevGrid *g, GridParams gp) {
-  if (threadIdx.x != 0 || blockIdx.x != 0) return;
-  double xmin = dec_d(ctrl->xmin), xmax = dec_d(ctrl->xmax);
-  double ymin = dec_d(ctrl->ymin), ymax = dec_d(ctrl->ymax);
-  double hmin = dec_d(ctrl->hmin_all), hmax = dec_d(ctrl->hmax_new);
-  ctrl->xmin = kEncMinId; ctrl->xmax = kEncMaxId; ctrl->ymin = kEncMinId; ctrl->ymax = kEncMaxId;
-  ctrl->hmin_all = kEncMinId; ctrl->hmax_new = kEncMaxId;
-  ctrl->alias_count = 0;
-  ctrl->tl_count = 0;
+// Both grids of one build from its bounds and h range; returns status bits.
+__device__ unsigned grid_setup(double xmin, double xmax, double ymin, double ymax, double hmin, double hmax,
+                               const GridParams &gp, DevGrid *g) {
   unsigned status = 0;
   bool fin = isfinite(xmin) && isfinite(xmax) && isfinite(ymin) && isfinite(ymax) && isfinite(hmin) &&
              isfinite(hmax);
@@ -259,7 +254,7 @@ __global__ void k_grid(DevCtrl *ctrl, DevGrid *g, GridParams gp) {
     return false;
   };
   int tsA = 0;
-  const bool fitsA = !huge && tile_fit((double)ncx, (double)ncy, SPH_TILE_SHIFT_REF, tsA);
+  const bool fitsA = !huge && tile_fit((double)ncx, (double)ncy, gp.ts_ref_max, tsA);
   if (!trunc_free && fitsA) {
     g->mode = 0;
     g->ntx = (int)ncx;
@@ -283,7 +278,7 @@ __global__ void k_grid(DevCtrl *ctrl, DevGrid *g, GridParams gp) {
     for (int it = 0; it < 64 && !fits; it++) {
       fnx = floor((xmax - xmin) / ct) + 1.0;
       fny = floor((ymax - ymin) / ct) + 1.0;
-      fits = tile_fit(fnx, fny, SPH_TILE_SHIFT_OWN, ts);
+      fits = tile_fit(fnx, fny, gp.ts_own_max, ts);
       if (!fits) {
         status |= SPH_STATUS_GRID_COARSENED;
         ct *= sqrt(fnx * fny / (double)gp.max_cells) * 1.05 + 1e-3;
@@ -308,27 +303,36 @@ __global__ void k_grid(DevCtrl *ctrl, DevGrid *g, GridParams gp) {
     g->wide = wd < 2 ? 2 : (wd > 1024 ? 1024 : wd);
   }
   g->valid = 1;
+  return status;
+}
+
+__global__ void k_grid(DevCtrl *ctrl, DevGrid *g, GridParams gp) {
+  if (threadIdx.x != 0 || blockIdx.x != 0) return;
+  const double xmin = dec_d(ctrl->xmin), xmax = dec_d(ctrl->xmax);
+  const double ymin = dec_d(ctrl->ymin), ymax = dec_d(ctrl->ymax);
+  const double hmin = dec_d(ctrl->hmin_all), hmax = dec_d(ctrl->hmax_new);
+  ctrl->xmin = kEncMinId; ctrl->xmax = kEncMaxId; ctrl->ymin = kEncMinId; ctrl->ymax = kEncMaxId;
+  ctrl->hmin_all = kEncMinId; ctrl->hmax_new = kEncMaxId;
+  ctrl->alias_count = 0;
+  ctrl->tl_count = 0;
+  const unsigned status = grid_setup(xmin, xmax, ymin, ymax, hmin, hmax, gp, g);
   if (status) atomicOr(&ctrl->status, status);
 }
 
 // ---------------------------------------------------------------------------
 // Keys: reference cell, traversal cell, histogram
 // ---------------------------------------------------------------------------
-__global__ void __launch_bounds__(kBlock) k_keys(const double *__restrict__ x, const double *__restrict__ y,
-                                                 long long n, const DevGrid *__restrict__ gp, DevCtrl *ctrl,
-                                                 int *__restrict__ keys, int2 *__restrict__ refcell,
-                                                 unsigned int *__restrict__ counts) {
-  long long i = (long long)blockIdx.x * blockDim.x + threadIdx.x;
-  bool alias = false, overflow = false;
-  if (i < n) {
-    const DevGrid &g = *gp;
-    const double xi = x[i], yi = y[i];
+// Traversal cell (tiled id; ncells = the dump cell) and raw reference cell of
+// the position (xi, yi) on grid g.
+__device__ __forceinline__ int cell_key(const DevGrid &g, double xi, double yi, int2 &ref, bool &alias,
+                                        bool &overflow) {
+  {
     const long long cx = ref_cell(xi, g.xmin, g.cs, g.inv_cs, g.xminf, g.inv_csf);
     const long long cy = ref_cell(yi, g.ymin, g.cs, g.inv_cs, g.yminf, g.inv_csf);
     const long long flat = cx + g.ncx * cy;
     overflow = !(cx >= 0 && cy >= 0 && flat < g.ncells_ref);
     alias = !overflow && cx == g.ncx;
-    refcell[i] = make_int2(sat_i32(cx), sat_i32(cy));
+    ref = make_int2(sat_i32(cx), sat_i32(cy));
     int key;
     if (overflow) {
       key = g.ncells;  // dump cell: never part of a stencil
@@ -347,6 +351,20 @@ __global__ void __launch_bounds__(kBlock) k_keys(const double *__restrict__ x, c
         key = tiled_key(min(max((int)floorf(tx), 0), g.ntx - 1), min(max((int)floorf(ty), 0), g.nty - 1), g.ts,
                         g.ntlx);
     }
+    return key;
+  }
+}
+
+__global__ void __launch_bounds__(kBlock) k_keys(const double *__restrict__ x, const double *__restrict__ y,
+                                                 long long n, const DevGrid *__restrict__ gp, DevCtrl *ctrl,
+                                                 int *__restrict__ keys, int2 *__restrict__ refcell,
+                                                 unsigned int *__restrict__ counts) {
+  long long i = (long long)blockIdx.x * blockDim.x + threadIdx.x;
+  bool alias = false, overflow = false;
+  if (i < n) {
+    int2 ref;
+    const int key = cell_key(*gp, x[i], y[i], ref, alias, overflow);
+    refcell[i] = ref;
     keys[i] = key;
     atomicAdd(&counts[key], 1u);
   }
@@ -515,6 +533,8 @@ void launch_build(const StepArgs &a, const WsPtrs &w, const sph_config_t &cfg, c
   gp.r0 = wc.r0;
   gp.kernel = cfg.kernel;
   gp.max_cells = w.max_cells;
+  gp.ts_ref_max = SPH_TILE_SHIFT_REF;
+  gp.ts_own_max = SPH_TILE_SHIFT_OWN;
   k_grid<<<1, 32, 0, st>>>(w.ctrl, w.grid, gp);
   unsigned nb = nblocks(a.n);
   k_keys<<<nb, kBlock, 0, st>>>(a.x, a.y, a.n, w.grid, w.ctrl, w.keys, w.refcell, w.counts);
@@ -531,14 +551,66 @@ void launch_build(const StepArgs &a, const WsPtrs &w, const sph_config_t &cfg, c
 // (SolverTools.py:122-127) are fused here; p, c and the fluid h go back to
 // the caller's arrays.
 // ---------------------------------------------------------------------------
-struct RecParams {
-  double h_fixed, gamma, B, inv_rho0, Pb, co;
-  float h_fixed_f, gamma_f, B_f, inv_rho0_f, rho0_hi, rho0_lo, Pb_f;
-  int h_fixed_on, Pb_on;
-  int write_state;   // write p, c, h to the caller's arrays
-  int from_state;    // p and h from the caller's arrays (second summation-density pass)
-  int reduce_h;      // min h over fluid for the step's TimeStep
-};
+
+// The mixed form's records of slot k (particle i): FP32 pair records, the h
+// reset and the Tait EOS on the relative density (no FP64 arithmetic); p, c
+// and the fluid h go back to the caller's arrays when asked.  eh / nf: the
+// fluid h for the TimeStep reduction.
+__device__ __forceinline__ void record_mixed(const StepArgs &a, long long k, int i, const RecParams &rp,
+                                             float4 *__restrict__ rec0, float4 *__restrict__ rec1,
+                                             float4 *__restrict__ rec2, unsigned long long &eh, unsigned int &nf) {
+  const int8_t lab = a.label[i];
+  const bool fl = is_fluid(lab);
+  const double m = a.m[i], rho = a.rho[i];
+  const double x = a.x[i], y = a.y[i];
+  float xh, xl, yh, yl;
+  split_df(x, xh, xl);
+  split_df(y, yh, yl);
+  const float mf = d2f_trunc(m);
+  // FP32 pair record; EOS on the relative density (no FP64 arithmetic)
+  float rh, rl;
+  split_df(rho, rh, rl);
+  float hf;
+  double hd;
+  if (rp.from_state || !fl) {
+    hd = a.h[i];
+    hf = d2f_trunc(hd);
+  } else if (rp.h_fixed_on) {
+    hd = rp.h_fixed;
+    hf = rp.h_fixed_f;
+  } else {
+    hf = rh > 1e-12f ? 1.3f * sqrtf(mf / rh) : 0.f;  // computeH in FP32
+    hd = f2d(hf);
+  }
+  float pf;  // gauge pressure B ((rho/rho0)^gamma - 1), FP32
+  double pd;
+  if (rp.from_state) {
+    pd = a.p[i];
+    pf = d2f_trunc(pd) - rp.Pb_f;
+  } else {
+    const float d = ((rh - rp.rho0_hi) + (rl - rp.rho0_lo)) * rp.inv_rho0_f;
+    pf = fl ? rp.B_f * tait_ratio_m1_f(d, rp.gamma_f) : 0.f;
+    pd = f2d(pf);
+    if (rp.Pb_on) pd += rp.Pb;
+  }
+  const float ir = rh != 0.f ? __frcp_rn(rh) : 0.f;
+  const float othr = (pf + rp.Pb_f) * ir * ir;
+  rec0[k] = make_float4(xh, yh, fl ? hf : -hf, mf);
+  rec1[k] = make_float4(xl, yl, rh, othr);
+  float vxh, vxl, vyh, vyl;
+  split_df(a.vx[i], vxh, vxl);
+  split_df(a.vy[i], vyh, vyl);
+  rec2[k] = make_float4(vxh, vyh, vxl, vyl);
+  if (rp.write_state) {
+    a.p[i] = pd;
+    a.c[i] = rp.co;
+    if (fl) a.h[i] = hd;
+  }
+  if (fl) {
+    eh = enc_d(hd);
+    nf = 1;
+  }
+}
 
 template <bool MIXED>
 __global__ void __launch_bounds__(kBlock) k_records(StepArgs a, const int *__restrict__ perm, RecParams rp,
@@ -562,49 +634,7 @@ __global__ void __launch_bounds__(kBlock) k_records(StepArgs a, const int *__res
     split_df(y, yh, yl);
     const float mf = d2f_trunc(m);
     if (MIXED) {
-      // FP32 pair record; EOS on the relative density (no FP64 arithmetic)
-      float rh, rl;
-      split_df(rho, rh, rl);
-      float hf;
-      double hd;
-      if (rp.from_state || !fl) {
-        hd = a.h[i];
-        hf = d2f_trunc(hd);
-      } else if (rp.h_fixed_on) {
-        hd = rp.h_fixed;
-        hf = rp.h_fixed_f;
-      } else {
-        hf = rh > 1e-12f ? 1.3f * sqrtf(mf / rh) : 0.f;  // computeH in FP32
-        hd = f2d(hf);
-      }
-      float pf;  // gauge pressure B ((rho/rho0)^gamma - 1), FP32
-      double pd;
-      if (rp.from_state) {
-        pd = a.p[i];
-        pf = d2f_trunc(pd) - rp.Pb_f;
-      } else {
-        const float d = ((rh - rp.rho0_hi) + (rl - rp.rho0_lo)) * rp.inv_rho0_f;
-        pf = fl ? rp.B_f * tait_ratio_m1_f(d, rp.gamma_f) : 0.f;
-        pd = f2d(pf);
-        if (rp.Pb_on) pd += rp.Pb;
-      }
-      const float ir = rh != 0.f ? __frcp_rn(rh) : 0.f;
-      const float othr = (pf + rp.Pb_f) * ir * ir;
-      rec0[k] = make_float4(xh, yh, fl ? hf : -hf, mf);
-      rec1[k] = make_float4(xl, yl, rh, othr);
-      float vxh, vxl, vyh, vyl;
-      split_df(a.vx[i], vxh, vxl);
-      split_df(a.vy[i], vyh, vyl);
-      rec2[k] = make_float4(vxh, vyh, vxl, vyl);
-      if (rp.write_state) {
-        a.p[i] = pd;
-        a.c[i] = rp.co;
-        if (fl) a.h[i] = hd;
-      }
-      if (fl) {
-        eh = enc_d(hd);
-        nf = 1;
-      }
+      record_mixed(a, k, i, rp, rec0, rec1, rec2, eh, nf);
     } else {
       // FP64 record, the reference's arithmetic
       double h = a.h[i];
@@ -674,6 +704,165 @@ void launch_records(const StepArgs &a, const WsPtrs &w, const sph_config_t &cfg,
   else
     k_records<false><<<nblocks(a.n), kBlock, 0, st>>>(a, w.perm, rp, w.ctrl, w.rec0, w.rec1, w.rec2, w.rec64a,
                                                       w.rec64b);
+}
+
+// ---------------------------------------------------------------------------
+// Batched form: many independent instances (tanks) in one particle set, each
+// with its own grid, constants, reductions and dt.  Every stage is one launch
+// over all instances.  Instance b's cells are the global ids
+// [coff[b], coff[b + 1]) (its dump cell last), so one counting sort over the
+// global ids sorts every instance at once and keeps each instance's slots in
+// its particle range.
+// ---------------------------------------------------------------------------
+__global__ void __launch_bounds__(kBlock) k_bt_bounds(StepArgs a, BatchPtrs B, BoundsParams bp, int prev, int cur,
+                                                      DevCtrl *ctrl) {
+  const long long i = (long long)blockIdx.x * blockDim.x + threadIdx.x;
+  unsigned long long v[6] = {kEncMinId, kEncMinId, kEncMinId, kEncMinId, kEncMinId, kEncMinId};
+  bool bad = false;
+  int b = -1;
+  if (i < a.n) {
+    b = B.inst[i];
+    BoundsParams bi = bp;
+    const RecParams &rp = B.ip[b].rp;
+    bi.h_fixed = rp.h_fixed;
+    bi.h_fixed_on = rp.h_fixed_on;
+    bi.dt_prev = B.sl[b].dt_ring[prev];
+    bi.dt_cur = B.sl[b].dt_ring[cur];
+    bounds_one(a, i, bi, v, bad);
+  }
+  if (__syncthreads_or(bad) && threadIdx.x == 0) atomicOr(&ctrl->status, (unsigned)SPH_STATUS_NONFINITE);
+  InstSlots *sl = B.sl;
+  seg_min_u64(v[0], b, [&](int q, unsigned long long m) { atomicMin(&sl[q].xmin, m); });
+  seg_min_u64(v[1], b, [&](int q, unsigned long long m) { atomicMax(&sl[q].xmax, ~m); });
+  seg_min_u64(v[2], b, [&](int q, unsigned long long m) { atomicMin(&sl[q].ymin, m); });
+  seg_min_u64(v[3], b, [&](int q, unsigned long long m) { atomicMax(&sl[q].ymax, ~m); });
+  seg_min_u64(v[4], b, [&](int q, unsigned long long m) { atomicMin(&sl[q].hmin_all, m); });
+  seg_min_u64(v[5], b, [&](int q, unsigned long long m) { atomicMax(&sl[q].hmax_new, ~m); });
+}
+
+// every instance's grids (one thread each), then the cell offsets
+__global__ void k_bt_grid(BatchPtrs B, DevCtrl *ctrl) {
+  unsigned status = 0;
+  for (int b = threadIdx.x; b < B.n_inst; b += blockDim.x) {
+    InstSlots &s = B.sl[b];
+    const double xmin = dec_d(s.xmin), xmax = dec_d(s.xmax), ymin = dec_d(s.ymin), ymax = dec_d(s.ymax);
+    const double hmin = dec_d(s.hmin_all), hmax = dec_d(s.hmax_new);
+    s.xmin = kEncMinId; s.xmax = kEncMaxId; s.ymin = kEncMinId; s.ymax = kEncMaxId;
+    s.hmin_all = kEncMinId; s.hmax_new = kEncMaxId;
+    s.alias_count = 0;
+    status |= grid_setup(xmin, xmax, ymin, ymax, hmin, hmax, B.ip[b].gp, &B.grids[b]);
+    B.coff[b] = B.grids[b].ncells + 1;  // its cells and its dump cell
+  }
+  if (status) atomicOr(&ctrl->status, status);
+  __syncthreads();
+  if (threadIdx.x == 0) {
+    int run = 0;
+    for (int b = 0; b < B.n_inst; b++) {
+      const int c = B.coff[b];
+      B.coff[b] = run;
+      run += c;
+    }
+    B.coff[B.n_inst] = run;
+    B.scan->ncells = run - 1;  // the scan kernels cover ids 0 .. run - 1
+    ctrl->tl_count = 0;
+  }
+}
+
+__global__ void __launch_bounds__(kBlock) k_bt_keys(const double *__restrict__ x, const double *__restrict__ y,
+                                                    long long n, BatchPtrs B, DevCtrl *ctrl, int *__restrict__ keys,
+                                                    int2 *__restrict__ refcell, unsigned int *__restrict__ counts) {
+  const long long i = (long long)blockIdx.x * blockDim.x + threadIdx.x;
+  bool alias = false, overflow = false;
+  if (i < n) {
+    const int b = B.inst[i];
+    int2 ref;
+    const int key = B.coff[b] + cell_key(B.grids[b], x[i], y[i], ref, alias, overflow);
+    refcell[i] = ref;
+    keys[i] = key;
+    atomicAdd(&counts[key], 1u);
+    if (alias) atomicAdd(&B.sl[b].alias_count, 1u);
+  }
+  const unsigned om = __ballot_sync(0xffffffffu, overflow);
+  if ((threadIdx.x & 31) == 0 && om) atomicOr(&ctrl->status, (unsigned)SPH_STATUS_CELL_OVERFLOW);
+}
+
+// k_cellsort with the tile list of every instance: entries (instance, tile)
+__global__ void __launch_bounds__(kBlock) k_bt_cellsort(const int *__restrict__ perm_tmp,
+                                                        const int *__restrict__ keys_sorted,
+                                                        const unsigned int *__restrict__ cstart,
+                                                        const int2 *__restrict__ refcell, long long n, BatchPtrs B,
+                                                        DevCtrl *ctrl, int *__restrict__ perm,
+                                                        int2 *__restrict__ meta) {
+  const long long k = (long long)blockIdx.x * blockDim.x + threadIdx.x;
+  if (k >= n) return;
+  const int key = keys_sorted[k];
+  const unsigned int s = cstart[key], e = cstart[key + 1];
+  const int v = perm_tmp[k];
+  unsigned int rank = 0;
+  for (unsigned int t = s; t < e; t++) rank += (unsigned)(perm_tmp[t] < v);
+  perm[s + rank] = v;
+  meta[s + rank] = refcell[v];
+  const int b = B.inst[v];
+  const int c0 = B.coff[b], lk = key - c0;
+  const DevGrid &g = B.grids[b];
+  const int ts2 = 2 * g.ts;
+  if (lk < g.ncells && (unsigned)k == __ldg(&cstart[c0 + ((lk >> ts2) << ts2)]))
+    B.tiles[atomicAdd(&ctrl->tl_count, 1u)] = make_int2(b, lk >> ts2);
+}
+
+// mixed-form records with each instance's constants; the TimeStep's min h
+// and fluid count per instance
+__global__ void __launch_bounds__(kBlock) k_bt_records(StepArgs a, const int *__restrict__ perm, BatchPtrs B,
+                                                       float4 *__restrict__ rec0, float4 *__restrict__ rec1,
+                                                       float4 *__restrict__ rec2) {
+  const long long k = (long long)blockIdx.x * blockDim.x + threadIdx.x;
+  unsigned long long eh = kEncMinId;
+  unsigned int nf = 0;
+  int b = -1;
+  if (k < a.n) {
+    const int i = perm[k];
+    b = B.inst[i];
+    record_mixed(a, k, i, B.ip[b].rp, rec0, rec1, rec2, eh, nf);
+  }
+  InstSlots *sl = B.sl;
+  seg_min_u64(eh, b, [&](int q, unsigned long long m) { atomicMin(&sl[q].pd_hmin, m); });
+  seg_add_u32(nf, b, [&](int q, unsigned int c) { atomicAdd(&sl[q].pd_nfluid, c); });
+}
+
+void launch_bt_bounds(const StepArgs &a, const WsPtrs &w, const BatchPtrs &B, const sph_config_t &cfg, int stage,
+                      int prev, int cur, cudaStream_t st) {
+  BoundsParams bp;
+  bp.stage = stage;
+  bp.euler = cfg.integrator == SPH_INTEGRATOR_EULER ? 1 : 0;
+  if (bp.euler && stage == kStagePredict) bp.stage = kStageNone;
+  bp.h_reset = 1;
+  bp.h_fixed = 0.0;
+  bp.h_fixed_on = 0;
+  bp.dt_fixed = 0.0;
+  bp.dt_fixed_on = 0;
+  bp.dt_prev = nullptr;
+  bp.dt_cur = nullptr;
+  bp.inv_damp = 1.0 / (1.0 + 0.5 * cfg.damping);
+  bp.c0 = 2.0 * bp.inv_damp - 1.0;
+  bp.damped = cfg.damping != 0.0 ? 1 : 0;
+  bp.use_xsph = cfg.pec_use_xsph;
+  bp.strict = cfg.pec_strict;
+  k_bt_bounds<<<nblocks(a.n), kBlock, 0, st>>>(a, B, bp, prev, cur, w.ctrl);
+}
+
+void launch_bt_build(const StepArgs &a, const WsPtrs &w, const BatchPtrs &B, cudaStream_t st) {
+  const unsigned nb = nblocks(a.n);
+  k_bt_grid<<<1, 256, 0, st>>>(B, w.ctrl);
+  k_bt_keys<<<nb, kBlock, 0, st>>>(a.x, a.y, a.n, B, w.ctrl, w.keys, w.refcell, w.counts);
+  k_scan_tiles<<<(unsigned)w.n_parts, kScanThreads, 0, st>>>(w.counts, B.scan, w.scan_part);
+  k_scan_top<<<1, 1024, 0, st>>>(w.scan_part, (int)w.n_parts);
+  k_scan_apply<<<(unsigned)w.n_parts, kScanThreads, 0, st>>>(w.counts, B.scan, w.scan_part, w.cstart);
+  k_scatter<<<nb, kBlock, 0, st>>>(w.keys, a.n, w.counts, w.cstart, w.perm_tmp, w.keys_sorted);
+  k_bt_cellsort<<<nb, kBlock, 0, st>>>(w.perm_tmp, w.keys_sorted, w.cstart, w.refcell, a.n, B, w.ctrl, w.perm, w.meta);
+}
+
+void launch_bt_records(const StepArgs &a, const WsPtrs &w, const BatchPtrs &B, cudaStream_t st) {
+  k_bt_records<<<nblocks(a.n), kBlock, 0, st>>>(a, w.perm, B, w.rec0, w.rec1, w.rec2);
 }
 
 }  // namespace sph

@@ -40,17 +40,6 @@ struct ListCap {
 #define SPH_PAIR_MIXED_BLOCKS 8
 #endif
 
-struct PairParams {
-  double alpha, beta, co, eps, r0, D, p1, p2;
-  int lj_42;  // p1 == 4 and p2 == 2
-  double cfl_c, cfl_f;
-  int do_dt;
-  long long n;
-  // wall load (FP64 form): fr[i] = -m_i x (x part of the Lennard-Jones
-  // acceleration from boundary neighbours at x >= wall_x), when fr != nullptr
-  double wall_x;
-  double *fr;
-};
 
 // Exact size of the reference's neighbour set of a query whose own cell is
 // not in its stencil (x-overflow alias) or whose h is not positive; those are
@@ -256,7 +245,9 @@ struct PairOcc {
 template <int KERNEL, bool XSPH, bool SUMDENS, bool MIXED>
 __device__ __forceinline__ unsigned long long pair_query(const StepArgs &a, const PairPtrs &P, const PairParams &pp,
                                                          const DevGrid &g, bool filter, long long k,
-                                                         unsigned int (*lists)[kPairBlock]) {
+                                                         unsigned int (*lists)[kPairBlock], int cell0 = 0) {
+  // cell0: global id of grid g's first cell (batched form)
+  const unsigned int *cst = P.cstart + cell0;
   constexpr int kListCap = ListCap<KERNEL>::value;
   const int tid = threadIdx.x;
   unsigned long long ea = kEncMaxId;
@@ -269,7 +260,7 @@ __device__ __forceinline__ unsigned long long pair_query(const StepArgs &a, cons
     if (!signbit(hif)) {
       const int i = P.perm[k];
       const int2 qref = P.meta[k];
-      const int qkey = P.keys_sorted[k];
+      const int qkey = P.keys_sorted[k] - cell0;
       const bool slow = qref.x >= g.ncx || !(hif > 0.f);
       const int W = g.mode == 0 ? 1 : (slow ? g.wide : g.wt);
       // query state
@@ -365,7 +356,7 @@ __device__ __forceinline__ unsigned long long pair_query(const StepArgs &a, cons
       // ---- phase 1: padded FP32 radius test, append to this thread's list
       const Stencil sten(g, qref, qkey, W);
       int nl = 0;
-      for_stencil(sten, P.cstart, [&](unsigned int j) {
+      for_stencil(sten, cst, [&](unsigned int j) {
         if (j == (unsigned int)k) return;  // the particle itself contributes zero
         if (filter && !in_ref_stencil(P.meta, j, g, qref)) return;
         const float4 qj = P.rec0[j];
@@ -394,7 +385,7 @@ __device__ __forceinline__ unsigned long long pair_query(const StepArgs &a, cons
           yi = a.y[i];
           hi = a.h[i];
         }
-        any = exact_count(a, P.perm, g, qref, qkey, W, g.mode == 1, P.meta, P.cstart, xi, yi, hi) > 0;
+        any = exact_count(a, P.perm, g, qref, qkey, W, g.mode == 1, P.meta, cst, xi, yi, hi) > 0;
       }
       if (any) {
         if (MIXED) {
@@ -622,34 +613,196 @@ __device__ __forceinline__ void fb_push(DevCtrl *ctrl, int2 *fb, unsigned int fb
   if (e < fb_cap) fb[e] = make_int2((int)s, (int)len);
 }
 
+// Geometry and constants of the grid a tile belongs to.
+struct TileGeom {
+  int ts, ntlx, ntx, nty, W, T, HW, HC;
+  int cell0;  // global id of the grid's first cell (batched form; 0 otherwise)
+  long long ncx;
+  float r0f, pad, hmaxf;
+};
+
+__device__ __forceinline__ TileGeom tile_geom(const DevGrid &g, double r0, int cell0) {
+  TileGeom tg;
+  tg.ts = g.ts;
+  tg.ntlx = g.ntlx;
+  tg.ntx = g.ntx;
+  tg.nty = g.nty;
+  tg.W = g.mode == 0 ? 1 : g.wt;
+  tg.T = 1 << g.ts;
+  tg.HW = tg.T + 2 * tg.W;
+  tg.HC = tg.HW * tg.HW;
+  tg.cell0 = cell0;
+  tg.ncx = g.ncx;
+  tg.r0f = (float)r0;
+  tg.pad = g.pad_e;
+  tg.hmaxf = g.hmaxf;
+  return tg;
+}
+
+// One tile (see above): stage its halo, run its queries.  Returns this
+// thread's largest encoded a^2 over its queries.  All threads of the block
+// call it together.
+template <int KERNEL, bool XSPH, bool SUMDENS>
+__device__ __forceinline__ unsigned long long tile_process(const StepArgs &a, const PairPtrs &P, const TileGeom &tg,
+                                                           const MixedConsts &mc, int t, float4 *h0, float4 *h1,
+                                                           float4 *h2, unsigned short (*lists)[kPairBlock],
+                                                           unsigned int *hoff, unsigned int *hgs, DevCtrl *ctrl,
+                                                           int2 *fb, unsigned int fb_cap) {
+  constexpr int kListCap = ListCap<KERNEL>::value;
+  const int tid = threadIdx.x;
+  const int ts = tg.ts, ntlx = tg.ntlx, W = tg.W, T = tg.T, HW = tg.HW, HC = tg.HC;
+  const unsigned int *cst = P.cstart + tg.cell0;  // this grid's cells
+  unsigned long long ea = kEncMaxId;
+  const unsigned int qs = __ldg(&cst[t << (2 * ts)]), qe = __ldg(&cst[(t + 1) << (2 * ts)]);
+  const int ox = (t % ntlx) * T - W, oy = (t / ntlx) * T - W;
+  // halo table: counts and first slots
+  for (int c = tid; c < HC; c += kPairBlock) {
+    const int x = ox + c % HW, y = oy + c / HW;
+    unsigned int gs = 0, cnt = 0;
+    if (x >= 0 && x < tg.ntx && y >= 0 && y < tg.nty) {
+      const int key = tiled_key(x, y, ts, ntlx);
+      gs = __ldg(&cst[key]);
+      cnt = __ldg(&cst[key + 1]) - gs;
+    }
+    hgs[c] = gs;
+    hoff[c] = cnt;
+  }
+  __syncthreads();
+  if (tid < 32) {  // exclusive scan of the counts, kHaloScanPer cells per lane
+    const int c0 = tid * kHaloScanPer;
+    unsigned int v[kHaloScanPer], sum = 0;
+#pragma unroll
+    for (int u = 0; u < kHaloScanPer; u++) {
+      v[u] = c0 + u < HC ? hoff[c0 + u] : 0u;
+      sum += v[u];
+    }
+    unsigned int inc = sum;
+#pragma unroll
+    for (int d = 1; d < 32; d <<= 1) {
+      const unsigned int o = __shfl_up_sync(0xffffffffu, inc, d);
+      if (tid >= d) inc += o;
+    }
+    unsigned int run = inc - sum;
+#pragma unroll
+    for (int u = 0; u < kHaloScanPer; u++) {
+      if (c0 + u < HC) hoff[c0 + u] = run;
+      run += v[u];
+    }
+    if (tid == 31) hoff[HC] = inc;
+  }
+  __syncthreads();
+  const unsigned int total = hoff[HC];
+  if (total > (unsigned)kHaloCap) {  // halo does not fit: global path
+    if (tid == 0)
+      for (unsigned int s = qs; s < qe; s += kPairBlock) fb_push(ctrl, fb, fb_cap, s, min((unsigned)kPairBlock, qe - s));
+    __syncthreads();
+    return ea;
+  }
+  // stage the halo's records: slot s belongs to the last cell whose offset is <= s
+  for (unsigned int s = tid; s < total; s += kPairBlock) {
+    int lo = 0, hi = HC;
+    while (hi - lo > 1) {
+      const int mid = (lo + hi) >> 1;
+      if (hoff[mid] <= s) lo = mid;
+      else hi = mid;
+    }
+    const unsigned int gsl = hgs[lo] + (s - hoff[lo]);
+    h0[s] = P.rec0[gsl];
+    h1[s] = P.rec1[gsl];
+    h2[s] = P.rec2[gsl];
+  }
+  __syncthreads();
+  // per-query candidate radius: the padded reach of the largest pair h
+  // (every |h| <= hmaxf), so that one compare per candidate suffices
+  const float SK = (KERNEL == SPH_KERNEL_CUBIC ? 2.0f : 3.0f) * 1.000002f;  // support / h, padded
+  for (unsigned int k = qs + tid; k < qe; k += kPairBlock) {
+    int cx, cy;
+    tiled_cell(P.keys_sorted[k] - tg.cell0, ts, ntlx, cx, cy);
+    const int hx = cx - ox, hy = cy - oy, hc = hy * HW + hx;
+    const unsigned int sq = hoff[hc] + (k - hgs[hc]);  // the query's own shared-memory slot
+    const float4 Qi = h0[sq];
+    const float hif = Qi.z;
+    if (signbit(hif)) continue;  // queries are fluid
+    if (P.meta[k].x >= tg.ncx || !(hif > 0.f)) {  // aliased query or h <= 0
+      fb_push(ctrl, fb, fb_cap, k, 1u);
+      continue;
+    }
+    const float4 Ri = h1[sq], Vi = h2[sq];
+    const int i = P.perm[k];
+    MixedAcc acc;
+    auto physics = [&](int cnt) {
+#pragma unroll kTileUnrollPairs
+      for (int u = 0; u < cnt; u++) {
+        const unsigned int j = lists[u][tid];
+        mixed_pair<KERNEL, XSPH, SUMDENS>(acc, mc, Qi, Ri, Vi, h0[j], h1[j], h2 + j);
+      }
+    };
+    const float hq = 0.5f * (hif + tg.hmaxf);
+    const float rq = fmaxf(SK * hq, fminf(tg.r0f, 3.0f * hq) * 1.000002f) + tg.pad;
+    const float rq2 = rq * rq;
+    int nl = 0;
+    for (int r = -W; r <= W; r++) {
+      const unsigned int *row = hoff + (hy + r) * HW + hx;
+      const unsigned int s1 = row[W + 1];
+#pragma unroll kTileUnrollCands
+      for (unsigned int j = row[-W]; j < s1; j++) {
+        const float4 qj = h0[j];
+        const float dx = Qi.x - qj.x, dy = Qi.y - qj.y;
+        if (fmaf(dx, dx, dy * dy) <= rq2 && j != sq) {  // j == sq: the particle itself contributes zero
+          lists[nl][tid] = (unsigned short)j;
+          if (++nl == kListCap) {
+            physics(nl);
+            nl = 0;
+          }
+        }
+      }
+    }
+    physics(nl);
+    const unsigned long long q = mixed_store<XSPH, SUMDENS>(acc, a, i);
+    ea = q > ea ? q : ea;
+  }
+  __syncthreads();
+  return ea;
+}
+
+// block-wide max of v in thread 0 (all threads call it)
+__device__ __forceinline__ unsigned long long block_max_u64(unsigned long long v, unsigned long long *red) {
+  const unsigned long long wm = warp_max_u64(v);
+  if ((threadIdx.x & 31) == 0) red[threadIdx.x >> 5] = wm;
+  __syncthreads();
+  unsigned long long b = kEncMaxId;
+  if (threadIdx.x == 0)
+    for (int w = 0; w < kPairBlock / 32; w++) b = red[w] > b ? red[w] : b;
+  __syncthreads();
+  return b;
+}
+
+// shared memory of the tile kernels
+template <int KERNEL>
+struct TileShared {
+  float4 h0[kHaloCap], h1[kHaloCap], h2[kHaloCap];  // rec0, rec1, rec2 of the halo
+  unsigned short lists[ListCap<KERNEL>::value][kPairBlock];
+  unsigned int hoff[kHaloCellsMax + 1];  // shared-memory offset of each halo cell, then the total
+  unsigned int hgs[kHaloCellsMax];       // its first sorted slot
+  int s_tile[2];                         // this and the next claimed tile (-1: none left)
+  int s_inst[2];                         // their instances (batched form)
+  unsigned long long red[kPairBlock / 32];
+};
+
 template <int KERNEL, bool XSPH, bool SUMDENS>
 __global__ void __launch_bounds__(kPairBlock, kTileBlocks)
     k_pair_tiles(StepArgs a, PairPtrs P, PairParams pp, const int *__restrict__ tiles, int2 *__restrict__ fb,
                  unsigned int fb_cap) {
-  constexpr int kListCap = ListCap<KERNEL>::value;
-  __shared__ float4 h0[kHaloCap], h1[kHaloCap], h2[kHaloCap];  // rec0, rec1, rec2 of the halo
-  __shared__ unsigned short lists[kListCap][kPairBlock];
-  __shared__ unsigned int hoff[kHaloCellsMax + 1];  // shared-memory offset of each halo cell, then the total
-  __shared__ unsigned int hgs[kHaloCellsMax];       // its first sorted slot
-  __shared__ int s_tile[2];                         // this and the next claimed tile (-1: none left)
-  __shared__ unsigned long long red[kPairBlock / 32];
+  __shared__ TileShared<KERNEL> sm;
   const int tid = threadIdx.x;
   DevCtrl *ctrl = P.ctrl;
   const DevGrid *gp = P.grid;
-  const int mode = gp->mode, ts = gp->ts, ntlx = gp->ntlx, ntx = gp->ntx, nty = gp->nty;
-  const long long ncx = gp->ncx;
-  const int W = mode == 0 ? 1 : gp->wt;
-  const int T = 1 << ts, HW = T + 2 * W, HC = HW * HW;
-  const bool filter = mode == 1 && (gp->need_filter || ctrl->alias_count > 0);
-  // per-query candidate radius: the padded reach of the largest pair h
-  // (every |h| <= hmaxf), so that one compare per candidate suffices
-  const float SK = (KERNEL == SPH_KERNEL_CUBIC ? 2.0f : 3.0f) * 1.000002f;  // support / h, padded
-  const float r0f = (float)pp.r0;
-  const float pad = gp->pad_e, hmaxf = gp->hmaxf;
+  const TileGeom tg = tile_geom(*gp, pp.r0, 0);
+  const bool filter = gp->mode == 1 && (gp->need_filter || ctrl->alias_count > 0);
   const MixedConsts mc = mixed_consts<KERNEL>(pp);
   unsigned long long ea = kEncMaxId;
 
-  if (filter || HC > kHaloCellsMax) {
+  if (filter || tg.HC > kHaloCellsMax) {
     // everything on the global path, in 128-slot chunks
     if (tid == 0) {
       const long long nch = (pp.n + kPairBlock - 1) / kPairBlock;
@@ -664,141 +817,121 @@ __global__ void __launch_bounds__(kPairBlock, kTileBlocks)
         for (unsigned int s = d0; s < d1; s += kPairBlock) fb_push(ctrl, fb, fb_cap, s, min((unsigned)kPairBlock, d1 - s));
       }
       const unsigned int c = atomicAdd(&ctrl->tile_next, 1u);
-      s_tile[0] = c < ntl ? tiles[c] : -1;
+      sm.s_tile[0] = c < ntl ? tiles[c] : -1;
     }
     __syncthreads();
     for (int it = 0;; it++) {
-      const int t = s_tile[it & 1];
+      const int t = sm.s_tile[it & 1];
       if (t < 0) break;
       if (tid == 0) {  // claim the next tile while this one runs
         const unsigned int c = atomicAdd(&ctrl->tile_next, 1u);
-        s_tile[(it + 1) & 1] = c < ntl ? tiles[c] : -1;
+        sm.s_tile[(it + 1) & 1] = c < ntl ? tiles[c] : -1;
       }
-      const unsigned int qs = __ldg(&P.cstart[t << (2 * ts)]), qe = __ldg(&P.cstart[(t + 1) << (2 * ts)]);
-      const int ox = (t % ntlx) * T - W, oy = (t / ntlx) * T - W;
-      // halo table: counts and first slots
-      for (int c = tid; c < HC; c += kPairBlock) {
-        const int x = ox + c % HW, y = oy + c / HW;
-        unsigned int gs = 0, cnt = 0;
-        if (x >= 0 && x < ntx && y >= 0 && y < nty) {
-          const int key = tiled_key(x, y, ts, ntlx);
-          gs = __ldg(&P.cstart[key]);
-          cnt = __ldg(&P.cstart[key + 1]) - gs;
-        }
-        hgs[c] = gs;
-        hoff[c] = cnt;
-      }
-      __syncthreads();
-      if (tid < 32) {  // exclusive scan of the counts, kHaloScanPer cells per lane
-        const int c0 = tid * kHaloScanPer;
-        unsigned int v[kHaloScanPer], sum = 0;
-#pragma unroll
-        for (int u = 0; u < kHaloScanPer; u++) {
-          v[u] = c0 + u < HC ? hoff[c0 + u] : 0u;
-          sum += v[u];
-        }
-        unsigned int inc = sum;
-#pragma unroll
-        for (int d = 1; d < 32; d <<= 1) {
-          const unsigned int o = __shfl_up_sync(0xffffffffu, inc, d);
-          if (tid >= d) inc += o;
-        }
-        unsigned int run = inc - sum;
-#pragma unroll
-        for (int u = 0; u < kHaloScanPer; u++) {
-          if (c0 + u < HC) hoff[c0 + u] = run;
-          run += v[u];
-        }
-        if (tid == 31) hoff[HC] = inc;
-      }
-      __syncthreads();
-      const unsigned int total = hoff[HC];
-      if (total > (unsigned)kHaloCap) {  // halo does not fit: global path
-        if (tid == 0)
-          for (unsigned int s = qs; s < qe; s += kPairBlock) fb_push(ctrl, fb, fb_cap, s, min((unsigned)kPairBlock, qe - s));
-        __syncthreads();
-        continue;
-      }
-      // stage the halo's records: slot s belongs to the last cell whose offset is <= s
-      for (unsigned int s = tid; s < total; s += kPairBlock) {
-        int lo = 0, hi = HC;
-        while (hi - lo > 1) {
-          const int mid = (lo + hi) >> 1;
-          if (hoff[mid] <= s) lo = mid;
-          else hi = mid;
-        }
-        const unsigned int gsl = hgs[lo] + (s - hoff[lo]);
-        h0[s] = P.rec0[gsl];
-        h1[s] = P.rec1[gsl];
-        h2[s] = P.rec2[gsl];
-      }
-      __syncthreads();
-      for (unsigned int k = qs + tid; k < qe; k += kPairBlock) {
-        int cx, cy;
-        tiled_cell(P.keys_sorted[k], ts, ntlx, cx, cy);
-        const int hx = cx - ox, hy = cy - oy, hc = hy * HW + hx;
-        const unsigned int sq = hoff[hc] + (k - hgs[hc]);  // the query's own shared-memory slot
-        const float4 Qi = h0[sq];
-        const float hif = Qi.z;
-        if (signbit(hif)) continue;  // queries are fluid
-        if (P.meta[k].x >= ncx || !(hif > 0.f)) {  // aliased query or h <= 0
-          fb_push(ctrl, fb, fb_cap, k, 1u);
-          continue;
-        }
-        const float4 Ri = h1[sq], Vi = h2[sq];
-        const int i = P.perm[k];
-        MixedAcc acc;
-        auto physics = [&](int cnt) {
-#pragma unroll kTileUnrollPairs
-          for (int u = 0; u < cnt; u++) {
-            const unsigned int j = lists[u][tid];
-            mixed_pair<KERNEL, XSPH, SUMDENS>(acc, mc, Qi, Ri, Vi, h0[j], h1[j], h2 + j);
-          }
-        };
-        const float hq = 0.5f * (hif + hmaxf);
-        const float rq = fmaxf(SK * hq, fminf(r0f, 3.0f * hq) * 1.000002f) + pad;
-        const float rq2 = rq * rq;
-        int nl = 0;
-        for (int r = -W; r <= W; r++) {
-          const unsigned int *row = hoff + (hy + r) * HW + hx;
-          const unsigned int s1 = row[W + 1];
-#pragma unroll kTileUnrollCands
-          for (unsigned int j = row[-W]; j < s1; j++) {
-            const float4 qj = h0[j];
-            const float dx = Qi.x - qj.x, dy = Qi.y - qj.y;
-            if (fmaf(dx, dx, dy * dy) <= rq2 && j != sq) {  // j == sq: the particle itself contributes zero
-              lists[nl][tid] = (unsigned short)j;
-              if (++nl == kListCap) {
-                physics(nl);
-                nl = 0;
-              }
-            }
-          }
-        }
-        physics(nl);
-        const unsigned long long q = mixed_store<XSPH, SUMDENS>(acc, a, i);
-        ea = q > ea ? q : ea;
-      }
-      __syncthreads();
+      const unsigned long long q = tile_process<KERNEL, XSPH, SUMDENS>(a, P, tg, mc, t, sm.h0, sm.h1, sm.h2, sm.lists,
+                                                                        sm.hoff, sm.hgs, ctrl, fb, fb_cap);
+      ea = q > ea ? q : ea;
     }
   }
   // this block's max a^2 (the list kernel finishes the TimeStep reduction);
   // the last block resets the tile counter
   if (pp.do_dt) {
-    const unsigned long long wm = warp_max_u64(ea);
-    if ((tid & 31) == 0) red[tid >> 5] = wm;
+    const unsigned long long ba = block_max_u64(ea, sm.red);
+    if (tid == 0 && ba != kEncMaxId) atomicMax(&ctrl->pd_a2max, ba);
   }
-  __syncthreads();
   if (tid == 0) {
-    if (pp.do_dt) {
-      unsigned long long ba = kEncMaxId;
-      for (int w = 0; w < kPairBlock / 32; w++) ba = red[w] > ba ? red[w] : ba;
-      if (ba != kEncMaxId) atomicMax(&ctrl->pd_a2max, ba);
-    }
     __threadfence();
     if (atomicAdd(&ctrl->tile_done, 1u) == gridDim.x - 1) {
       ctrl->tile_next = 0;
       ctrl->tile_done = 0;
+    }
+  }
+}
+
+// ---------------------------------------------------------------------------
+// Batched form: the tile kernel over the (instance, tile) list of all
+// instances, each tile with its instance's grid and constants, and the
+// fallback list with each entry's instance (see nn_build.cu).
+// ---------------------------------------------------------------------------
+template <int KERNEL, bool XSPH, bool SUMDENS>
+__global__ void __launch_bounds__(kPairBlock, kTileBlocks)
+    k_bt_pair_tiles(StepArgs a, PairPtrs P, BatchPtrs B, int2 *__restrict__ fb, unsigned int fb_cap) {
+  __shared__ TileShared<KERNEL> sm;
+  const int tid = threadIdx.x;
+  DevCtrl *ctrl = P.ctrl;
+  const unsigned int ntl = ctrl->tl_count;
+  if (tid == 0) {
+    if (blockIdx.x == 0)  // every instance's dump cell (reference-OOB particles) is in no tile
+      for (int b = 0; b < B.n_inst; b++) {
+        const int c = B.coff[b] + B.grids[b].ncells;
+        const unsigned int d0 = __ldg(&P.cstart[c]), d1 = __ldg(&P.cstart[c + 1]);
+        for (unsigned int s = d0; s < d1; s += kPairBlock) fb_push(ctrl, fb, fb_cap, s, min((unsigned)kPairBlock, d1 - s));
+      }
+    const unsigned int c = atomicAdd(&ctrl->tile_next, 1u);
+    const int2 e = c < ntl ? B.tiles[c] : make_int2(-1, -1);
+    sm.s_inst[0] = e.x;
+    sm.s_tile[0] = e.y;
+  }
+  __syncthreads();
+  for (int it = 0;; it++) {
+    const int t = sm.s_tile[it & 1], b = sm.s_inst[it & 1];
+    if (t < 0) break;
+    if (tid == 0) {  // claim the next tile while this one runs
+      const unsigned int c = atomicAdd(&ctrl->tile_next, 1u);
+      const int2 e = c < ntl ? B.tiles[c] : make_int2(-1, -1);
+      sm.s_inst[(it + 1) & 1] = e.x;
+      sm.s_tile[(it + 1) & 1] = e.y;
+    }
+    const DevGrid &g = B.grids[b];
+    const PairParams &pp = B.ip[b].pp;
+    const TileGeom tg = tile_geom(g, pp.r0, B.coff[b]);
+    const bool filter = g.mode == 1 && (g.need_filter || B.sl[b].alias_count > 0);
+    if (filter || tg.HC > kHaloCellsMax) {  // this instance's tiles go to the global path
+      if (tid == 0) {
+        const unsigned int *cst = P.cstart + tg.cell0;
+        const unsigned int qs = __ldg(&cst[t << (2 * tg.ts)]), qe = __ldg(&cst[(t + 1) << (2 * tg.ts)]);
+        for (unsigned int s = qs; s < qe; s += kPairBlock) fb_push(ctrl, fb, fb_cap, s, min((unsigned)kPairBlock, qe - s));
+      }
+      __syncthreads();
+      continue;
+    }
+    const MixedConsts mc = mixed_consts<KERNEL>(pp);
+    const unsigned long long ea = tile_process<KERNEL, XSPH, SUMDENS>(a, P, tg, mc, t, sm.h0, sm.h1, sm.h2, sm.lists,
+                                                                       sm.hoff, sm.hgs, ctrl, fb, fb_cap);
+    const unsigned long long ba = block_max_u64(ea, sm.red);
+    if (tid == 0 && ba != kEncMaxId) atomicMax(&B.sl[b].pd_a2max, ba);
+  }
+  if (tid == 0) {
+    __threadfence();
+    if (atomicAdd(&ctrl->tile_done, 1u) == gridDim.x - 1) {
+      ctrl->tile_next = 0;
+      ctrl->tile_done = 0;
+    }
+  }
+}
+
+template <int KERNEL, bool XSPH, bool SUMDENS>
+__global__ void __launch_bounds__(kPairBlock, kListBlocks)
+    k_bt_pair_list(StepArgs a, PairPtrs P, BatchPtrs B, const int2 *__restrict__ fb) {
+  __shared__ unsigned int lists[ListCap<KERNEL>::value][kPairBlock];
+  __shared__ unsigned long long red[kPairBlock / 32];
+  const unsigned int cnt = *(volatile unsigned int *)&P.ctrl->fb_count;
+  for (unsigned int e = blockIdx.x; e < cnt; e += gridDim.x) {
+    const int2 r = fb[e];
+    const int b = B.inst[P.perm[r.x]];  // an entry lies in one instance
+    const DevGrid &g = B.grids[b];
+    const PairParams &pp = B.ip[b].pp;
+    const bool filter = g.mode == 1 && (g.need_filter || B.sl[b].alias_count > 0);
+    unsigned long long ea = kEncMaxId;
+    if ((int)threadIdx.x < r.y)
+      ea = pair_query<KERNEL, XSPH, SUMDENS, true>(a, P, pp, g, filter, r.x + threadIdx.x, lists, B.coff[b]);
+    const unsigned long long ba = block_max_u64(ea, red);
+    if (threadIdx.x == 0 && ba != kEncMaxId) atomicMax(&B.sl[b].pd_a2max, ba);
+  }
+  if (threadIdx.x == 0) {
+    __threadfence();
+    if (atomicAdd(&P.ctrl->fb_done, 1u) == gridDim.x - 1) {
+      P.ctrl->fb_count = 0;
+      P.ctrl->fb_done = 0;
     }
   }
 }
@@ -896,6 +1029,27 @@ void launch_nn_count(const StepArgs &a, const WsPtrs &w, int64_t *counts, const 
                      cudaStream_t st) {
   k_nn_export<<<nblocks(a.n, kPairBlock), kPairBlock, 0, st>>>(a.x, a.y, a.h, a.n, w.perm, w.keys_sorted, w.meta,
                                                                w.cstart, w.grid, counts, offsets, idx);
+}
+
+template <int KERNEL, bool XSPH, bool SUMDENS>
+static void bt_pair_dispatch(const StepArgs &a, const WsPtrs &w, const BatchPtrs &B, int tile_blocks,
+                             cudaStream_t st) {
+  const int sms = sm_count();
+  k_bt_pair_tiles<KERNEL, XSPH, SUMDENS><<<sms * tile_blocks, kPairBlock, 0, st>>>(a, pair_ptrs(w), B, w.fb,
+                                                                                   (unsigned)w.fb_cap);
+  k_bt_pair_list<KERNEL, XSPH, SUMDENS><<<sms * kListBlocks, kPairBlock, 0, st>>>(a, pair_ptrs(w), B, w.fb);
+}
+
+void launch_bt_pair(const StepArgs &a, const WsPtrs &w, const BatchPtrs &B, int kernel, bool xsph, int tile_blocks,
+                    cudaStream_t st) {
+  if (tile_blocks < 1 || tile_blocks > kTileBlocks) tile_blocks = kTileBlocks;
+  if (kernel == SPH_KERNEL_CUBIC) {
+    if (xsph) bt_pair_dispatch<SPH_KERNEL_CUBIC, true, false>(a, w, B, tile_blocks, st);
+    else bt_pair_dispatch<SPH_KERNEL_CUBIC, false, false>(a, w, B, tile_blocks, st);
+  } else {
+    if (xsph) bt_pair_dispatch<SPH_KERNEL_GAUSSIAN, true, false>(a, w, B, tile_blocks, st);
+    else bt_pair_dispatch<SPH_KERNEL_GAUSSIAN, false, false>(a, w, B, tile_blocks, st);
+  }
 }
 
 }  // namespace sph

@@ -186,6 +186,95 @@ struct WsLayout {
 
 WsLayout make_layout(long long n_cap, long long max_cells);
 
+// ---------------------------------------------------------------------------
+// Per-call parameter blocks of the stages (one per instance in the batched
+// form).
+// ---------------------------------------------------------------------------
+struct GridParams {
+  double scale, r0;
+  int kernel;
+  long long max_cells;
+  int ts_ref_max, ts_own_max;  // largest tile shifts of the cell numbering
+};
+
+struct RecParams {
+  double h_fixed, gamma, B, inv_rho0, Pb, co;
+  float h_fixed_f, gamma_f, B_f, inv_rho0_f, rho0_hi, rho0_lo, Pb_f;
+  int h_fixed_on, Pb_on;
+  int write_state;   // write p, c, h to the caller's arrays
+  int from_state;    // p and h from the caller's arrays (second summation-density pass)
+  int reduce_h;      // min h over fluid for the step's TimeStep
+};
+
+struct PairParams {
+  double alpha, beta, co, eps, r0, D, p1, p2;
+  int lj_42;  // p1 == 4 and p2 == 2
+  double cfl_c, cfl_f;
+  int do_dt;
+  long long n;
+  // wall load (FP64 form): fr[i] = -m_i x (x part of the Lennard-Jones
+  // acceleration from boundary neighbours at x >= wall_x), when fr != nullptr
+  double wall_x;
+  double *fr;
+};
+
+// One instance of the batched form: its particle range, its stage
+// parameters, and its reductions and dt ring.
+struct InstParams {
+  long long off, n;
+  RecParams rp;
+  PairParams pp;
+  GridParams gp;
+  double cfl_c, cfl_f;
+};
+struct InstSlots {
+  unsigned long long xmin, xmax, ymin, ymax, hmin_all, hmax_new;  // bounds of the next build
+  unsigned long long pd_hmin, pd_a2max;                            // TimeStep of the next step
+  unsigned long long ts_cmax;                                      // initial TimeStep: max c
+  unsigned int pd_nfluid, alias_count;
+  double dt_ring[2][3];
+};
+struct BatchPtrs {
+  InstParams *ip;
+  InstSlots *sl;
+  DevGrid *grids;    // per instance
+  int *coff;         // first global cell id of each instance, then the total
+  int *inst;         // instance of each particle (caller order)
+  int2 *tiles;       // (instance, tile) of the non-empty tiles of the build
+  DevGrid *scan;     // ncells = total cells - 1, for the scan kernels
+  int n_inst;
+};
+
+// Reductions over a warp whose lanes may belong to different instances of
+// the batched form; lanes of one instance are contiguous (instance-major
+// order), b < 0 for lanes without a particle.  commit(b, value) applies the
+// atomic to instance b's slot.  Every lane of the warp must call.
+template <class F>
+__device__ __forceinline__ void seg_min_u64(unsigned long long v, int b, F &&commit) {
+  const int b0 = __shfl_sync(0xffffffffu, b, 0);
+  if (__all_sync(0xffffffffu, b == b0)) {
+    unsigned long long m = v;
+#pragma unroll
+    for (int o = 16; o > 0; o >>= 1) {
+      const unsigned long long t = __shfl_xor_sync(0xffffffffu, m, o);
+      m = t < m ? t : m;
+    }
+    if ((threadIdx.x & 31) == 0 && b0 >= 0 && m != kEncMinId) commit(b0, m);
+  } else if (b >= 0 && v != kEncMinId) {
+    commit(b, v);
+  }
+}
+template <class F>
+__device__ __forceinline__ void seg_add_u32(unsigned int v, int b, F &&commit) {
+  const int b0 = __shfl_sync(0xffffffffu, b, 0);
+  if (__all_sync(0xffffffffu, b == b0)) {
+    const unsigned int s = __reduce_add_sync(0xffffffffu, v);
+    if ((threadIdx.x & 31) == 0 && b0 >= 0 && s) commit(b0, s);
+  } else if (b >= 0 && v) {
+    commit(b, v);
+  }
+}
+
 // Sorted pair records (slot k = k-th particle in cell order):
 //   rec0  float4 (x_hi, y_hi, h, m)  x_hi, y_hi: FP64 position with its mantissa
 //                                    truncated to 24 bits; h with the sign bit

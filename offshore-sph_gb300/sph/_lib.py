@@ -65,7 +65,8 @@ EXPORTS = ("sph_abi_version", "sph_workspace_size", "sph_default_max_cells", "sp
            "sph_get_status", "sph_status_string", "sph_status_bit_string", "sph_initialize", "sph_eos", "sph_nn_update",
            "sph_nn_count", "sph_nn_export", "sph_compute", "sph_timestep", "sph_predict", "sph_correct",
            "sph_run", "sph_kernel_eval", "sph_kernel_grad", "sph_gauss_deriv", "sph_run_profiled",
-           "sph_compute_static", "sph_run_wall_load", "sph_adjoint_step")
+           "sph_compute_static", "sph_run_wall_load", "sph_adjoint_step", "sph_batch_workspace_size",
+           "sph_batch_setup", "sph_batch_instance_cells", "sph_batch_run")
 SPH_ERR_STATIC_LIMIT = 5
 STATIC_MAX_PARTICLES = 32768
 
@@ -113,6 +114,11 @@ def load():
         "sph_compute_static": (C.c_int, [PP, WP, CP, vp, vp]),
         "sph_run_wall_load": (C.c_int, [PP, WP, CP, WS, C.c_int64, C.c_double, vp, vp, vp]),
         "sph_adjoint_step": (C.c_int, [PP, PP, WP, CP, WS, C.POINTER(Adjoint), vp]),
+        "sph_batch_workspace_size": (C.c_int, [C.c_int64, C.c_int64, C.c_int64, C.POINTER(C.c_size_t)]),
+        "sph_batch_setup": (C.c_int, [WS, C.c_int64, C.POINTER(C.c_int64), WP, C.POINTER(C.c_double), CP,
+                                      C.c_int32, vp]),
+        "sph_batch_instance_cells": (C.c_int64, [WS, C.c_int64, C.POINTER(C.c_int64), C.c_int64]),
+        "sph_batch_run": (C.c_int, [PP, CP, WS, C.c_int64, C.c_int64, vp, C.c_int32, vp]),
     }
     for name, (res, args) in sig.items():
         f = getattr(L, name)

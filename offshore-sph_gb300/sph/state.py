@@ -84,6 +84,15 @@ class DeviceParticles:
         self._c = s
         return s
 
+    def cstruct_range(self, off, n):
+        """sph_particles_t of the particles [off, off + n)."""
+        s = L.Particles()
+        s.n = int(n)
+        s.label = self.label.data_ptr() + int(off)
+        for k in FLOAT_FIELDS:
+            setattr(s, k, self.fields[k].data_ptr() + 8 * int(off))
+        return s
+
 
 class DeviceWorkspace:
     """Scratch of the neighbour build and pair kernels (sph_workspace_t)."""
