@@ -378,6 +378,50 @@ def adjoint_cost(reps=3):
             "grad_vs_fd": {k: [g, d] for k, (g, d) in checks.items()}}
 
 
+def batch_bench(count=256, steps=50, warmup=5):
+    """The batched form: 256 seeded dam breaks (column width U(0.5, 2.0) m,
+    height U(1.0, 3.0) m, dx U(0.02, 0.05) m, tank 4x by 1.5x), mixed form,
+    every instance with its own Courant dt.  Autotunes, captures `steps`
+    steps in a CUDA graph and times its replays with CUDA events."""
+    import torch
+    from sph import batch, scenarios
+    cases = scenarios.ensemble(count=count, seed=1)
+    E = batch.Ensemble(cases)
+    nf = E.fluid_count()
+    E.run(warmup)
+    E.check()
+    t0 = time.perf_counter()
+    tune = E.autotune(steps=5, warmup=2)
+    tune_s = time.perf_counter() - t0
+    g = E.capture(steps)
+    g.replay()  # warm replay
+    torch.cuda.synchronize()
+    ev0, ev1 = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
+    reps = 3
+    ev0.record()
+    for _ in range(reps):
+        g.replay()
+    ev1.record()
+    torch.cuda.synchronize()
+    el = ev0.elapsed_time(ev1) / 1e3
+    E.check()
+    # the same steps launched eagerly, for the graph's effect
+    ev0.record()
+    E.run(steps)
+    ev1.record()
+    torch.cuda.synchronize()
+    el_eager = ev0.elapsed_time(ev1) / 1e3
+    sizes = [int(np.sum(pa["label"] == 0)) for pa, _ in cases]
+    best = min(tune, key=tune.get)
+    return {"case": "%d dam breaks, width U(0.5,2.0) m, height U(1.0,3.0) m, dx U(0.02,0.05) m, seed 1, "
+                    "mixed form, PEC, Courant 0.3 per instance" % count,
+            "instances": count, "n_particles": E.n, "n_fluid": nf, "fluid_per_instance": [min(sizes), max(sizes)],
+            "value": nf * steps * reps / el, "unit": UNIT, "ms_per_step": el / (steps * reps) * 1e3,
+            "eager_ms_per_step": el_eager / steps * 1e3, "graph_steps": steps,
+            "autotune": {"chosen": {"tile_shift": best[0], "tile_blocks_per_sm": best[1]},
+                         "ms_per_step": {"%d/%d" % k: v for k, v in sorted(tune.items())}, "seconds": tune_s}}
+
+
 def accuracy(names):
     """Mixed form against the GPU's own FP64 path (the oracle for the mixed
     form) from identical states: the per-step derivative error of one
@@ -434,6 +478,8 @@ def main():
     ap.add_argument("--no-extras", action="store_true", help="skip the FP64 / e2e / CPU / profile passes")
     ap.add_argument("--accuracy", default=None,
                     help="comma-separated workloads: mixed vs FP64 derivative and trajectory errors, then exit")
+    ap.add_argument("--batch", action="store_true",
+                    help="batched form only: 256-instance ensemble in a CUDA graph, then exit")
     ap.add_argument("--adjoint", action="store_true",
                     help="differentiation form only: adjoint/forward cost and finite-difference checks, then exit")
     args = ap.parse_args()
@@ -444,6 +490,11 @@ def main():
         from sph import build as sph_build
         sph_build.build()
         print(json.dumps(adjoint_cost()))
+        return
+    if args.batch:
+        from sph import build as sph_build
+        sph_build.build()
+        print(json.dumps(batch_bench()))
         return
     if args.warmup < 3:
         raise SystemExit("--warmup must be >= 3")
@@ -531,6 +582,8 @@ def main():
         del dp, ws
         torch.cuda.empty_cache()
         out["adjoint"] = adjoint_cost()
+        torch.cuda.empty_cache()
+        out["batched"] = batch_bench()
     if rank == 0:
         print(json.dumps(out))
     if world > 1:
