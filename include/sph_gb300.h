@@ -44,16 +44,18 @@ typedef struct CUstream_st *sph_stream_t; /* identical to cudaStream_t */
 /* particle labels (src/Common.py:8-12 ParticleType) */
 enum { SPH_FLUID = 0, SPH_BOUNDARY = 1, SPH_TEMP_BOUNDARY = 2, SPH_COUPLED = 3 };
 
-/* smoothing kernels (src/Kernels/CubicSpline.py, src/Kernels/Gaussian.py) */
-enum { SPH_KERNEL_CUBIC = 0, SPH_KERNEL_GAUSSIAN = 1 };
+/* smoothing kernels (src/Kernels/CubicSpline.py, src/Kernels/Gaussian.py,
+ * src/Kernels/Wendland.py) */
+enum { SPH_KERNEL_CUBIC = 0, SPH_KERNEL_GAUSSIAN = 1, SPH_KERNEL_WENDLAND = 2 };
 
 /* arithmetic of the pair interaction: FP64 throughout, or FP32 pair
  * arithmetic over FP64 state (positions, velocities, densities, dt and the
  * integrator stay FP64) */
 enum { SPH_PREC_FP64 = 0, SPH_PREC_MIXED = 1 };
 
-/* integrators (src/Integrators/PEC.py, src/Integrators/Euler.py) */
-enum { SPH_INTEGRATOR_PEC = 0, SPH_INTEGRATOR_EULER = 1 };
+/* integrators (src/Integrators/PEC.py, src/Integrators/Euler.py,
+ * src/Integrators/Verlet.py) */
+enum { SPH_INTEGRATOR_PEC = 0, SPH_INTEGRATOR_EULER = 1, SPH_INTEGRATOR_VERLET = 2 };
 
 /* host-side return codes */
 enum {

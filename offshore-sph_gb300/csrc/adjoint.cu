@@ -104,6 +104,16 @@ __device__ __forceinline__ void grad_coef(double r, double q, double ih, double 
     const double a = al * ih * ir;
     coef = a * g;
     dcoef = a * (gp * ih - g * ir);
+  } else if (KERNEL == SPH_KERNEL_WENDLAND) {
+    // g(q) = (1 - q/2)^5 (-14/3) q (1 + 2.5 q) (Wendland.py:58-60)
+    if (q >= 2.0 || r < 1e-10) return;
+    const double al = kWendFac * ih2;
+    const double in = 1.0 - 0.5 * q, in2 = in * in, in4 = in2 * in2;
+    const double g = in4 * in * (-14.0 / 3.0) * q * (1.0 + 2.5 * q);
+    const double gp = (-14.0 / 3.0) * (in4 * in * (1.0 + 5.0 * q) - 2.5 * in4 * q * (1.0 + 2.5 * q));
+    const double a = al * ih * ir;
+    coef = a * g;
+    dcoef = a * (gp * ih - g * ir);
   } else {
     if (!(q <= 3.0) || !(r > 1e-12 * ih)) return;
     coef = -2.0 * kInvPi * ih2 * exp(-q * q) * ih2;
@@ -146,7 +156,7 @@ __device__ __forceinline__ void adjoint_query(const AdjPtrs &P, const AdjParams 
   // nothing (kernel support for fluid, min(r0, 3 h_ij) for boundary)
   const float4 Qi = P.rec0[k];
   const float hif = Qi.z, r0f = (float)ap.r0, pad = g.pad_e;
-  const float SK = (KERNEL == SPH_KERNEL_CUBIC ? 2.0f : 3.0f) * 1.000002f;
+  const float SK = (float)Support<KERNEL>::q * 1.000002f;
   const Stencil sten(g, qref, qkey, W);
   for_stencil(sten, P.cstart, [&](unsigned int j) {
     if ((cnt++ % kAdjSplit) != part) return;
@@ -409,6 +419,7 @@ void launch_adjoint_step(const StepArgs &s, const StepArgs &h, const WsPtrs &w, 
   ap.n = n;
   const unsigned nbp = nblocks(n * kAdjSplit, kAdjBlock);
   if (cfg.kernel == SPH_KERNEL_CUBIC) k_pair_adjoint<SPH_KERNEL_CUBIC><<<nbp, kAdjBlock, 0, st>>>(P, ap);
+  else if (cfg.kernel == SPH_KERNEL_WENDLAND) k_pair_adjoint<SPH_KERNEL_WENDLAND><<<nbp, kAdjBlock, 0, st>>>(P, ap);
   else k_pair_adjoint<SPH_KERNEL_GAUSSIAN><<<nbp, kAdjBlock, 0, st>>>(P, ap);
   k_adj_post<<<nb, kBlock, 0, st>>>(s.label, n, dt, adj.xb, adj.yb, adj.vxb, adj.vyb, adj.rhob, adj.axb, adj.ayb,
                                     adj.drhob, adj.xhb, adj.yhb, adj.vxhb, adj.vyhb, adj.rhohb, adj.alb, adj.alphab);

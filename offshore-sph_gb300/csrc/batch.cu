@@ -110,7 +110,8 @@ int sph_batch_setup(const sph_workspace_t *ws, int64_t n_inst, const int64_t *of
   if (!ws || !ws->ptr || !offsets || !w || !h_fixed || !cfg || n_inst < 1 || n_inst > (1 << 20))
     return SPH_ERR_INVALID_ARGUMENT;
   if (cfg->precision != SPH_PREC_MIXED || cfg->integrator != SPH_INTEGRATOR_PEC || cfg->dt_fixed > 0.0 ||
-      cfg->pec_use_xsph || cfg->nn_scale <= 0.0 || (cfg->kernel != SPH_KERNEL_CUBIC && cfg->kernel != SPH_KERNEL_GAUSSIAN))
+      cfg->pec_use_xsph || cfg->nn_scale <= 0.0 ||
+      (cfg->kernel != SPH_KERNEL_CUBIC && cfg->kernel != SPH_KERNEL_GAUSSIAN && cfg->kernel != SPH_KERNEL_WENDLAND))
     return SPH_ERR_INVALID_ARGUMENT;
   if (ws->max_cells < 2 * n_inst || ws->bytes < make_batch_layout(ws->n_cap, ws->max_cells, n_inst).total)
     return SPH_ERR_WORKSPACE_TOO_SMALL;

@@ -123,9 +123,11 @@ static int ws_ok(const sph_workspace_t *ws, int64_t n) {
 }
 
 static bool config_ok(const sph_config_t *c) {
-  return c && (c->kernel == SPH_KERNEL_CUBIC || c->kernel == SPH_KERNEL_GAUSSIAN) &&
+  return c && (c->kernel == SPH_KERNEL_CUBIC || c->kernel == SPH_KERNEL_GAUSSIAN || c->kernel == SPH_KERNEL_WENDLAND) &&
          (c->precision == SPH_PREC_FP64 || c->precision == SPH_PREC_MIXED) &&
-         (c->integrator == SPH_INTEGRATOR_PEC || c->integrator == SPH_INTEGRATOR_EULER) && c->nn_scale > 0.0;
+         (c->integrator == SPH_INTEGRATOR_PEC || c->integrator == SPH_INTEGRATOR_EULER ||
+          c->integrator == SPH_INTEGRATOR_VERLET) &&
+         c->nn_scale > 0.0;
 }
 
 extern "C" {
@@ -209,7 +211,8 @@ int sph_eos(sph_particles_t *pa, const sph_wcsph_t *w, sph_stream_t stream) {
 }
 
 int sph_kernel_eval(int kernel, int64_t n, const double *r, const double *h, double *out, sph_stream_t stream) {
-  if ((kernel != SPH_KERNEL_CUBIC && kernel != SPH_KERNEL_GAUSSIAN) || n < 0 || (n && (!r || !h || !out)))
+  if ((kernel != SPH_KERNEL_CUBIC && kernel != SPH_KERNEL_GAUSSIAN && kernel != SPH_KERNEL_WENDLAND) || n < 0 ||
+      (n && (!r || !h || !out)))
     return SPH_ERR_INVALID_ARGUMENT;
   if (n == 0) return SPH_OK;
   launch_kernel_map(kernel, 0, n, nullptr, r, h, out, (cudaStream_t)stream);
@@ -218,7 +221,8 @@ int sph_kernel_eval(int kernel, int64_t n, const double *r, const double *h, dou
 
 int sph_kernel_grad(int kernel, int64_t n, const double *x, const double *r, const double *h, double *out,
                     sph_stream_t stream) {
-  if ((kernel != SPH_KERNEL_CUBIC && kernel != SPH_KERNEL_GAUSSIAN) || n < 0 || (n && (!x || !r || !h || !out)))
+  if ((kernel != SPH_KERNEL_CUBIC && kernel != SPH_KERNEL_GAUSSIAN && kernel != SPH_KERNEL_WENDLAND) || n < 0 ||
+      (n && (!x || !r || !h || !out)))
     return SPH_ERR_INVALID_ARGUMENT;
   if (n == 0) return SPH_OK;
   launch_kernel_map(kernel, 1, n, x, r, h, out, (cudaStream_t)stream);

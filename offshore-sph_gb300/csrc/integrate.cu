@@ -21,6 +21,11 @@ __global__ void __launch_bounds__(kBlock) k_predict(StepArgs a, IntParams ip) {
   long long i = (long long)blockIdx.x * blockDim.x + threadIdx.x;
   if (i >= a.n || !is_fluid(a.label[i])) return;
   const double hdt = 0.5 * load_dt(ip);
+  if (ip.integrator == SPH_INTEGRATOR_VERLET) {  // Verlet.predict (src/Integrators/Verlet.py:28-35)
+    a.x[i] += hdt * a.vx[i];
+    a.y[i] += hdt * a.vy[i];
+    return;
+  }
   double x = a.x[i], y = a.y[i], vx = a.vx[i], vy = a.vy[i], rho = a.rho[i];
   a.x0[i] = x;
   a.y0[i] = y;
@@ -47,6 +52,19 @@ __device__ __forceinline__ void correct_one(const StepArgs &a, long long i, cons
   const double dt = load_dt(ip);
   const double hdt = 0.5 * dt;
   const double ax = a.ax[i], ay = a.ay[i], drho = a.drho[i];
+  if (ip.integrator == SPH_INTEGRATOR_VERLET) {  // Verlet.correct (src/Integrators/Verlet.py:37-53)
+    const double vx = fma(dt, ax, a.vx[i]), vy = fma(dt, ay, a.vy[i]);
+    a.vx[i] = vx;
+    a.vy[i] = vy;
+    if (ip.use_xsph) {
+      a.x[i] = fma(hdt, a.xsphx[i], a.x[i]);
+      a.y[i] = fma(hdt, a.xsphy[i], a.y[i]);
+    } else {
+      a.x[i] = fma(hdt, vx, a.x[i]);
+      a.y[i] = fma(hdt, vy, a.y[i]);
+    }
+    return;
+  }
   if (ip.integrator == SPH_INTEGRATOR_EULER) {
     const double vx = a.vx[i], vy = a.vy[i];
     a.x[i] = a.x[i] + dt * vx + 0.5 * dt * dt * ax;
@@ -214,8 +232,12 @@ __global__ void __launch_bounds__(kBlock) k_kernel_map(int kernel, int what, lon
   const double rj = r[j], hj = h[j];
   double v;
   if (what == 2) v = gauss_dwdq(rj, hj);
-  else if (what == 0) v = kernel == SPH_KERNEL_CUBIC ? cubic_w(rj, hj) : gauss_w(rj, hj);
-  else v = (kernel == SPH_KERNEL_CUBIC ? cubic_gcoef(rj, hj) : gauss_gcoef(rj, hj)) * x[j];
+  else if (what == 0)
+    v = kernel == SPH_KERNEL_CUBIC ? cubic_w(rj, hj) : (kernel == SPH_KERNEL_WENDLAND ? wendland_w(rj, hj) : gauss_w(rj, hj));
+  else
+    v = (kernel == SPH_KERNEL_CUBIC ? cubic_gcoef(rj, hj)
+                                    : (kernel == SPH_KERNEL_WENDLAND ? wendland_gcoef(rj, hj) : gauss_gcoef(rj, hj))) *
+        x[j];
   out[j] = v;
 }
 

@@ -29,7 +29,7 @@ struct BoundsParams {
   int h_fixed_on; // h_fixed > 0
   int dt_fixed_on;
   int damped;     // damping != 0
-  int use_xsph, strict, euler;
+  int use_xsph, strict, euler, verlet;
   double h_fixed, dt_fixed;
   double inv_damp;  // 1 / (1 + 0.5 damping)
   double c0;        // 2 inv_damp - 1
@@ -44,6 +44,33 @@ struct BoundsParams {
 // sees the fused multiply-adds of the updates.
 __device__ __forceinline__ void integrate_front(const StepArgs &a, long long i, const BoundsParams &bp, double &x,
                                                 double &y, double &rho) {
+  if (bp.verlet) {
+    // [Verlet.correct (src/Integrators/Verlet.py:37-53): kick, second half
+    // drift with the new velocity or XSPH] then [Verlet.predict (:28-35):
+    // half drift]; the density is not integrated
+    double vx = a.vx[i], vy = a.vy[i];
+    if (bp.stage == kStageCorrectPredict) {
+      const double dtc = bp.dt_fixed_on ? bp.dt_fixed : bp.dt_prev[0];
+      const double hc = half_exact(dtc);
+      vx = fma(dtc, a.ax[i], vx);
+      vy = fma(dtc, a.ay[i], vy);
+      if (bp.use_xsph) {
+        x = fma(hc, a.xsphx[i], x);
+        y = fma(hc, a.xsphy[i], y);
+      } else {
+        x = fma(hc, vx, x);
+        y = fma(hc, vy, y);
+      }
+      a.vx[i] = vx;
+      a.vy[i] = vy;
+    }
+    const double hdt = half_exact(bp.dt_fixed_on ? bp.dt_fixed : bp.dt_cur[0]);
+    x = fma(hdt, vx, x);
+    y = fma(hdt, vy, y);
+    a.x[i] = x;
+    a.y[i] = y;
+    return;
+  }
   double vx, vy;
   const double axv = a.ax[i], ayv = a.ay[i], drho = a.drho[i];
   if (bp.stage == kStageCorrectPredict) {
@@ -176,6 +203,7 @@ void launch_bounds(const StepArgs &a, const WsPtrs &w, const sph_config_t &cfg, 
   BoundsParams bp;
   bp.stage = stage;
   bp.euler = cfg.integrator == SPH_INTEGRATOR_EULER ? 1 : 0;
+  bp.verlet = cfg.integrator == SPH_INTEGRATOR_VERLET ? 1 : 0;
   if (bp.euler && stage == kStagePredict) bp.stage = kStageNone;  // Euler.predict is a no-op
   bp.h_reset = h_reset ? 1 : 0;
   bp.h_fixed = cfg.h_fixed;
@@ -228,7 +256,8 @@ __device__ unsigned grid_setup(double xmin, double xmax, double ymin, double yma
   g->hmaxf = __double2float_ru(hmax) * 1.00001f;
   // interaction radius: the kernel support (cubic 2h, Gaussian 3h) and the
   // Lennard-Jones reach min(r0, 3h)
-  const bool cubic = gp.kernel == SPH_KERNEL_CUBIC;
+  // support 2h (cubic spline, Wendland C4: zero with zero gradient at q = 2) or 3h (Gaussian)
+  const bool cubic = gp.kernel != SPH_KERNEL_GAUSSIAN;
   double R = fmax((cubic ? 2.0 : 3.0) * hmax, fmin(gp.r0, 3.0 * hmax));
   double ext = fmax(xmax - xmin, ymax - ymin);
   R = fmax(R, fmax(ext * 1e-7, 1e-300));
@@ -834,6 +863,7 @@ void launch_bt_bounds(const StepArgs &a, const WsPtrs &w, const BatchPtrs &B, co
   BoundsParams bp;
   bp.stage = stage;
   bp.euler = cfg.integrator == SPH_INTEGRATOR_EULER ? 1 : 0;
+  bp.verlet = cfg.integrator == SPH_INTEGRATOR_VERLET ? 1 : 0;
   if (bp.euler && stage == kStagePredict) bp.stage = kStageNone;
   bp.h_reset = 1;
   bp.h_fixed = 0.0;

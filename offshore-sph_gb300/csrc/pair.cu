@@ -23,6 +23,8 @@
 // state.
 #include <math.h>
 
+#include <type_traits>
+
 #include "sph_internal.cuh"
 
 namespace sph {
@@ -34,7 +36,7 @@ constexpr int kPairBlock = 128;
 // stays rare
 template <int KERNEL>
 struct ListCap {
-  static constexpr int value = KERNEL == SPH_KERNEL_CUBIC ? 32 : 64;
+  static constexpr int value = Support<KERNEL>::q == 2 ? 32 : 64;
 };
 #ifndef SPH_PAIR_MIXED_BLOCKS
 #define SPH_PAIR_MIXED_BLOCKS 8
@@ -128,7 +130,7 @@ struct MixedConsts {
 template <int KERNEL>
 __device__ __forceinline__ MixedConsts mixed_consts(const PairParams &pp) {
   MixedConsts c;
-  c.KC = KERNEL == SPH_KERNEL_CUBIC ? 4.0f : 9.0f;  // (support / h)^2
+  c.KC = (float)(Support<KERNEL>::q * Support<KERNEL>::q);  // (support / h)^2
   const float r0f = (float)pp.r0;
   c.r02f = r0f * r0f;
   c.co = (float)pp.co;
@@ -171,6 +173,13 @@ __device__ __forceinline__ void mixed_pair(MixedAcc &acc, const MixedConsts &c, 
     const bool outer = q > 1.0f;
     w = outer ? al * 0.25f * (t2 * t2 * t2) : al * (1.0f - 1.5f * (q * q) * (1.0f - 0.5f * q));
     const float gq = outer ? -0.75f * (t2 * t2) : -3.0f * q * (1.0f - 0.75f * q);
+    coef = r >= 1e-10f ? al * gq * inv_h * inv_r : 0.f;
+  } else if (KERNEL == SPH_KERNEL_WENDLAND) {
+    const float al = (float)kWendFac * inv_h * inv_h;
+    const float inner = fmaxf(1.0f - 0.5f * q, 0.f);
+    const float i2 = inner * inner, i5 = i2 * i2 * inner;
+    w = al * (i5 * inner) * ((35.0f / 12.0f) * q * q + 3.0f * q + 1.0f);
+    const float gq = i5 * (-14.0f / 3.0f) * q * (1.0f + 2.5f * q);
     coef = r >= 1e-10f ? al * gq * inv_h * inv_r : 0.f;
   } else {
     const float ac = (float)kInvPi * inv_h * inv_h;
@@ -251,7 +260,7 @@ __device__ __forceinline__ unsigned long long pair_query(const StepArgs &a, cons
   constexpr int kListCap = ListCap<KERNEL>::value;
   const int tid = threadIdx.x;
   unsigned long long ea = kEncMaxId;
-  const float SK = (KERNEL == SPH_KERNEL_CUBIC ? 2.0f : 3.0f) * 1.000002f;  // support / h, padded
+  const float SK = (float)Support<KERNEL>::q * 1.000002f;  // support / h, padded
   const float r0f = (float)pp.r0;
   const float pad = g.pad_e;
   {
@@ -309,6 +318,9 @@ __device__ __forceinline__ unsigned long long pair_query(const StepArgs &a, cons
                   if (r >= 1e-10) coef = al * (-3.0 * q * (1.0 - 0.75 * q)) / (hij * r);
                 }
               }
+            } else if (KERNEL == SPH_KERNEL_WENDLAND) {
+              w = wendland_w(r, hij);
+              coef = wendland_gcoef(r, hij);
             } else {
               const double ac = kInvPi / (hij * hij);
               const double e = exp(-q * q);
@@ -480,8 +492,8 @@ __global__ void __launch_bounds__(kPairBlock) k_sumdens(StepArgs a, PairPtrs P, 
     const double4_32a A = P.r64a[k], B = P.r64b[k];
     xi = A.x; yi = A.y; hi = B.w;
   }
-  const float KC = KERNEL == SPH_KERNEL_CUBIC ? 4.0f : 9.0f;
-  const float SK = (KERNEL == SPH_KERNEL_CUBIC ? 2.0f : 3.0f) * 1.000002f;
+  const float KC = (float)(Support<KERNEL>::q * Support<KERNEL>::q);
+  const float SK = (float)Support<KERNEL>::q * 1.000002f;
   double rho = 0.0;
   float rhof = 0.f;
   const Stencil sten(g, qref, qkey, W);
@@ -502,6 +514,9 @@ __global__ void __launch_bounds__(kPairBlock) k_sumdens(StepArgs a, PairPtrs P, 
           const float al = (float)kCubicFac / (hij * hij);
           const float t = fmaxf(2.0f - q, 0.f);
           w = q > 1.0f ? al * 0.25f * t * t * t : al * (1.0f - 1.5f * q * q * (1.0f - 0.5f * q));
+        } else if (KERNEL == SPH_KERNEL_WENDLAND) {
+          const float inner = fmaxf(1.0f - 0.5f * q, 0.f), i2 = inner * inner;
+          w = (float)kWendFac / (hij * hij) * (i2 * i2 * i2) * ((35.0f / 12.0f) * q * q + 3.0f * q + 1.0f);
         } else {
           w = (float)kInvPi / (hij * hij) * __expf(-q * q);
         }
@@ -514,7 +529,9 @@ __global__ void __launch_bounds__(kPairBlock) k_sumdens(StepArgs a, PairPtrs P, 
         const double ddx = xi - A.x, ddy = yi - A.y;
         const double r = __dsqrt_rn(__dadd_rn(__dmul_rn(ddx, ddx), __dmul_rn(ddy, ddy)));
         const double h = __dmul_rn(0.5, __dadd_rn(hi, fabs(B.w)));
-        if (__ddiv_rn(r, h) <= 3.0) rho += B.x * (KERNEL == SPH_KERNEL_CUBIC ? cubic_w(r, h) : gauss_w(r, h));
+        if (__ddiv_rn(r, h) <= 3.0)
+          rho += B.x * (KERNEL == SPH_KERNEL_CUBIC ? cubic_w(r, h)
+                                                   : (KERNEL == SPH_KERNEL_WENDLAND ? wendland_w(r, h) : gauss_w(r, h)));
       }
    });
   a.rho[P.perm[k]] = MIXED ? f2d(rhof) : rho;
@@ -714,7 +731,7 @@ __device__ __forceinline__ unsigned long long tile_process(const StepArgs &a, co
   __syncthreads();
   // per-query candidate radius: the padded reach of the largest pair h
   // (every |h| <= hmaxf), so that one compare per candidate suffices
-  const float SK = (KERNEL == SPH_KERNEL_CUBIC ? 2.0f : 3.0f) * 1.000002f;  // support / h, padded
+  const float SK = (float)Support<KERNEL>::q * 1.000002f;  // support / h, padded
   for (unsigned int k = qs + tid; k < qe; k += kPairBlock) {
     int cx, cy;
     tiled_cell(P.keys_sorted[k] - tg.cell0, ts, ntlx, cx, cy);
@@ -998,17 +1015,16 @@ void launch_pair(const StepArgs &a, const WsPtrs &w, const sph_config_t &cfg, co
     pp.fr = wall->fr;
   }
   const bool xs = wc.use_xsph != 0, sd = wc.use_summation_density != 0;
-  if (cfg.kernel == SPH_KERNEL_CUBIC) {
-    if (xs) sd ? pair_dispatch<SPH_KERNEL_CUBIC, true, true>(a, w, cfg, pp, dt_out, dt_hist, st)
-               : pair_dispatch<SPH_KERNEL_CUBIC, true, false>(a, w, cfg, pp, dt_out, dt_hist, st);
-    else sd ? pair_dispatch<SPH_KERNEL_CUBIC, false, true>(a, w, cfg, pp, dt_out, dt_hist, st)
-            : pair_dispatch<SPH_KERNEL_CUBIC, false, false>(a, w, cfg, pp, dt_out, dt_hist, st);
-  } else {
-    if (xs) sd ? pair_dispatch<SPH_KERNEL_GAUSSIAN, true, true>(a, w, cfg, pp, dt_out, dt_hist, st)
-               : pair_dispatch<SPH_KERNEL_GAUSSIAN, true, false>(a, w, cfg, pp, dt_out, dt_hist, st);
-    else sd ? pair_dispatch<SPH_KERNEL_GAUSSIAN, false, true>(a, w, cfg, pp, dt_out, dt_hist, st)
-            : pair_dispatch<SPH_KERNEL_GAUSSIAN, false, false>(a, w, cfg, pp, dt_out, dt_hist, st);
-  }
+  auto go = [&](auto kern) {
+    constexpr int K = decltype(kern)::value;
+    if (xs) sd ? pair_dispatch<K, true, true>(a, w, cfg, pp, dt_out, dt_hist, st)
+               : pair_dispatch<K, true, false>(a, w, cfg, pp, dt_out, dt_hist, st);
+    else sd ? pair_dispatch<K, false, true>(a, w, cfg, pp, dt_out, dt_hist, st)
+            : pair_dispatch<K, false, false>(a, w, cfg, pp, dt_out, dt_hist, st);
+  };
+  if (cfg.kernel == SPH_KERNEL_CUBIC) go(std::integral_constant<int, SPH_KERNEL_CUBIC>());
+  else if (cfg.kernel == SPH_KERNEL_WENDLAND) go(std::integral_constant<int, SPH_KERNEL_WENDLAND>());
+  else go(std::integral_constant<int, SPH_KERNEL_GAUSSIAN>());
 }
 
 void launch_sumdens(const StepArgs &a, const WsPtrs &w, const sph_config_t &cfg, const sph_wcsph_t &wc,
@@ -1016,13 +1032,15 @@ void launch_sumdens(const StepArgs &a, const WsPtrs &w, const sph_config_t &cfg,
   const unsigned nb = nblocks(a.n, kPairBlock);
   const bool mixed = cfg.precision == SPH_PREC_MIXED;
   const PairPtrs P = pair_ptrs(w);
-  if (cfg.kernel == SPH_KERNEL_CUBIC) {
-    if (mixed) k_sumdens<SPH_KERNEL_CUBIC, true><<<nb, kPairBlock, 0, st>>>(a, P, a.n);
-    else k_sumdens<SPH_KERNEL_CUBIC, false><<<nb, kPairBlock, 0, st>>>(a, P, a.n);
-  } else {
-    if (mixed) k_sumdens<SPH_KERNEL_GAUSSIAN, true><<<nb, kPairBlock, 0, st>>>(a, P, a.n);
-    else k_sumdens<SPH_KERNEL_GAUSSIAN, false><<<nb, kPairBlock, 0, st>>>(a, P, a.n);
-  }
+  auto go = [&](auto kern) {
+    constexpr int K = decltype(kern)::value;
+    if (mixed) k_sumdens<K, true><<<nb, kPairBlock, 0, st>>>(a, P, a.n);
+    else k_sumdens<K, false><<<nb, kPairBlock, 0, st>>>(a, P, a.n);
+  };
+  if (cfg.kernel == SPH_KERNEL_CUBIC) go(std::integral_constant<int, SPH_KERNEL_CUBIC>());
+  else if (cfg.kernel == SPH_KERNEL_WENDLAND) go(std::integral_constant<int, SPH_KERNEL_WENDLAND>());
+  else go(std::integral_constant<int, SPH_KERNEL_GAUSSIAN>());
+  (void)wc;
 }
 
 void launch_nn_count(const StepArgs &a, const WsPtrs &w, int64_t *counts, const int64_t *offsets, int64_t *idx,
@@ -1043,13 +1061,10 @@ static void bt_pair_dispatch(const StepArgs &a, const WsPtrs &w, const BatchPtrs
 void launch_bt_pair(const StepArgs &a, const WsPtrs &w, const BatchPtrs &B, int kernel, bool xsph, int tile_blocks,
                     cudaStream_t st) {
   if (tile_blocks < 1 || tile_blocks > kTileBlocks) tile_blocks = kTileBlocks;
-  if (kernel == SPH_KERNEL_CUBIC) {
-    if (xsph) bt_pair_dispatch<SPH_KERNEL_CUBIC, true, false>(a, w, B, tile_blocks, st);
-    else bt_pair_dispatch<SPH_KERNEL_CUBIC, false, false>(a, w, B, tile_blocks, st);
-  } else {
-    if (xsph) bt_pair_dispatch<SPH_KERNEL_GAUSSIAN, true, false>(a, w, B, tile_blocks, st);
-    else bt_pair_dispatch<SPH_KERNEL_GAUSSIAN, false, false>(a, w, B, tile_blocks, st);
-  }
+  (void)xsph;  // the batched form has no XSPH
+  if (kernel == SPH_KERNEL_CUBIC) bt_pair_dispatch<SPH_KERNEL_CUBIC, false, false>(a, w, B, tile_blocks, st);
+  else if (kernel == SPH_KERNEL_WENDLAND) bt_pair_dispatch<SPH_KERNEL_WENDLAND, false, false>(a, w, B, tile_blocks, st);
+  else bt_pair_dispatch<SPH_KERNEL_GAUSSIAN, false, false>(a, w, B, tile_blocks, st);
 }
 
 }  // namespace sph

@@ -525,6 +525,15 @@ __device__ __forceinline__ double reset_h(double h_fixed, double m, double rho) 
 // ---------------------------------------------------------------------------
 constexpr double kCubicFac = 10.0 / (7.0 * M_PI);  // CubicSpline.py:24
 constexpr double kInvPi = 1.0 / M_PI;              // Gaussian.py:18
+constexpr double kWendFac = 9.0 / (4.0 * M_PI);    // Wendland.py:22
+
+// support of a kernel in units of h: 3 for the Gaussian (cut at q <= 3), 2
+// for the cubic spline and Wendland C4, which vanish with a zero gradient at
+// q = 2
+template <int KERNEL>
+struct Support {
+  static constexpr int q = KERNEL == SPH_KERNEL_GAUSSIAN ? 3 : 2;
+};
 
 // CubicSpline.evaluate (CubicSpline.py:12-36)
 __device__ __forceinline__ double cubic_w(double r, double h) {
@@ -550,6 +559,23 @@ __device__ __forceinline__ double cubic_gcoef(double r, double h) {
     g = -3.0 * q * (1.0 - 0.75 * q);
   }
   return alpha * g / (h * r);
+}
+// Wendland.evaluate (Wendland.py:10-34)
+__device__ __forceinline__ double wendland_w(double r, double h) {
+  const double alpha = kWendFac / (h * h);
+  const double q = r / h;
+  if (q >= 2.0) return 0.0;
+  const double inner = 1.0 - 0.5 * q;
+  return alpha * (pow(inner, 6.0) * (35.0 / 12.0 * q * q + 3.0 * q + 1.0));
+}
+// Wendland.gradient (Wendland.py:36-64): the factor multiplying x
+__device__ __forceinline__ double wendland_gcoef(double r, double h) {
+  const double alpha = kWendFac / (h * h);
+  const double q = r / h;
+  if ((q >= 2.0) || (r < 1e-10)) return 0.0;
+  const double inner = 1.0 - 0.5 * q;
+  const double grad = pow(inner, 5.0) * (-14.0 / 3.0) * q * (1 + 2.5 * q);
+  return alpha * grad / (h * r);
 }
 // Gaussian.evaluate (Gaussian.py:16-24)
 __device__ __forceinline__ double gauss_w(double r, double h) {

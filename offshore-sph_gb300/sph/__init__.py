@@ -14,11 +14,13 @@ from .Common import ParticleType, particle_dtype, get_label_code
 from .Methods.WCSPH import WCSPH
 from .Kernels.CubicSpline import CubicSpline
 from .Kernels.Gaussian import Gaussian
+from .Kernels.Wendland import Wendland
 from .Integrators.PEC import PEC
 from .Integrators.Euler import Euler
+from .Integrators.Verlet import Verlet
 from .Tools.NNLinkedList import NNLinkedList
 from .Equations.TimeStep import TimeStep
 from .Solver import Solver
 
-__all__ = ["ParticleType", "particle_dtype", "get_label_code", "WCSPH", "CubicSpline", "Gaussian", "PEC", "Euler",
-           "NNLinkedList", "TimeStep", "Solver"]
+__all__ = ["ParticleType", "particle_dtype", "get_label_code", "WCSPH", "CubicSpline", "Gaussian", "Wendland", "PEC",
+           "Euler", "Verlet", "NNLinkedList", "TimeStep", "Solver"]

@@ -12,9 +12,9 @@ LIB_PATH = _build.LIB
 
 # enums of include/sph_gb300.h
 FLUID, BOUNDARY, TEMP_BOUNDARY, COUPLED = 0, 1, 2, 3
-KERNEL_CUBIC, KERNEL_GAUSSIAN = 0, 1
+KERNEL_CUBIC, KERNEL_GAUSSIAN, KERNEL_WENDLAND = 0, 1, 2
 PREC_FP64, PREC_MIXED = 0, 1
-INTEGRATOR_PEC, INTEGRATOR_EULER = 0, 1
+INTEGRATOR_PEC, INTEGRATOR_EULER, INTEGRATOR_VERLET = 0, 1, 2
 
 SPH_OK = 0
 STATUS_CELL_OVERFLOW = 1 << 0

@@ -72,6 +72,8 @@ def lib():
         L.or_pec_predict.argtypes = [C.c_void_p, C.c_void_p, C.c_double, C.c_double, C.c_int, C.c_int]
         L.or_pec_correct.argtypes = [C.c_void_p, C.c_void_p, C.c_double, C.c_double, C.c_int, C.c_int]
         L.or_euler_correct.argtypes = [C.c_void_p, C.c_void_p, C.c_double]
+        L.or_verlet_predict.argtypes = [C.c_void_p, C.c_void_p, C.c_double]
+        L.or_verlet_correct.argtypes = [C.c_void_p, C.c_void_p, C.c_double, C.c_int]
         L.or_eos.argtypes = [C.c_int64, C.c_void_p, dp, C.c_double, C.c_double, C.c_double, C.c_double, dp]
         L.or_tait_height.argtypes = [C.c_int64, dp, C.c_double, C.c_double, C.c_double, C.c_double, dp]
         L.or_kernel_eval.argtypes = [C.c_int, C.c_int64, dp, dp, dp]
@@ -288,6 +290,18 @@ def euler_correct(P, dt, mask=None):
     keep, mp = _mask(P, mask)
     s = P.cstruct()
     lib().or_euler_correct(C.byref(s), mp, dt)
+
+
+def verlet_predict(P, dt, mask=None):
+    keep, mp = _mask(P, mask)
+    s = P.cstruct()
+    lib().or_verlet_predict(C.byref(s), mp, dt)
+
+
+def verlet_correct(P, dt, use_xsph=False, mask=None):
+    keep, mp = _mask(P, mask)
+    s = P.cstruct()
+    lib().or_verlet_correct(C.byref(s), mp, dt, int(bool(use_xsph)))
 
 
 def loop(params, nn, P, nthreads=1):

@@ -94,10 +94,34 @@ static double gauss_grad(double x, double r, double h) {
   return 0.0;
 }
 
-/* kernel id: 0 = CubicSpline, 1 = Gaussian */
-static double kern_w(int k, double r, double h) { return k == 0 ? cubic_w(r, h) : gauss_w(r, h); }
+/* src/Kernels/Wendland.py:10-34 (evaluate, Wendland C4) */
+static double wendland_w(double r, double h) {
+  const double fac = 9.0 / (4.0 * M_PI);
+  double alpha = fac / (h * h);
+  double q = r / h;
+  if (q >= 2.0) return 0.0;
+  double inner = 1.0 - 0.5 * q;
+  return alpha * (pow(inner, 6) * (35.0 / 12.0 * q * q + 3.0 * q + 1.0));
+}
+
+/* src/Kernels/Wendland.py:36-64 (gradient) */
+static double wendland_grad(double x, double r, double h) {
+  const double fac = 9.0 / (4.0 * M_PI);
+  double alpha = fac / (h * h);
+  double q = r / h;
+  if ((q >= 2.0) || (r < 1e-10)) return 0.0;
+  double inner = 1.0 - 0.5 * q;
+  double grad = pow(inner, 5) * (-14.0 / 3.0) * q * (1 + 2.5 * q);
+  double norm = alpha * grad / (h * r);
+  return norm * x;
+}
+
+/* kernel id: 0 = CubicSpline, 1 = Gaussian, 2 = Wendland */
+static double kern_w(int k, double r, double h) {
+  return k == 0 ? cubic_w(r, h) : (k == 1 ? gauss_w(r, h) : wendland_w(r, h));
+}
 static double kern_grad(int k, double x, double r, double h) {
-  return k == 0 ? cubic_grad(x, r, h) : gauss_grad(x, r, h);
+  return k == 0 ? cubic_grad(x, r, h) : (k == 1 ? gauss_grad(x, r, h) : wendland_grad(x, r, h));
 }
 
 void or_kernel_eval(int kernel, int64_t n, const double *r, const double *h, double *out) {
@@ -657,11 +681,37 @@ void or_euler_correct(or_particles *P, const uint8_t *mask, double dt) {
   }
 }
 
+/* Verlet.predict (src/Integrators/Verlet.py:28-35): drift by half a step */
+void or_verlet_predict(or_particles *P, const uint8_t *mask, double dt) {
+  for (int64_t j = 0; j < P->n; j++) {
+    if (mask && !mask[j]) continue;
+    P->x[j] += 0.5 * dt * P->vx[j];
+    P->y[j] += 0.5 * dt * P->vy[j];
+  }
+}
+
+/* Verlet.correct (src/Integrators/Verlet.py:37-53): kick, then the second
+ * half drift with the new velocity (or XSPH); the density is not integrated */
+void or_verlet_correct(or_particles *P, const uint8_t *mask, double dt, int use_xsph) {
+  for (int64_t j = 0; j < P->n; j++) {
+    if (mask && !mask[j]) continue;
+    P->vx[j] += dt * P->ax[j];
+    P->vy[j] += dt * P->ay[j];
+    if (use_xsph) {
+      P->x[j] += 0.5 * dt * P->xsphx[j];
+      P->y[j] += 0.5 * dt * P->xsphy[j];
+    } else {
+      P->x[j] += 0.5 * dt * P->vx[j];
+      P->y[j] += 0.5 * dt * P->vy[j];
+    }
+  }
+}
+
 /* ------------------------------------------------------------------------ */
 /* Bare time steps (the body of Solver.run, src/Solver.py:366-410)           */
 /* ------------------------------------------------------------------------ */
 
-/* Step options: integrator 0 = PEC, 1 = Euler.  dt_fixed > 0 is the
+/* Step options: integrator 0 = PEC, 1 = Euler, 2 = Verlet.  dt_fixed > 0 is the
  * Solver's timeStep (Solver.py:370-372), else TimeStep with gamma_c/gamma_f
  * (Solver.py:210-230).  dt_out (3*nsteps: dt, dt_c, dt_f) may be NULL. */
 typedef struct {
@@ -684,9 +734,11 @@ int or_run(const or_wcsph *w, void *nnp, or_particles *P, const or_stepopt *o, i
     if (dt_out) { dt_out[3 * s] = dts[0]; dt_out[3 * s + 1] = dts[1]; dt_out[3 * s + 2] = dts[2]; }
     double dt = dts[0];
     if (o->integrator == 0) or_pec_predict(P, fmask, dt, o->damping, o->pec_use_xsph, o->pec_strict);
+    else if (o->integrator == 2) or_verlet_predict(P, fmask, dt);
     int st = or_compute(w, nnp, P, o->h_fixed, o->nthreads);
     if (st) { free(fmask); return st; }
     if (o->integrator == 0) or_pec_correct(P, fmask, dt, o->damping, o->pec_use_xsph, o->pec_strict);
+    else if (o->integrator == 2) or_verlet_correct(P, fmask, dt, o->pec_use_xsph);
     else or_euler_correct(P, fmask, dt);
   }
   free(fmask);

@@ -7,8 +7,8 @@ physics is plain torch arithmetic in FP64, following the reference:
 continuity (src/Equations/Continuity.py), momentum with artificial viscosity
 and gravity (src/Equations/Momentum.py, src/Methods/WCSPH.py:151-169), the
 Tait EOS (src/Equations/TaitEOS.py), the Lennard-Jones boundary force
-(src/Equations/BoundaryForce.py), the cubic spline gradient
-(src/Kernels/CubicSpline.py:40-70) and PEC with a fixed dt
+(src/Equations/BoundaryForce.py), the cubic spline or Wendland C4 gradient
+and PEC with a fixed dt
 (src/Integrators/PEC.py:32-89).
 """
 import math
@@ -50,10 +50,17 @@ def _evaluate(case, wc, alpha, x, y, vx, vy, rho, i, j):
     hij = 0.5 * (h[i] + h[j])
     q = r / hij
     jf = f[j]
-    # cubic spline gradient factor
-    al = 10.0 / (7.0 * math.pi) / (hij * hij)
-    g = torch.where(q > 1.0, -0.75 * (2.0 - q) ** 2, -3.0 * q * (1.0 - 0.75 * q))
-    inside = (q <= 2.0) & (r >= 1e-10) & jf
+    if case.cfg.kernel == 2:
+        # Wendland C4 gradient factor (src/Kernels/Wendland.py:36-64)
+        al = 9.0 / (4.0 * math.pi) / (hij * hij)
+        inner = torch.clamp(1.0 - 0.5 * q, min=0.0)
+        g = inner ** 5 * (-14.0 / 3.0) * q * (1.0 + 2.5 * q)
+        inside = (q < 2.0) & (r >= 1e-10) & jf
+    else:
+        # cubic spline gradient factor (src/Kernels/CubicSpline.py:40-70)
+        al = 10.0 / (7.0 * math.pi) / (hij * hij)
+        g = torch.where(q > 1.0, -0.75 * (2.0 - q) ** 2, -3.0 * q * (1.0 - 0.75 * q))
+        inside = (q <= 2.0) & (r >= 1e-10) & jf
     coef = torch.where(inside, al * g / (hij * r), torch.zeros_like(r))
     dWx, dWy = coef * dx, coef * dy
     vxij = vx[i] - vx[j]

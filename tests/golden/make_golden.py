@@ -225,6 +225,41 @@ def gen_eos_integrators(ref):
           **{"in_" + k: np.array(f[k]) for k in f.dtype.names if k != "deleted"}, **res)
 
 
+def gen_extra(ref):
+    """Wendland C4 kernel values and gradients; Verlet predict / correct on a
+    fluid-only array."""
+    from src.Common import particle_dtype
+    from src.Kernels.Wendland import Wendland
+    from src.Integrators.Verlet import Verlet
+    rng = np.random.default_rng(11)
+    n = 500
+    h = rng.uniform(0.01, 0.05, n)
+    r = rng.uniform(0, 2.2, n) * h
+    r[:5] = [0.0, 1e-11, 2.0 * h[2], 1.999999 * h[3], 1.0 * h[4]]
+    x = r * rng.uniform(-1, 1, n)
+    res = dict(r=r, h=h, x=x, wend_w=np.asarray(Wendland.evaluate(r, h), dtype=np.float64),
+               wend_grad=np.asarray(Wendland.gradient(x, r, h), dtype=np.float64))
+    rng = np.random.default_rng(17)
+    f = np.zeros(64, dtype=particle_dtype)
+    f["label"] = 0
+    for k in ("x", "y", "vx", "vy", "ax", "ay", "drho", "xsphx", "xsphy"):
+        f[k] = rng.normal(0, 1, len(f))
+    f["rho"] = rng.uniform(900, 1100, len(f))
+    for k in f.dtype.names:
+        if k != "deleted":
+            res["in_" + k] = np.array(f[k])
+    for xs in (False, True):
+        it = Verlet(xs)
+        a = it.predict(0.003, f.copy(), 0.0)
+        tag = "verlet_x%d" % xs
+        for k in ("x", "y", "vx", "vy", "rho"):
+            res[tag + "_pred_" + k] = np.array(a[k])
+        a = it.correct(0.003, a, 0.0)
+        for k in ("x", "y", "vx", "vy", "rho"):
+            res[tag + "_corr_" + k] = np.array(a[k])
+    _save("wendland_verlet.npz", **res)
+
+
 def _nn_case(name, pa, scale=2.0):
     from src.Tools.NNLinkedList import NNLinkedList
     nn = NNLinkedList(scale)
@@ -327,8 +362,11 @@ def _solver_case(name, pa, height, r0, kernel, useXSPH=False, sumdens=False, h=N
     from src.Integrators.Euler import Euler
     from src.Equations.TimeStep import TimeStep
     method = WCSPH(height=height, r0=r0, rho0=1000.0, useXSPH=useXSPH, Pb=0.0, useSummationDensity=sumdens)
-    kern = CubicSpline() if kernel == 0 else Gaussian()
-    integ = PEC(useXSPH=useXSPH, strict=strict) if integrator == "pec" else Euler()
+    from src.Kernels.Wendland import Wendland
+    from src.Integrators.Verlet import Verlet
+    kern = (CubicSpline(), Gaussian(), Wendland())[kernel]
+    integ = {"pec": lambda: PEC(useXSPH=useXSPH, strict=strict), "euler": Euler,
+             "verlet": lambda: Verlet(useXSPH)}[integrator]()
     solver = Solver(method, integ, kern, 1.0, incrementalWriteout=False, h=h, damping=0.0)
     Solver.particleArray = None
     solver.particleArray = None
@@ -366,11 +404,16 @@ def _solver_case(name, pa, height, r0, kernel, useXSPH=False, sumdens=False, h=N
         st = solver.particleArray.copy()
         out.update({"step%d_%s" % (s + 1, k): np.array(st[k]) for k in st.dtype.names if k != "deleted"})
     meta = dict(height=height, r0=r0, kernel=kernel, useXSPH=int(useXSPH), sumdens=int(sumdens),
-                h=-1.0 if h is None else h, steps=steps, integrator=0 if integrator == "pec" else 1,
+                h=-1.0 if h is None else h, steps=steps, integrator={"pec": 0, "euler": 1, "verlet": 2}[integrator],
                 gamma_c=gamma_c, strict=int(strict), fixed_dt=-1.0 if fixed_dt is None else fixed_dt,
                 setup=int(setup))
     _save(name, dts=np.array(dts).reshape(-1, 3), **{"meta_" + k: v for k, v in meta.items()}, **out)
     print("  %s: %.1f s" % (name, time.time() - t0))
+
+
+def _new_solver_cases(tank, dx):
+    _solver_case("solver_tank_wendland.npz", tank, 0.4, dx, 2, h=1.3 * dx, steps=2, gamma_c=0.3)
+    _solver_case("solver_tank_verlet.npz", tank, 0.4, dx, 0, h=1.3 * dx, steps=2, integrator="verlet")
 
 
 def gen_solver(ref, skip_large=False, only_large=False):
@@ -388,6 +431,7 @@ def gen_solver(ref, skip_large=False, only_large=False):
     _solver_case("solver_tank_dynh.npz", tank, 0.4, dx, 0, h=None, steps=2)
     _solver_case("solver_tank_euler.npz", tank, 0.4, dx, 0, h=1.3 * dx, steps=2, integrator="euler",
                  fixed_dt=1e-4)
+    _new_solver_cases(tank, dx)
     lat = S.jittered_lattice(24, 24, 0.01, seed=3)
     _solver_case("solver_lattice_cubic.npz", lat, 0.24, 0.01, 0, h=0.013, steps=2, setup=False)
     _solver_case("solver_lattice_gauss.npz", lat, 0.24, 0.01, 1, h=0.013, steps=2, setup=False)
@@ -408,12 +452,15 @@ def main():
         sys.exit("--ref must point at an Offshore-SPH checkout")
     _install_shims()
     sys.path.insert(0, a.ref)
-    gens = dict(kernels=gen_kernels, equations=gen_equations, eos=gen_eos_integrators, nn=gen_nn)
+    gens = dict(kernels=gen_kernels, equations=gen_equations, eos=gen_eos_integrators, nn=gen_nn, extra=gen_extra)
     for k, g in gens.items():
         if a.only and k not in a.only.split(","):
             continue
         g(a.ref)
-    if not a.only or "solver" in a.only.split(","):
+    if "new_solver" in a.only.split(","):
+        from sph import scenarios as S
+        _new_solver_cases(S.dam_break(width=0.2, height=0.4, dx=0.025, tank_width=0.8, tank_height=0.6), 0.025)
+    elif not a.only or "solver" in a.only.split(","):
         gen_solver(a.ref, a.skip_large)
     elif "large" in a.only.split(","):
         gen_solver(a.ref, only_large=True)

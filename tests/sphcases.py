@@ -12,7 +12,7 @@ STATE_FIELDS = ("m", "rho", "p", "c", "drho", "h", "x", "y", "vx", "vy", "ax", "
 
 SOLVER_CASES = ["solver_tank_cubic", "solver_tank_gauss", "solver_tank_xsph", "solver_tank_sumdens",
                 "solver_tank_dynh", "solver_tank_euler", "solver_lattice_cubic", "solver_lattice_gauss",
-                "solver_alias"]
+                "solver_alias", "solver_tank_wendland", "solver_tank_verlet"]
 
 
 def load(name):

@@ -62,6 +62,28 @@ def test_adjoint_matches_torch_autograd(case):
     assert _rel(gv, rv) <= 1e-8
 
 
+def test_wendland_adjoint_matches_torch_autograd(case):
+    import adjoint_ref
+    from sph import adjoint, scenarios
+    dx = 0.02
+    pa = scenarios.dam_break(0.2, 0.4, dx, 0.8, 0.6, side="right")
+    wc = adjoint.WallLoadCase(pa, height=0.4, r0=dx, h=1.3 * dx, dt=1e-4, nsteps=20, wall_x=0.8, checkpoint=10,
+                              kernel=2)
+    torch.manual_seed(5)
+    pos = wc.positions()
+    vel = wc.velocities() + 0.05 * torch.randn_like(pos)
+    loss, ga, gp, gv = adjoint.gradients(wc, 0.01, pos, vel)
+    a = torch.tensor(0.01, dtype=torch.float64, device="cuda", requires_grad=True)
+    p = pos.clone().requires_grad_(True)
+    v = vel.clone().requires_grad_(True)
+    ref = adjoint_ref.reference_loss(wc, a, p, v)
+    ra, rp, rv = torch.autograd.grad(ref, (a, p, v))
+    assert loss.item() > 0.0 and loss.item() == pytest.approx(ref.item(), rel=1e-11)
+    assert _rel(ga, ra) <= 1e-8
+    assert _rel(gp, rp) <= 1e-8
+    assert _rel(gv, rv) <= 1e-8
+
+
 def test_adjoint_matches_central_differences(case):
     from sph import adjoint
     torch.manual_seed(1)

@@ -45,6 +45,27 @@ def test_gaussian_matches_reference(sph):
     assert SC.rel_err(g.gradient(z["x"], z["r"], z["h"]), z["gauss_grad"]) <= 1e-14
 
 
+def test_wendland_and_verlet_match_reference(sph):
+    """src/Kernels/Wendland.py, src/Integrators/Verlet.py on the reference's outputs."""
+    z = SC.load("wendland_verlet")
+    k = sph.Wendland()
+    assert SC.rel_err(k.evaluate(z["r"], z["h"]), z["wend_w"]) <= 1e-14
+    assert SC.rel_err(k.gradient(z["x"], z["r"], z["h"]), z["wend_grad"]) <= 1e-14
+    base = np.zeros(len(z["in_x"]), dtype=sph.particle_dtype)
+    for name in base.dtype.names:
+        if "in_" + name in z.files:
+            base[name] = z["in_" + name]
+    for xs in (0, 1):
+        it = sph.Verlet(bool(xs))
+        a = it.predict(0.003, base.copy(), 0.0)
+        tag = "verlet_x%d" % xs
+        for f in ("x", "y", "vx", "vy", "rho"):
+            assert SC.rel_err(a[f], z[tag + "_pred_" + f]) <= 1e-15, (tag, f)
+        a = it.correct(0.003, a, 0.0)
+        for f in ("x", "y", "vx", "vy", "rho"):
+            assert SC.rel_err(a[f], z[tag + "_corr_" + f]) <= 1e-15, (tag, f)
+
+
 def _particle(sph, label):
     p = np.zeros(1, dtype=sph.particle_dtype)
     p["label"] = label

@@ -32,6 +32,24 @@ def test_kernels(oracle_lib):
         assert O.kernel_eval(0, [1.0], [h])[0] == pytest.approx(want, abs=1e-7)
 
 
+def test_wendland_and_verlet(oracle_lib):
+    """src/Kernels/Wendland.py and src/Integrators/Verlet.py against the
+    reference's own outputs."""
+    import oracle
+    z = SC.load("wendland_verlet")
+    assert SC.rel_err(oracle.kernel_eval(2, z["r"], z["h"]), z["wend_w"]) <= 1e-15
+    assert SC.rel_err(oracle.kernel_grad(2, z["x"], z["r"], z["h"]), z["wend_grad"]) <= 1e-15
+    for xs in (0, 1):
+        P = oracle.Particles(arrays={k[3:]: z[k] for k in z.files if k.startswith("in_")})
+        oracle.verlet_predict(P, 0.003)
+        tag = "verlet_x%d" % xs
+        for k in ("x", "y", "vx", "vy", "rho"):
+            assert np.array_equal(getattr(P, k), z[tag + "_pred_" + k]), (tag, k)
+        oracle.verlet_correct(P, 0.003, use_xsph=bool(xs))
+        for k in ("x", "y", "vx", "vy", "rho"):
+            assert np.array_equal(getattr(P, k), z[tag + "_corr_" + k]), (tag, k)
+
+
 def test_equations(oracle_lib):
     O = oracle_lib
     z = SC.load("equations")
