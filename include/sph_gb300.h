@@ -196,6 +196,29 @@ int sph_nn_count(const sph_particles_t *pa, const sph_config_t *cfg, const sph_w
 int sph_nn_export(const sph_particles_t *pa, const sph_config_t *cfg, const sph_workspace_t *ws, const int64_t *offsets,
                   int64_t *idx, sph_stream_t stream);
 
+/* NNLinkedList.nearPos (src/Tools/NNLinkedList.py:41-84) for np points
+ * (px, py, ph device arrays) on the table of the last build in ws (as the
+ * reference, distances use pa's current positions): the same count /
+ * offsets / export protocol as sph_nn_count / sph_nn_export, each list in
+ * ascending index order with its h_ij, q and r (device arrays, offsets[np]
+ * entries). */
+int sph_nn_probe_count(const sph_particles_t *pa, const sph_workspace_t *ws, int64_t np, const double *px,
+                       const double *py, const double *ph, int64_t *counts, sph_stream_t stream);
+int sph_nn_probe_export(const sph_particles_t *pa, const sph_workspace_t *ws, int64_t np, const double *px,
+                        const double *py, const double *ph, const int64_t *offsets, int64_t *idx, double *hij,
+                        double *q, double *r, sph_stream_t stream);
+
+/* Density and pressure at np points, the interpolation the reference's
+ * ice-coupling example builds from nearPos (examples/IceBreak.py:253-285):
+ * over the nearPos set of (px, py, h_search), W = kernel(r, h_kernel), the
+ * Shepard normalisation (src/Equations/Shepard.py) and summation density
+ * (src/Equations/SummationDensity.py) give rho = sum_fluid m W /
+ * sum_{fluid, rho >= 1e-3} W m / rho, and p = B ((rho / rho0)^gamma - 1).
+ * Uses the table of the last build in ws. */
+int sph_probe_density(const sph_particles_t *pa, const sph_wcsph_t *w, int kernel, const sph_workspace_t *ws,
+                      int64_t np, const double *px, const double *py, const double *h_search, const double *h_kernel,
+                      double *rho, double *p, sph_stream_t stream);
+
 /* Solver._compute (src/Solver.py:232-256) = NNLinkedList.update, the h reset
  * (fixed or computeH, src/Tools/SolverTools.py:106-118) and the derivative
  * loop _loop (src/Tools/SolverTools.py:120-175) as one fused pair kernel:

@@ -272,6 +272,44 @@ int sph_nn_export(const sph_particles_t *pa, const sph_config_t *cfg, const sph_
   return check_launch();
 }
 
+int sph_nn_probe_count(const sph_particles_t *pa, const sph_workspace_t *ws, int64_t np, const double *px,
+                       const double *py, const double *ph, int64_t *counts, sph_stream_t stream) {
+  if (!particles_ok(pa) || np < 0 || (np && (!px || !py || !ph || !counts))) return SPH_ERR_INVALID_ARGUMENT;
+  int e = ws_ok(ws, pa->n);
+  if (e) return e;
+  if (np == 0) return SPH_OK;
+  launch_nn_probe(step_args(pa), ws_ptrs(ws), np, px, py, ph, counts, nullptr, nullptr, nullptr, nullptr, nullptr,
+                  (cudaStream_t)stream);
+  return check_launch();
+}
+
+int sph_nn_probe_export(const sph_particles_t *pa, const sph_workspace_t *ws, int64_t np, const double *px,
+                        const double *py, const double *ph, const int64_t *offsets, int64_t *idx, double *hij,
+                        double *q, double *r, sph_stream_t stream) {
+  if (!particles_ok(pa) || np < 0 || (np && (!px || !py || !ph || !offsets || !idx || !hij || !q || !r)))
+    return SPH_ERR_INVALID_ARGUMENT;
+  int e = ws_ok(ws, pa->n);
+  if (e) return e;
+  if (np == 0) return SPH_OK;
+  launch_nn_probe(step_args(pa), ws_ptrs(ws), np, px, py, ph, nullptr, offsets, idx, hij, q, r, (cudaStream_t)stream);
+  return check_launch();
+}
+
+int sph_probe_density(const sph_particles_t *pa, const sph_wcsph_t *w, int kernel, const sph_workspace_t *ws,
+                      int64_t np, const double *px, const double *py, const double *h_search, const double *h_kernel,
+                      double *rho, double *p, sph_stream_t stream) {
+  if (!particles_ok(pa) || !w || np < 0 || (np && (!px || !py || !h_search || !h_kernel || !rho || !p)))
+    return SPH_ERR_INVALID_ARGUMENT;
+  if (kernel != SPH_KERNEL_CUBIC && kernel != SPH_KERNEL_GAUSSIAN && kernel != SPH_KERNEL_WENDLAND)
+    return SPH_ERR_INVALID_ARGUMENT;
+  int e = ws_ok(ws, pa->n);
+  if (e) return e;
+  if (np == 0) return SPH_OK;
+  launch_probe_density(step_args(pa), ws_ptrs(ws), kernel, np, px, py, h_search, h_kernel, w->rho0, w->B, w->gamma,
+                       rho, p, (cudaStream_t)stream);
+  return check_launch();
+}
+
 static void compute_body(const StepArgs &a, const WsPtrs &w, const sph_wcsph_t &wc, const sph_config_t &cfg,
                          double *dt_out, double *dt_hist, cudaStream_t st, const WallLoad *wall = nullptr) {
   const bool do_dt = dt_out != nullptr || dt_hist != nullptr;

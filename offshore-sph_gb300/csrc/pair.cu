@@ -954,6 +954,151 @@ __global__ void __launch_bounds__(kPairBlock, kListBlocks)
 }
 
 // ---------------------------------------------------------------------------
+// Probes: NNLinkedList.nearPos (src/Tools/NNLinkedList.py:41-84) at arbitrary
+// points, on the table of the last build, and the pressure interpolation the
+// reference's ice-coupling example composes from it (Shepard-normalised
+// summation density + Tait EOS, examples/IceBreak.py:253-285,
+// src/Equations/Shepard.py, src/Equations/SummationDensity.py).
+// ---------------------------------------------------------------------------
+// Raw reference cell (qref) of point (x, y), its own-grid cell key (clamped
+// binning; mode 1) and the stencil half-width W that covers q <= 3 for a
+// point with smoothing length h: r <= 1.5 (h + hmax).
+__device__ __forceinline__ int probe_cell(const DevGrid &g, double x, double y, double h, int2 &qref, int &W) {
+  const long long cx = ref_cell(x, g.xmin, g.cs, g.inv_cs, g.xminf, g.inv_csf);
+  const long long cy = ref_cell(y, g.ymin, g.cs, g.inv_cs, g.yminf, g.inv_csf);
+  qref = make_int2(sat_i32(cx), sat_i32(cy));
+  if (g.mode == 0) {
+    W = 1;
+    return 0;
+  }
+  const float tx = fminf(fmaxf((d2f_trunc(x) - g.oxf) * g.inv_ctf, 0.f), (float)(g.ntx - 1));
+  const float ty = fminf(fmaxf((d2f_trunc(y) - g.oyf) * g.inv_ctf, 0.f), (float)(g.nty - 1));
+  const int kx = min(max((int)floorf(tx), 0), g.ntx - 1), ky = min(max((int)floorf(ty), 0), g.nty - 1);
+  const double reach = 1.5 * (h + g.hmax) * (1.0 + 1e-6);
+  const double wd = ceil(reach / g.ct) + 1.0;
+  W = wd < 1.0 ? 1 : (wd > 1024.0 ? 1024 : (int)wd);
+  return tiled_key(kx, ky, g.ts, g.ntlx);
+}
+
+__global__ void __launch_bounds__(kPairBlock)
+    k_nn_probe(const double *__restrict__ px, const double *__restrict__ py, const double *__restrict__ ph,
+               long long np, const double *__restrict__ x, const double *__restrict__ y,
+               const double *__restrict__ h, const int *__restrict__ perm, const int2 *__restrict__ meta,
+               const unsigned int *__restrict__ cstart, const DevGrid *__restrict__ gp, int64_t *counts,
+               const int64_t *offsets, int64_t *idx, double *hij_out, double *q_out, double *r_out) {
+  const DevGrid g = *gp;
+  const long long k = (long long)blockIdx.x * blockDim.x + threadIdx.x;
+  if (k >= np) return;
+  const double xi = px[k], yi = py[k], hi = ph[k];
+  int2 qref;
+  int W;
+  const int qkey = probe_cell(g, xi, yi, hi, qref, W);
+  const bool filter = g.mode == 1;
+  long long cnt = 0;
+  const long long base = idx ? offsets[k] : 0;
+  const Stencil sten(g, qref, qkey, W);
+  for_stencil(sten, cstart, [&](unsigned int j) {
+    if (filter && !in_ref_stencil(meta, j, g, qref)) return;
+    const int pj = perm[j];
+    const double dx = xi - x[pj], dy = yi - y[pj];
+    const double r = __dsqrt_rn(__dadd_rn(__dmul_rn(dx, dx), __dmul_rn(dy, dy)));
+    const double hij = __dmul_rn(0.5, __dadd_rn(hi, h[pj]));
+    const double q = __ddiv_rn(r, hij);
+    if (q <= 3.0) {
+      if (idx) {
+        idx[base + cnt] = pj;
+        hij_out[base + cnt] = hij;
+        q_out[base + cnt] = q;
+        r_out[base + cnt] = r;
+      }
+      cnt++;
+    }
+  });
+  if (!idx) {
+    counts[k] = cnt;
+    return;
+  }
+  for (long long s = 1; s < cnt; s++) {  // ascending particle index
+    const int64_t v = idx[base + s];
+    const double a0 = hij_out[base + s], a1 = q_out[base + s], a2 = r_out[base + s];
+    long long t = s - 1;
+    while (t >= 0 && idx[base + t] > v) {
+      idx[base + t + 1] = idx[base + t];
+      hij_out[base + t + 1] = hij_out[base + t];
+      q_out[base + t + 1] = q_out[base + t];
+      r_out[base + t + 1] = r_out[base + t];
+      t--;
+    }
+    idx[base + t + 1] = v;
+    hij_out[base + t + 1] = a0;
+    q_out[base + t + 1] = a1;
+    r_out[base + t + 1] = a2;
+  }
+}
+
+// rho = sum_fluid m_j W(r_j, hk) / sum_{fluid, rho_j >= 1e-3} W(r_j, hk) m_j / rho_j over
+// the nearPos set of (x, y, h_search); p = B ((rho / rho0)^gamma - 1)
+template <int KERNEL>
+__global__ void __launch_bounds__(kPairBlock)
+    k_probe_density(const double *__restrict__ px, const double *__restrict__ py, const double *__restrict__ ph,
+                    const double *__restrict__ hk, long long np, StepArgs a, const int *__restrict__ perm,
+                    const int2 *__restrict__ meta, const unsigned int *__restrict__ cstart,
+                    const DevGrid *__restrict__ gp, double rho0, double B, double gamma, double *rho_out,
+                    double *p_out) {
+  const DevGrid g = *gp;
+  const long long k = (long long)blockIdx.x * blockDim.x + threadIdx.x;
+  if (k >= np) return;
+  const double xi = px[k], yi = py[k], hi = ph[k], hw = hk[k];
+  int2 qref;
+  int W;
+  const int qkey = probe_cell(g, xi, yi, hi, qref, W);
+  const bool filter = g.mode == 1;
+  double shep = 0.0, sum = 0.0;
+  int nf = 0;
+  const Stencil sten(g, qref, qkey, W);
+  for_stencil(sten, cstart, [&](unsigned int j) {
+    if (filter && !in_ref_stencil(meta, j, g, qref)) return;
+    const int pj = perm[j];
+    const double dx = xi - a.x[pj], dy = yi - a.y[pj];
+    const double r = __dsqrt_rn(__dadd_rn(__dmul_rn(dx, dx), __dmul_rn(dy, dy)));
+    const double hij = __dmul_rn(0.5, __dadd_rn(hi, a.h[pj]));
+    if (!(__ddiv_rn(r, hij) <= 3.0)) return;
+    if (!is_fluid(a.label[pj])) return;  // Shepard and SummationDensity take fluid only
+    const double w = KERNEL == SPH_KERNEL_CUBIC ? cubic_w(r, hw)
+                                                : (KERNEL == SPH_KERNEL_WENDLAND ? wendland_w(r, hw) : gauss_w(r, hw));
+    const double m = a.m[pj], rho = a.rho[pj];
+    if (!(rho < 1e-3)) shep += w * m / rho;
+    sum += m * w;
+    nf++;
+  });
+  const double rho = nf ? sum / shep : 0.0;  // an empty sum without fluid neighbours
+  rho_out[k] = rho;
+  p_out[k] = (pow(rho / rho0, gamma) - 1.0) * B;
+}
+
+void launch_nn_probe(const StepArgs &a, const WsPtrs &w, long long np, const double *px, const double *py,
+                     const double *ph, int64_t *counts, const int64_t *offsets, int64_t *idx, double *hij, double *q,
+                     double *r, cudaStream_t st) {
+  k_nn_probe<<<nblocks(np, kPairBlock), kPairBlock, 0, st>>>(px, py, ph, np, a.x, a.y, a.h, w.perm, w.meta, w.cstart,
+                                                              w.grid, counts, offsets, idx, hij, q, r);
+}
+
+void launch_probe_density(const StepArgs &a, const WsPtrs &w, int kernel, long long np, const double *px,
+                          const double *py, const double *ph, const double *hk, double rho0, double B, double gamma,
+                          double *rho, double *p, cudaStream_t st) {
+  const unsigned nb = nblocks(np, kPairBlock);
+  if (kernel == SPH_KERNEL_CUBIC)
+    k_probe_density<SPH_KERNEL_CUBIC><<<nb, kPairBlock, 0, st>>>(px, py, ph, hk, np, a, w.perm, w.meta, w.cstart,
+                                                                  w.grid, rho0, B, gamma, rho, p);
+  else if (kernel == SPH_KERNEL_WENDLAND)
+    k_probe_density<SPH_KERNEL_WENDLAND><<<nb, kPairBlock, 0, st>>>(px, py, ph, hk, np, a, w.perm, w.meta, w.cstart,
+                                                                     w.grid, rho0, B, gamma, rho, p);
+  else
+    k_probe_density<SPH_KERNEL_GAUSSIAN><<<nb, kPairBlock, 0, st>>>(px, py, ph, hk, np, a, w.perm, w.meta, w.cstart,
+                                                                     w.grid, rho0, B, gamma, rho, p);
+}
+
+// ---------------------------------------------------------------------------
 // Launchers
 // ---------------------------------------------------------------------------
 static PairPtrs pair_ptrs(const WsPtrs &w) {

@@ -690,6 +690,12 @@ void launch_pair(const StepArgs &a, const WsPtrs &w, const sph_config_t &cfg, co
 void launch_sum_fixed(const double *v, long long n, double *out, cudaStream_t st);
 void launch_adjoint_step(const StepArgs &s, const StepArgs &h, const WsPtrs &w, const sph_config_t &cfg,
                          const sph_wcsph_t &wc, const sph_adjoint_t &adj, cudaStream_t st);
+void launch_nn_probe(const StepArgs &a, const WsPtrs &w, long long np, const double *px, const double *py,
+                     const double *ph, int64_t *counts, const int64_t *offsets, int64_t *idx, double *hij, double *q,
+                     double *r, cudaStream_t st);
+void launch_probe_density(const StepArgs &a, const WsPtrs &w, int kernel, long long np, const double *px,
+                          const double *py, const double *ph, const double *hk, double rho0, double B, double gamma,
+                          double *rho, double *p, cudaStream_t st);
 void launch_sumdens(const StepArgs &a, const WsPtrs &w, const sph_config_t &cfg, const sph_wcsph_t &wc,
                     cudaStream_t st);
 void launch_nn_count(const StepArgs &a, const WsPtrs &w, int64_t *counts, const int64_t *offsets, int64_t *idx,

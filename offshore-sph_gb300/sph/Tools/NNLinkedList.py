@@ -46,6 +46,13 @@ class NNLinkedList:
         return (hij.cpu().numpy(), (r / hij).cpu().numpy(), r.cpu().numpy(),
                 nb.cpu().numpy().astype(np.uint64))
 
-    def nearPos(self, x: float, y: float, h: float, pA):
-        raise NotImplementedError("point queries (NNLinkedList.nearPos) are not on the device path yet; "
-                                  "use near(i) or neighbour_sets()")
+    def nearPos(self, x: float, y: float, h: float, pA=None):
+        """(h_ij, q, r, nbrs) of the point (x, y) with smoothing length h on
+        the table of the last update (NNLinkedList.py:41-82), on the device."""
+        return self.nearPos_many([x], [y], [h])[0]
+
+    def nearPos_many(self, x, y, h):
+        """nearPos for many points at once: a list of (h_ij, q, r, nbrs)."""
+        off, idx, hij, q, r = core.nn_probe(self._dp, self._ws, x, y, h)
+        return [(hij[off[k]:off[k + 1]], q[off[k]:off[k + 1]], r[off[k]:off[k + 1]],
+                 idx[off[k]:off[k + 1]].astype(np.uint64)) for k in range(len(off) - 1)]

@@ -66,7 +66,8 @@ EXPORTS = ("sph_abi_version", "sph_workspace_size", "sph_default_max_cells", "sp
            "sph_nn_count", "sph_nn_export", "sph_compute", "sph_timestep", "sph_predict", "sph_correct",
            "sph_run", "sph_kernel_eval", "sph_kernel_grad", "sph_gauss_deriv", "sph_run_profiled",
            "sph_compute_static", "sph_run_wall_load", "sph_adjoint_step", "sph_batch_workspace_size",
-           "sph_batch_setup", "sph_batch_instance_cells", "sph_batch_run")
+           "sph_batch_setup", "sph_batch_instance_cells", "sph_batch_run", "sph_nn_probe_count",
+           "sph_nn_probe_export", "sph_probe_density")
 SPH_ERR_STATIC_LIMIT = 5
 STATIC_MAX_PARTICLES = 32768
 
@@ -119,6 +120,9 @@ def load():
                                       C.c_int32, vp]),
         "sph_batch_instance_cells": (C.c_int64, [WS, C.c_int64, C.POINTER(C.c_int64), C.c_int64]),
         "sph_batch_run": (C.c_int, [PP, CP, WS, C.c_int64, C.c_int64, vp, C.c_int32, vp]),
+        "sph_nn_probe_count": (C.c_int, [PP, WS, C.c_int64, vp, vp, vp, vp, vp]),
+        "sph_nn_probe_export": (C.c_int, [PP, WS, C.c_int64, vp, vp, vp, vp, vp, vp, vp, vp, vp]),
+        "sph_probe_density": (C.c_int, [PP, WP, C.c_int, WS, C.c_int64, vp, vp, vp, vp, vp, vp, vp]),
     }
     for name, (res, args) in sig.items():
         f = getattr(L, name)

@@ -110,6 +110,49 @@ def nn_export(dp, cfg, ws):
     return offsets.cpu().numpy(), idx[:total].cpu().numpy()
 
 
+def _dev(v, n=None):
+    t = torch.as_tensor(v, dtype=torch.float64, device="cuda").reshape(-1).contiguous()
+    if n is not None and t.numel() == 1 and n > 1:
+        t = t.expand(n).contiguous()
+    return t
+
+
+def nn_probe(dp, ws, px, py, ph):
+    """NNLinkedList.nearPos for many points on the table of the last build:
+    (offsets[np+1], idx, h_ij, q, r) as numpy, each list ascending."""
+    lib = L.load()
+    px = _dev(px)
+    n = px.numel()
+    py, ph = _dev(py, n), _dev(ph, n)
+    counts = torch.zeros(n, dtype=torch.int64, device=dp.device)
+    L.check(lib.sph_nn_probe_count(_P(dp), C.byref(ws.ws), n, px.data_ptr(), py.data_ptr(), ph.data_ptr(),
+                                   counts.data_ptr(), current_stream()), "sph_nn_probe_count")
+    offsets = torch.zeros(n + 1, dtype=torch.int64, device=dp.device)
+    offsets[1:] = torch.cumsum(counts, 0)
+    total = int(offsets[-1].item())
+    idx = torch.zeros(max(total, 1), dtype=torch.int64, device=dp.device)
+    hij, q, r = (torch.zeros(max(total, 1), dtype=torch.float64, device=dp.device) for _ in range(3))
+    L.check(lib.sph_nn_probe_export(_P(dp), C.byref(ws.ws), n, px.data_ptr(), py.data_ptr(), ph.data_ptr(),
+                                    offsets.data_ptr(), idx.data_ptr(), hij.data_ptr(), q.data_ptr(), r.data_ptr(),
+                                    current_stream()), "sph_nn_probe_export")
+    return (offsets.cpu().numpy(), idx[:total].cpu().numpy(), hij[:total].cpu().numpy(), q[:total].cpu().numpy(),
+            r[:total].cpu().numpy())
+
+
+def probe_density(dp, wc, kernel, ws, px, py, h_search, h_kernel):
+    """Density and pressure at points (Shepard-normalised summation density +
+    Tait EOS over the nearPos sets); device tensors (rho, p)."""
+    px = _dev(px)
+    n = px.numel()
+    py, hs, hk = _dev(py, n), _dev(h_search, n), _dev(h_kernel, n)
+    rho = torch.empty(n, dtype=torch.float64, device=dp.device)
+    p = torch.empty(n, dtype=torch.float64, device=dp.device)
+    L.check(L.load().sph_probe_density(_P(dp), C.byref(wc), int(kernel), C.byref(ws.ws), n, px.data_ptr(),
+                                       py.data_ptr(), hs.data_ptr(), hk.data_ptr(), rho.data_ptr(), p.data_ptr(),
+                                       current_stream()), "sph_probe_density")
+    return rho, p
+
+
 def kernel_eval(kernel, r, h):
     r = torch.as_tensor(r, dtype=torch.float64, device="cuda").contiguous()
     h = torch.as_tensor(h, dtype=torch.float64, device="cuda").contiguous()

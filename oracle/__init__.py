@@ -304,6 +304,34 @@ def verlet_correct(P, dt, use_xsph=False, mask=None):
     lib().or_verlet_correct(C.byref(s), mp, dt, int(bool(use_xsph)))
 
 
+def probe_density(nn, P, x, y, h_search, h_kernel, kernel, rho0, B, gamma):
+    """The ice-coupling example's pressure interpolation at points
+    (examples/IceBreak.py:253-285): nearPos (the C restatement), kernel values
+    W(r, h_kernel), Shepard normalisation (src/Equations/Shepard.py:5-12),
+    summation density (src/Equations/SummationDensity.py:5-13), Tait EOS.
+    Returns (rho, p) arrays."""
+    rho_out, p_out = [], []
+    for xi, yi, hs, hk in zip(np.atleast_1d(x), np.atleast_1d(y), np.atleast_1d(h_search), np.atleast_1d(h_kernel)):
+        hij, q, r, idx = nn.near(float(xi), float(yi), float(hs))
+        w = kernel_eval(kernel, r, np.full(len(r), float(hk)))
+        lab, m, rb = P.label[idx], P.m[idx], P.rho[idx]
+        den = 0.0
+        for k in range(len(w)):
+            if rb[k] < 1e-3 or lab[k] != 0:
+                continue
+            den += w[k] * m[k] / rb[k]
+        with np.errstate(divide="ignore", invalid="ignore"):  # as the reference: w / 0 on empty or boundary-only sets
+            wt = w / den
+        rho = 0.0
+        for k in range(len(w)):
+            if lab[k] != 0:
+                continue
+            rho += m[k] * wt[k]
+        rho_out.append(rho)
+        p_out.append(((rho / rho0) ** gamma - 1.0) * B)
+    return np.array(rho_out), np.array(p_out)
+
+
 def loop(params, nn, P, nthreads=1):
     s = P.cstruct()
     return lib().or_loop(C.byref(params), nn.h, C.byref(s), nthreads)

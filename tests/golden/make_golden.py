@@ -260,6 +260,54 @@ def gen_extra(ref):
     _save("wendland_verlet.npz", **res)
 
 
+def gen_probes(ref):
+    """nearPos at points and the ice-coupling example's pressure
+    interpolation (examples/IceBreak.py:253-285) on the small tank after
+    Solver.setup and one _compute."""
+    from src.Solver import Solver
+    from src.Methods.WCSPH import WCSPH
+    from src.Kernels.CubicSpline import CubicSpline
+    from src.Integrators.PEC import PEC
+    from src.Tools.NNLinkedList import NNLinkedList
+    from src.Equations.Shepard import Shepard
+    from src.Equations.SummationDensity import SummationDensity
+    from sph import scenarios as S
+    dx = 0.025
+    tank = S.dam_break(width=0.2, height=0.4, dx=dx, tank_width=0.8, tank_height=0.6)
+    method = WCSPH(height=0.4, r0=dx, rho0=1000.0, useXSPH=False, Pb=0.0, useSummationDensity=False)
+    solver = Solver(method, PEC(False, True), CubicSpline(), 1.0, incrementalWriteout=False, h=1.3 * dx, damping=0.0)
+    Solver.particleArray = None
+    solver.particleArray = None
+    solver.addParticles(tank.copy())
+    solver.setup()
+    solver._compute()
+    pA = solver.particleArray
+    nn = NNLinkedList(2.0)
+    nn.update(pA)
+    rng = np.random.default_rng(23)
+    px = np.concatenate([rng.uniform(-0.05, 0.85, 16), [0.1, 0.19, 0.01, 0.21, 0.4, -0.3, 1.2, 0.0]])
+    py = np.concatenate([rng.uniform(-0.05, 0.5, 16), [0.2, 0.39, 0.01, 0.05, 0.1, 0.2, 0.1, 0.0]])
+    h = 1.3 * dx
+    offs, idx, hijs, qs, rs, rhos, ps = [0], [], [], [], [], [], []
+    for x, y in zip(px, py):
+        hij, q, r, nb = nn.nearPos(float(x), float(y), h, pA)
+        order = np.argsort(nb)
+        idx.extend(nb[order].tolist())
+        hijs.extend(np.asarray(hij)[order].tolist())
+        qs.extend(np.asarray(q)[order].tolist())
+        rs.extend(np.asarray(r)[order].tolist())
+        offs.append(len(idx))
+        w = CubicSpline.evaluate(np.asarray(r, dtype=np.float64), np.ones(len(nb)) * h)
+        wt = Shepard(w, pA[nb]["label"], pA[nb]["m"], pA[nb]["rho"])
+        rho = SummationDensity(pA[nb]["label"], pA[nb]["m"], wt)
+        p = ((rho / method.rho0) ** method.gamma - 1.0) * method.B
+        rhos.append(rho)
+        ps.append(p)
+    _save("probes.npz", px=px, py=py, h=h, offsets=np.array(offs), idx=np.array(idx, dtype=np.int64),
+          hij=np.array(hijs), q=np.array(qs), r=np.array(rs), rho=np.array(rhos), p=np.array(ps),
+          **{"st_" + k: np.array(pA[k]) for k in pA.dtype.names if k != "deleted"})
+
+
 def _nn_case(name, pa, scale=2.0):
     from src.Tools.NNLinkedList import NNLinkedList
     nn = NNLinkedList(scale)
@@ -452,7 +500,7 @@ def main():
         sys.exit("--ref must point at an Offshore-SPH checkout")
     _install_shims()
     sys.path.insert(0, a.ref)
-    gens = dict(kernels=gen_kernels, equations=gen_equations, eos=gen_eos_integrators, nn=gen_nn, extra=gen_extra)
+    gens = dict(kernels=gen_kernels, equations=gen_equations, eos=gen_eos_integrators, nn=gen_nn, extra=gen_extra, probes=gen_probes)
     for k, g in gens.items():
         if a.only and k not in a.only.split(","):
             continue

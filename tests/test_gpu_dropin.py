@@ -66,6 +66,39 @@ def test_wendland_and_verlet_match_reference(sph):
             assert SC.rel_err(a[f], z[tag + "_corr_" + f]) <= 1e-15, (tag, f)
 
 
+def test_probes_match_reference(sph):
+    """NNLinkedList.nearPos and the ice-coupling pressure interpolation
+    (examples/IceBreak.py:253-285) at 24 points, on the reference's tank state."""
+    from sph import core, state
+    from sph.Tools import Probes
+    z = SC.load("probes")
+    pa = np.zeros(len(z["st_x"]), dtype=sph.particle_dtype)
+    for name in pa.dtype.names:
+        if "st_" + name in z.files:
+            pa[name] = z["st_" + name]
+    nn = sph.NNLinkedList(2.0)
+    nn.update(pa)
+    h = float(z["h"])
+    res = nn.nearPos_many(z["px"], z["py"], np.full(len(z["px"]), h))
+    off = z["offsets"]
+    for k, (hij, q, r, nb) in enumerate(res):
+        assert np.array_equal(nb.astype(np.int64), z["idx"][off[k]:off[k + 1]]), k
+        assert SC.rel_err(r, z["r"][off[k]:off[k + 1]]) <= 1e-15 and SC.rel_err(q, z["q"][off[k]:off[k + 1]]) <= 1e-15
+    hij, q, r, nb = nn.nearPos(float(z["px"][0]), float(z["py"][0]), h, pa)
+    assert np.array_equal(nb.astype(np.int64), z["idx"][off[0]:off[1]])
+    # the pressure probe on a solver holding this state
+    solver = sph.Solver(sph.WCSPH(0.4, 0.025, 1000.0, False, 0.0), sph.PEC(False, True), sph.CubicSpline(), 1.0,
+                        h=h, incrementalWriteout=False)
+    solver.addParticles(pa.copy())
+    solver._masks()
+    solver._upload()
+    core.nn_update(solver._dp, solver._cfg(), solver._ws)
+    rho, p = Probes.pressure_SPH(z["px"], z["py"], solver, h)
+    ok = np.isfinite(z["rho"])
+    assert np.array_equal(np.isfinite(rho), ok)
+    assert SC.rel_err(rho[ok], z["rho"][ok]) <= 1e-13 and SC.rel_err(p[ok], z["p"][ok]) <= 1e-11
+
+
 def _particle(sph, label):
     p = np.zeros(1, dtype=sph.particle_dtype)
     p["label"] = label

@@ -50,6 +50,30 @@ def test_wendland_and_verlet(oracle_lib):
             assert np.array_equal(getattr(P, k), z[tag + "_corr_" + k]), (tag, k)
 
 
+def test_probes(oracle_lib):
+    """nearPos at points and the ice-coupling example's pressure interpolation
+    (examples/IceBreak.py:253-285) against the reference's outputs."""
+    import oracle
+    z = SC.load("probes")
+    P = oracle.Particles(arrays={k[3:]: z[k] for k in z.files if k.startswith("st_")})
+    nn = oracle.NN(2.0)
+    nn.update(P.x, P.y, P.h)
+    h = float(z["h"])
+    off = z["offsets"]
+    for k, (x, y) in enumerate(zip(z["px"], z["py"])):
+        hij, q, r, idx = nn.near(float(x), float(y), h)
+        o = np.argsort(idx)
+        want = z["idx"][off[k]:off[k + 1]]
+        assert np.array_equal(idx[o], want), k
+        assert np.array_equal(r[o], z["r"][off[k]:off[k + 1]]) and np.array_equal(q[o], z["q"][off[k]:off[k + 1]])
+    par = oracle.wcsph_params(0.4, 0.025, 1000.0)
+    rho, p = oracle.probe_density(nn, P, z["px"], z["py"], np.full(len(z["px"]), h), np.full(len(z["px"]), h), 0,
+                                  1000.0, par.B, 7.0)
+    ok = np.isfinite(z["rho"])
+    assert np.array_equal(np.isfinite(rho), ok)
+    assert SC.rel_err(rho[ok], z["rho"][ok]) <= 1e-14 and SC.rel_err(p[ok], z["p"][ok]) <= 1e-12
+
+
 def test_equations(oracle_lib):
     O = oracle_lib
     z = SC.load("equations")
