@@ -66,6 +66,27 @@ def run(dp, wc, cfg, ws, nsteps, dt_hist=None):
                              current_stream()), "sph_run")
 
 
+class StepGraph:
+    """`steps` bare steps (sph_run) captured once in a CUDA graph; replay()
+    advances the state by that many steps with one launch from the host.
+    Capturing needs the device state and workspace to stay where they are."""
+
+    def __init__(self, dp, wc, cfg, ws, steps):
+        self.steps = int(steps)
+        self._keep = (wc, cfg)  # the ctypes blocks the launches were made from
+        side = torch.cuda.Stream()
+        side.wait_stream(torch.cuda.current_stream())
+        with torch.cuda.stream(side):
+            run(dp, wc, cfg, ws, 1)  # first-launch work outside the capture
+        torch.cuda.current_stream().wait_stream(side)
+        self.graph = torch.cuda.CUDAGraph()
+        with torch.cuda.graph(self.graph):
+            run(dp, wc, cfg, ws, self.steps)
+
+    def replay(self):
+        self.graph.replay()
+
+
 def run_profiled(dp, wc, cfg, ws, nsteps):
     """sph_run with CUDA-event laps per stage; returns {stage: ms summed over steps}."""
     ms = (C.c_double * len(L.STAGES))()
