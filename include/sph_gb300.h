@@ -263,6 +263,27 @@ int sph_timestep(const sph_particles_t *pa, const sph_wcsph_t *w, const sph_conf
 int sph_predict(sph_particles_t *pa, const sph_config_t *cfg, const double *dt, sph_stream_t stream);
 int sph_correct(sph_particles_t *pa, const sph_config_t *cfg, const double *dt, sph_stream_t stream);
 
+/* NewmarkBeta.predict / correct (src/Integrators/NewmarkBeta.py:41-69), the
+ * coupling integrator of Solver.run (src/Solver.py:381-382, 397-398), on the
+ * particles labelled SPH_COUPLED, dt read from the device double *dt.
+ * SPH_ERR_INVALID_ARGUMENT unless 2 beta >= gamma (NewmarkBeta.py:32). */
+int sph_newmark_predict(sph_particles_t *pa, double beta, double gamma, const double *dt, sph_stream_t stream);
+int sph_newmark_correct(sph_particles_t *pa, double beta, double gamma, const double *dt, sph_stream_t stream);
+
+/* Scratch bytes of sph_newmark_acceleration for n nodes and matrices with
+ * kl sub- and ku superdiagonals (0 <= kl, ku <= n - 1; n - 1: dense). */
+int sph_newmark_work_size(int64_t n, int32_t kl, int32_t ku, size_t *bytes);
+
+/* NewmarkBeta.acceleration (src/Integrators/NewmarkBeta.py:71-93):
+ * a = (M + C gamma dt + K beta dt^2)^-1 (F - K r - C v).  M, K, C: device
+ * n x (kl + ku + 1) row band storage (row i, column j at
+ * [i (kl + ku + 1) + j - i + kl]); F, r, v, a: device n-vectors; work:
+ * device scratch of work_bytes; info: device int32, set to 0, or to j + 1
+ * when pivot j is exactly zero (the matrix is singular; a is not written). */
+int sph_newmark_acceleration(int64_t n, int32_t kl, int32_t ku, const double *M, const double *K, const double *C,
+                             double beta, double gamma, double dt, const double *F, const double *r, const double *v,
+                             double *a, void *work, size_t work_bytes, int32_t *info, sph_stream_t stream);
+
 /* nsteps bare time steps of Solver.run's loop body (src/Solver.py:366-410)
  * with settling and storage left out: dt (TimeStep or cfg->dt_fixed) ->
  * predict -> _compute -> correct, all on the device.  dt_hist, if not NULL,

@@ -179,8 +179,12 @@ class Solver:
                 self.dt = self.timeStep
             dt_dev.fill_(self.dt)
             cfg = self._cfg()
+            if self.integrator.isMultiStage():
+                self._compute()
             start = perf_counter()
             core.predict(self._dp, cfg, dt_dev)
+            if self.coupling is not None:
+                self._coupled_update(dt_dev, predict=True)
             self.timing_data["integrate_prediction"] += perf_counter() - start
             self._compute()
             if self.coupling is not None:
@@ -191,6 +195,8 @@ class Solver:
                 self.timing_data["coupling"] += perf_counter() - start
             start = perf_counter()
             core.correct(self._dp, cfg, dt_dev)
+            if self.coupling is not None:
+                self._coupled_update(dt_dev, predict=False)
             self.timing_data["integrate_correction"] += perf_counter() - start
             start = perf_counter()
             self._store(t_step)
@@ -213,6 +219,20 @@ class Solver:
         self._download()
         self.timing_data["total"] = perf_counter() - start_all
         self.t_step = t_step
+
+    def _coupled_update(self, dt_dev, predict):
+        """couplingIntegrator.predict / correct of the Coupled particles
+        (Solver.py:381-382, 397-398): on the device for an integrator that
+        has a device path (NewmarkBeta), else on the host array."""
+        ci = self.couplingIntegrator
+        fn = getattr(ci, "device_predict" if predict else "device_correct", None)
+        if fn is not None:
+            fn(self._dp, dt_dev)
+            return
+        self._download()
+        c = self.c_indexes
+        self.particleArray[c] = (ci.predict if predict else ci.correct)(self.dt, self.particleArray[c], self.damping)
+        self._upload()
 
     def _settle(self):
         """End of settling (Solver.py:420-451): delete TempBoundary

@@ -18,9 +18,10 @@ from .Kernels.Wendland import Wendland
 from .Integrators.PEC import PEC
 from .Integrators.Euler import Euler
 from .Integrators.Verlet import Verlet
+from .Integrators.NewmarkBeta import NewmarkBeta
 from .Tools.NNLinkedList import NNLinkedList
 from .Equations.TimeStep import TimeStep
 from .Solver import Solver
 
 __all__ = ["ParticleType", "particle_dtype", "get_label_code", "WCSPH", "CubicSpline", "Gaussian", "Wendland", "PEC",
-           "Euler", "Verlet", "NNLinkedList", "TimeStep", "Solver"]
+           "Euler", "Verlet", "NewmarkBeta", "NNLinkedList", "TimeStep", "Solver"]

@@ -18,7 +18,7 @@ LIBDIR = os.path.join(PKG, "_lib")
 OBJDIR = os.path.join(ROOT, "_build")
 LIB = os.path.join(LIBDIR, "libsph_gb300.so")
 
-SOURCES = ["nn_build.cu", "pair.cu", "integrate.cu", "capi.cu", "static_ws.cu", "adjoint.cu", "batch.cu"]
+SOURCES = ["nn_build.cu", "pair.cu", "integrate.cu", "capi.cu", "static_ws.cu", "adjoint.cu", "batch.cu", "newmark.cu"]
 ARCH = ["-gencode", "arch=compute_103a,code=sm_103a"]
 FLAGS = ["-O3", "-std=c++17", "-lineinfo", "-Xcompiler", "-fPIC", "--expt-relaxed-constexpr",
          "-I", INCLUDE, "-I", CSRC]

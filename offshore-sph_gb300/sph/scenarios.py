@@ -15,6 +15,9 @@ Workloads (all 2D):
 * ``jittered_lattice`` -- an all-fluid square lattice with seeded position
   jitter, random velocities and densities (no boundaries).
 * ``ensemble``         -- seeded random dam breaks for the batched form.
+* ``beam_layer`` / ``beam_matrices`` -- a row of Coupled particles and the
+  clamped-free beam matrices of the ice-sheet coupling example, for
+  ``NewmarkBeta``.
 """
 import math
 
@@ -107,6 +110,37 @@ def ensemble(count=256, seed=1, width=(0.5, 2.0), height=(1.0, 3.0), dx=(0.02, 0
         pa = dam_break(width=wk, height=hk, dx=d[k], tank_width=4.0 * wk, tank_height=1.5 * hk, rho0=rho0)
         out.append((pa, dict(width=wk, height=hk, dx=float(d[k]))))
     return out
+
+
+def beam_layer(x0, x1, y, dx, mass=0.0, rho0=0.0):
+    """A row of Coupled particles from x0 to x1 at height y, dx apart (the
+    ice sheet of examples/IceBreak.py:76-78, one particle per beam node)."""
+    n = int(round((x1 - x0) / dx)) + 1
+    pa = np.zeros(n, dtype=particle_dtype)
+    pa["label"] = ParticleType.Coupled
+    pa["x"] = x0 + dx * np.arange(n)
+    pa["y"] = y
+    pa["m"] = mass
+    pa["rho"] = rho0
+    return pa
+
+
+def beam_matrices(n, E, I, A, rho, L_n):
+    """(K, M) of the coupling example's clamped-free Euler-Bernoulli beam
+    (examples/IceBreak.py:80-108): K = E I / L_n^4 times the central
+    fourth-difference operator, with the example's boundary rows at the
+    clamped (first) and free (last two) nodes; M = rho A times the identity."""
+    D = np.zeros((n, n))
+    for i in range(n):
+        for k, c in zip(range(-2, 3), (1.0, -4.0, 6.0, -4.0, 1.0)):
+            if 0 <= i + k < n:
+                D[i, i + k] = c
+    D[0, 0] = 7.0
+    D[n - 1, n - 1] = 2.0
+    D[n - 1, n - 3] = 2.0
+    D[n - 2, n - 1] = -2.0
+    D[n - 2, n - 2] = 5.0
+    return (E * I / L_n ** 4) * D, np.eye(n, n) * rho * A
 
 
 def count_fluid(pa):

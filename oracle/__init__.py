@@ -304,6 +304,35 @@ def verlet_correct(P, dt, use_xsph=False, mask=None):
     lib().or_verlet_correct(C.byref(s), mp, dt, int(bool(use_xsph)))
 
 
+def newmark_predict(P, dt, beta, gamma, mask=None):
+    """NewmarkBeta.predict (src/Integrators/NewmarkBeta.py:41-54) on the
+    particles in mask (all when None), elementwise in the reference's order."""
+    m = np.ones(len(P.x), dtype=bool) if mask is None else np.asarray(mask)
+    ax, ay = P.ax[m], P.ay[m]
+    P.x[m] = P.x[m] + P.vx[m] * dt + ax * (0.5 - beta) * dt ** 2
+    P.y[m] = P.y[m] + P.vy[m] * dt + ay * (0.5 - beta) * dt ** 2
+    P.vx[m] = P.vx[m] + ax * (1 - gamma) * dt
+    P.vy[m] = P.vy[m] + ay * (1 - gamma) * dt
+
+
+def newmark_correct(P, dt, beta, gamma, mask=None):
+    """NewmarkBeta.correct (src/Integrators/NewmarkBeta.py:56-69)."""
+    m = np.ones(len(P.x), dtype=bool) if mask is None else np.asarray(mask)
+    ax, ay = P.ax[m], P.ay[m]
+    P.x[m] = P.x[m] + ax * beta * dt ** 2
+    P.y[m] = P.y[m] + ay * beta * dt ** 2
+    P.vx[m] = P.vx[m] + ax * gamma * dt
+    P.vy[m] = P.vy[m] + ay * gamma * dt
+
+
+def newmark_acceleration(M, K, Cm, beta, gamma, dt, F, r, v):
+    """NewmarkBeta.acceleration (src/Integrators/NewmarkBeta.py:71-93):
+    inv(M + C gamma dt + K beta dt^2) . (F - K r - C v)."""
+    rhs = F - np.dot(K, r) - np.dot(Cm, v)
+    lhs = M + Cm * gamma * dt + K * beta * dt ** 2
+    return np.dot(np.linalg.inv(lhs), rhs)
+
+
 def probe_density(nn, P, x, y, h_search, h_kernel, kernel, rho0, B, gamma):
     """The ice-coupling example's pressure interpolation at points
     (examples/IceBreak.py:253-285): nearPos (the C restatement), kernel values

@@ -308,6 +308,84 @@ def gen_probes(ref):
           **{"st_" + k: np.array(pA[k]) for k in pA.dtype.names if k != "deleted"})
 
 
+def gen_newmark(ref):
+    """NewmarkBeta (src/Integrators/NewmarkBeta.py): predict / correct of
+    Coupled particles, acceleration of the coupling example's beam and of a
+    dense system; then Solver.run with a beam coupling function
+    (src/Solver.py:346-475 with coupling, couplingIntegrator)."""
+    from src.Common import particle_dtype
+    from src.Integrators.NewmarkBeta import NewmarkBeta
+    from sph import scenarios as S
+    sys.path.insert(0, os.path.dirname(HERE))
+    import sphcases as SC
+    res = {}
+    rng = np.random.default_rng(31)
+    f = np.zeros(40, dtype=particle_dtype)
+    f["label"] = 3
+    for k in ("x", "y", "vx", "vy", "ax", "ay"):
+        f[k] = rng.normal(0, 1, len(f))
+    for k in ("x", "y", "vx", "vy", "ax", "ay"):
+        res["in_" + k] = np.array(f[k])
+    n = 12
+    K0, M0 = S.beam_matrices(n, 2e6, 0.02 ** 3 / 12, 0.02, 917.0, 0.025)
+    for tag, (beta, gamma) in (("a", (0.25, 0.5)), ("b", (0.3025, 0.6))):
+        it = NewmarkBeta(beta, gamma, M0, K0, np.eye(n))
+        a = it.predict(0.0021, f.copy(), 0.0)
+        for k in ("x", "y", "vx", "vy"):
+            res[tag + "_pred_" + k] = np.array(a[k])
+        a = it.correct(0.0021, a, 0.0)
+        for k in ("x", "y", "vx", "vy"):
+            res[tag + "_corr_" + k] = np.array(a[k])
+    # accelerations: the beam (banded) and a dense, nonsymmetric system
+    M, K, C = SC.beam_case(S)[2]
+    nb = M.shape[0]
+    F, r, v = rng.normal(0, 10, nb), rng.normal(0, 1e-3, nb), rng.normal(0, 1e-2, nb)
+    res.update(beam_M=M, beam_K=K, beam_C=C, beam_F=F, beam_r=r, beam_v=v,
+               beam_a=NewmarkBeta(0.25, 0.5, M, K, C).acceleration(2.9e-4, F, r, v))
+    nd = 24
+    Md = np.diag(rng.uniform(1, 2, nd)) + 0.1 * rng.normal(0, 1, (nd, nd))
+    Kd = rng.normal(0, 50, (nd, nd))
+    Cd = rng.normal(0, 5, (nd, nd))
+    F, r, v = rng.normal(0, 1, nd), rng.normal(0, 1, nd), rng.normal(0, 1, nd)
+    res.update(dense_M=Md, dense_K=Kd, dense_C=Cd, dense_F=F, dense_r=r, dense_v=v,
+               dense_a=NewmarkBeta(0.3025, 0.6, Md, Kd, Cd).acceleration(0.01, F, r, v))
+    _save("newmark.npz", **res)
+    gen_coupled_run(ref)
+
+
+def gen_coupled_run(ref):
+    """Solver.run of the small tank with the beam of Coupled particles above
+    the water, coupling = sphcases.beam_coupling, NewmarkBeta(1/4, 1/2)."""
+    from src.Solver import Solver
+    from src.Methods.WCSPH import WCSPH
+    from src.Kernels.CubicSpline import CubicSpline
+    from src.Integrators.PEC import PEC
+    from src.Integrators.NewmarkBeta import NewmarkBeta
+    from sph import scenarios as S
+    sys.path.insert(0, os.path.dirname(HERE))
+    import sphcases as SC
+    pa, P, (M, K, C) = SC.beam_case(S)
+    dx = SC.BEAM["dx"]
+    method = WCSPH(height=0.4, r0=dx, rho0=1000.0, useXSPH=False, Pb=0.0, useSummationDensity=False)
+    solver = Solver(method, PEC(False, True), CubicSpline(), SC.BEAM_RUN["duration"], incrementalWriteout=False,
+                    h=1.3 * dx, maxSettle=SC.BEAM_RUN["maxSettle"], coupling=SC.beam_coupling,
+                    couplingIntegrator=NewmarkBeta(0.25, 0.5, M, K, C), couplingProperties=P,
+                    customSettle=SC.settle_now, exportProperties=["x", "y", "p"])
+    Solver.particleArray = None
+    solver.particleArray = None
+    solver.addParticles(pa.copy())
+    t0 = time.time()
+    solver.setup()
+    init = solver.particleArray.copy()
+    solver.run()
+    fin = solver.particleArray
+    _save("solver_coupled.npz", dt_a=np.array(solver.dt_a), t=solver.t, settleTime=solver.settleTime,
+          **{"init_" + k: np.array(init[k]) for k in init.dtype.names},
+          **{"final_" + k: np.array(fin[k]) for k in fin.dtype.names},
+          export_y=np.array(solver.export["y"]))
+    print("  solver_coupled: %.1f s, %d steps" % (time.time() - t0, len(solver.dt_a)))
+
+
 def _nn_case(name, pa, scale=2.0):
     from src.Tools.NNLinkedList import NNLinkedList
     nn = NNLinkedList(scale)
@@ -500,7 +578,8 @@ def main():
         sys.exit("--ref must point at an Offshore-SPH checkout")
     _install_shims()
     sys.path.insert(0, a.ref)
-    gens = dict(kernels=gen_kernels, equations=gen_equations, eos=gen_eos_integrators, nn=gen_nn, extra=gen_extra, probes=gen_probes)
+    gens = dict(kernels=gen_kernels, equations=gen_equations, eos=gen_eos_integrators, nn=gen_nn, extra=gen_extra, probes=gen_probes,
+                newmark=gen_newmark)
     for k, g in gens.items():
         if a.only and k not in a.only.split(","):
             continue

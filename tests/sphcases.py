@@ -78,3 +78,53 @@ def compare_state(got, want, fields, tol):
         if not (e <= tol):
             bad[k] = e
     return bad
+
+
+# ---------------------------------------------------------------------------
+# Beam coupling case (NewmarkBeta, Solver.run with a coupling function)
+# ---------------------------------------------------------------------------
+BEAM = dict(dx=0.025, E=2.0e6, thick=0.02, rho_ice=917.0, g=9.81, tip=5.0, xi=0.5)
+
+
+def beam_case(S):
+    """The small tank with a row of Coupled particles just above the water
+    (S: sph.scenarios); returns (particles, couplingProperties, (M, K, C))."""
+    b = BEAM
+    dx = b["dx"]
+    tank = S.dam_break(width=0.2, height=0.4, dx=dx, tank_width=0.8, tank_height=0.6)
+    y0 = 0.4 - dx / 2 + 0.9 * dx
+    beam = S.beam_layer(0.0125, 0.3125, y0, dx)
+    n = len(beam)
+    L_n = dx
+    A = b["thick"] * 1.0
+    I = b["thick"] ** 3 / 12.0
+    K, M = S.beam_matrices(n, b["E"], I, A, b["rho_ice"], L_n)
+    C = np.eye(n) * 2 * b["xi"] * np.sqrt(b["rho_ice"] * A * 1000.0 * b["g"])
+    P = dict(y0=y0, m=b["rho_ice"] * A, g=b["g"], tip=b["tip"], L_n=L_n)
+    return np.concatenate((tank, beam)), P, (M, K, C)
+
+
+def beam_coupling(pA, solver):
+    """A coupling function in the style of the ice-sheet example's model 0
+    (examples/IceBreak.py:110-178): beam weight on every node, a static tip
+    load on the last, Newmark-beta accelerations into ay."""
+    P = solver.couplingProperties
+    c = pA["label"] == 3
+    w = pA["y"][c] - P["y0"]
+    wdot = pA["vy"][c]
+    F = np.full(len(w), -P["m"] * P["g"])
+    F[-1] = F[-1] + P["tip"] / P["L_n"]
+    a = solver.couplingIntegrator.acceleration(solver.dt, F, w, wdot)
+    pA["ay"][c] = a
+    return pA
+
+
+BEAM_RUN = dict(duration=1.5e-3, maxSettle=2)
+
+
+def settle_now(pA, solver):
+    """customSettle: end the settling at the first check (the reference's
+    kinetic-energy check, src/Solver.py:416, passes the total particle count
+    as the loop length over the fluid-only array, which plain Python rejects
+    when boundaries exist)."""
+    return True

@@ -66,3 +66,19 @@ def test_invalid_arguments_rejected_on_host(lib):
     assert lib.sph_compute(C.byref(pa), C.byref(wc), C.byref(cfg), C.byref(ws), None) == 1  # invalid argument
     assert lib.sph_run(None, C.byref(wc), C.byref(cfg), C.byref(ws), 1, None, None) != 0
     assert lib.sph_compute(C.byref(pa), C.byref(wc), C.byref(bad), C.byref(ws), None) == 1
+
+
+def test_newmark_arguments_checked_on_host(lib):
+    from sph import _lib
+    nbytes = C.c_size_t()
+    assert lib.sph_newmark_work_size(40, 2, 2, C.byref(nbytes)) == 0
+    assert nbytes.value >= 40 * 7 * 8 + 40 * 8 + 40 * 4
+    assert lib.sph_newmark_work_size(40, 40, 0, C.byref(nbytes)) == 1  # band wider than the matrix
+    assert lib.sph_newmark_work_size(-1, 0, 0, C.byref(nbytes)) == 1
+    pa = _lib.Particles()
+    pa.n = 10  # null arrays
+    assert lib.sph_newmark_predict(C.byref(pa), 0.25, 0.5, None, None) == 1
+    assert lib.sph_newmark_correct(None, 0.25, 0.5, None, None) == 1
+    # 2 beta >= gamma (src/Integrators/NewmarkBeta.py:32)
+    assert lib.sph_newmark_acceleration(4, 0, 0, None, None, None, 0.1, 0.5, 1e-3, None, None, None, None, None,
+                                        0, None, None) == 1

@@ -236,3 +236,88 @@ def test_solver_run_settles_and_advances(sph, tmp_path):
     s2.load(path if os.path.exists(path) else path + ".npz")
     np.testing.assert_array_equal(s2.particleArray["x"], solver.particleArray["x"])
     assert len(s2.dt_a) == len(solver.dt_a)
+
+
+def test_newmark_matches_reference(sph):
+    """src/Integrators/NewmarkBeta.py: predict / correct bit for bit,
+    acceleration of the beam (banded) and of a dense system to rounding."""
+    z = SC.load("newmark")
+    n = 12
+    for tag, (beta, gamma) in (("a", (0.25, 0.5)), ("b", (0.3025, 0.6))):
+        pa = np.zeros(len(z["in_x"]), dtype=sph.particle_dtype)
+        pa["label"] = 3
+        for k in ("x", "y", "vx", "vy", "ax", "ay"):
+            pa[k] = z["in_" + k]
+        it = sph.NewmarkBeta(beta, gamma, np.eye(n), np.eye(n), np.eye(n))
+        pa = it.predict(0.0021, pa, 0.0)
+        for k in ("x", "y", "vx", "vy"):
+            assert np.array_equal(pa[k], z[tag + "_pred_" + k]), (tag, k)
+        pa = it.correct(0.0021, pa, 0.0)
+        for k in ("x", "y", "vx", "vy"):
+            assert np.array_equal(pa[k], z[tag + "_corr_" + k]), (tag, k)
+    for tag, (beta, gamma, dt) in (("beam", (0.25, 0.5, 2.9e-4)), ("dense", (0.3025, 0.6, 0.01))):
+        it = sph.NewmarkBeta(beta, gamma, z[tag + "_M"], z[tag + "_K"], z[tag + "_C"])
+        a = it.acceleration(dt, z[tag + "_F"], z[tag + "_r"], z[tag + "_v"])
+        assert SC.rel_err(a, z[tag + "_a"]) <= 1e-12, (tag, SC.rel_err(a, z[tag + "_a"]))
+    kl, ku = 2, 2
+    assert sph.Integrators.NewmarkBeta._bandwidths(z["beam_M"], z["beam_K"], z["beam_C"]) == (kl, ku)
+    with pytest.raises(AssertionError):
+        sph.NewmarkBeta(0.1, 0.5, np.eye(2), np.eye(2), np.eye(2))
+
+
+def test_newmark_singular_and_large_systems(sph):
+    """An exactly singular system raises LinAlgError like np.linalg.inv; a
+    300-node beam and a 200-node dense system agree with numpy."""
+    import oracle
+    z = np.zeros((3, 3))
+    it = sph.NewmarkBeta(0.25, 0.5, z, z, z)
+    with pytest.raises(np.linalg.LinAlgError):
+        it.acceleration(1e-3, np.ones(3), np.zeros(3), np.zeros(3))
+    from sph import scenarios as S
+    rng = np.random.default_rng(5)
+    K, M = S.beam_matrices(300, 5e9, 0.25 ** 3 / 12, 0.25, 917.0, 0.05)
+    Cm = np.eye(300) * 40.0
+    F, r, v = rng.normal(0, 1e3, 300), rng.normal(0, 1e-3, 300), rng.normal(0, 1e-2, 300)
+    a = sph.NewmarkBeta(0.25, 0.5, M, K, Cm).acceleration(1e-4, F, r, v)
+    want = oracle.newmark_acceleration(M, K, Cm, 0.25, 0.5, 1e-4, F, r, v)
+    assert SC.rel_err(a, want) <= 1e-10
+    Md = np.eye(200) * 3 + rng.normal(0, 0.1, (200, 200))
+    Kd, Cd = rng.normal(0, 10, (200, 200)), rng.normal(0, 1, (200, 200))
+    F, r, v = rng.normal(0, 1, 200), rng.normal(0, 1, 200), rng.normal(0, 1, 200)
+    a = sph.NewmarkBeta(0.25, 0.5, Md, Kd, Cd).acceleration(0.02, F, r, v)
+    want = oracle.newmark_acceleration(Md, Kd, Cd, 0.25, 0.5, 0.02, F, r, v)
+    assert SC.rel_err(a, want) <= 1e-10
+
+
+def test_solver_coupled_run_matches_reference(sph):
+    """Solver.run with a coupling function and NewmarkBeta as the coupling
+    integrator (src/Solver.py:366-410), against the reference's own run of
+    the same case: settling, Courant/force dt, fluid PEC, the beam's
+    Newmark-beta predict / correct and its accelerations."""
+    from sph import scenarios as S
+    z = SC.load("solver_coupled")
+    pa, P, (M, K, Cm) = SC.beam_case(S)
+    dx = SC.BEAM["dx"]
+    solver = sph.Solver(sph.WCSPH(0.4, dx, 1000.0, False, 0.0), sph.PEC(False, True), sph.CubicSpline(),
+                        SC.BEAM_RUN["duration"], incrementalWriteout=False, h=1.3 * dx,
+                        maxSettle=SC.BEAM_RUN["maxSettle"], coupling=SC.beam_coupling,
+                        couplingIntegrator=sph.NewmarkBeta(0.25, 0.5, M, K, Cm), couplingProperties=P,
+                        customSettle=SC.settle_now, exportProperties=["x", "y", "p"])
+    solver.addParticles(pa.copy())
+    solver.setup()
+    solver._download()
+    for k in SC.STATE_FIELDS:
+        assert SC.rel_err(solver.particleArray[k], z["init_" + k]) <= 1e-12, k  # pow / exp of the device
+    solver.run()
+    assert len(solver.dt_a) == len(z["dt_a"])
+    np.testing.assert_allclose(solver.dt_a, z["dt_a"], rtol=1e-9)
+    assert solver.settleTime == pytest.approx(float(z["settleTime"]), rel=1e-12)
+    assert solver.t == pytest.approx(float(z["t"]), rel=1e-9)
+    fin = solver.particleArray
+    bad = {k: SC.rel_err(fin[k], z["final_" + k]) for k in ("x", "y", "vx", "vy", "rho", "p", "ax", "ay", "drho")
+           if not SC.rel_err(fin[k], z["final_" + k]) <= 1e-8}
+    assert not bad, bad
+    c = fin["label"] == 3
+    for k in ("x", "y", "vx", "vy", "ay"):
+        assert SC.rel_err(fin[k][c], z["final_" + k][c]) <= 1e-8, k
+    assert SC.rel_err(np.array(solver.export["y"]), z["export_y"]) <= 1e-8

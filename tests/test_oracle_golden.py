@@ -50,6 +50,26 @@ def test_wendland_and_verlet(oracle_lib):
             assert np.array_equal(getattr(P, k), z[tag + "_corr_" + k]), (tag, k)
 
 
+def test_newmark(oracle_lib):
+    """src/Integrators/NewmarkBeta.py (predict, correct, acceleration) against
+    the reference's own outputs."""
+    import types
+    import oracle
+    z = SC.load("newmark")
+    for tag, (beta, gamma) in (("a", (0.25, 0.5)), ("b", (0.3025, 0.6))):
+        P = types.SimpleNamespace(**{k[3:]: z[k].copy() for k in z.files if k.startswith("in_")})
+        oracle.newmark_predict(P, 0.0021, beta, gamma)
+        for k in ("x", "y", "vx", "vy"):
+            assert np.array_equal(getattr(P, k), z[tag + "_pred_" + k]), (tag, k)
+        oracle.newmark_correct(P, 0.0021, beta, gamma)
+        for k in ("x", "y", "vx", "vy"):
+            assert np.array_equal(getattr(P, k), z[tag + "_corr_" + k]), (tag, k)
+    for tag, (beta, gamma, dt) in (("beam", (0.25, 0.5, 2.9e-4)), ("dense", (0.3025, 0.6, 0.01))):
+        a = oracle.newmark_acceleration(z[tag + "_M"], z[tag + "_K"], z[tag + "_C"], beta, gamma, dt,
+                                        z[tag + "_F"], z[tag + "_r"], z[tag + "_v"])
+        assert SC.rel_err(a, z[tag + "_a"]) <= 1e-13, tag
+
+
 def test_probes(oracle_lib):
     """nearPos at points and the ice-coupling example's pressure interpolation
     (examples/IceBreak.py:253-285) against the reference's outputs."""
