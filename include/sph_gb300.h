@@ -83,7 +83,10 @@ enum {
   /* no fluid particle to take the time step from */
   SPH_STATUS_NO_FLUID = 1u << 4,
   /* TimeStep's dt fell below 1e-6 (the reference records it, src/Solver.py:219-224) */
-  SPH_STATUS_SMALL_DT = 1u << 5
+  SPH_STATUS_SMALL_DT = 1u << 5,
+  /* a block of the pair tile kernel gave up waiting for its shared-memory
+   * staging copies (a bounded wait ran out); that evaluation is incomplete */
+  SPH_STATUS_STAGING_TIMEOUT = 1u << 6
 };
 
 /* WCSPH method constants, the attributes of src/Methods/WCSPH.py:33-79.

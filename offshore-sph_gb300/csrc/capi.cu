@@ -192,6 +192,7 @@ const char *sph_status_bit_string(uint32_t bit) {
     case SPH_STATUS_GRID_TOO_LARGE: return "reference grid exceeds 2^30 cells per axis";
     case SPH_STATUS_NO_FLUID: return "no fluid particle";
     case SPH_STATUS_SMALL_DT: return "time step below 1e-6";
+    case SPH_STATUS_STAGING_TIMEOUT: return "pair kernel staging wait timed out (evaluation incomplete)";
     default: return "unknown";
   }
 }

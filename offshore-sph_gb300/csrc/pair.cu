@@ -616,13 +616,15 @@ constexpr int kHaloScanPer = (kHaloCellsMax + 31) / 32;
 #define SPH_TILE_UNROLL_PAIRS 1
 #endif
 #ifndef SPH_TILE_UNROLL_CANDS
-#define SPH_TILE_UNROLL_CANDS 1
+#define SPH_TILE_UNROLL_CANDS 2
 #endif
 constexpr int kTileBlocks = SPH_TILE_BLOCKS;
 constexpr int kTileUnrollPairs = SPH_TILE_UNROLL_PAIRS;  // ILP over list entries
 constexpr int kTileUnrollCands = SPH_TILE_UNROLL_CANDS;  // ILP over stencil candidates
 constexpr int kHaloCap = SPH_HALO_CAP;  // particles of one halo in shared memory
 static_assert(kHaloCap <= 65535, "list entries are 16-bit");
+static_assert(kHaloCellsMax < 256, "query map entries are 8-bit halo cells");
+static_assert(kHaloCap * 48 < (1 << 20), "an mbarrier phase counts fewer than 2^20 bytes");
 
 __device__ __forceinline__ void fb_push(DevCtrl *ctrl, int2 *fb, unsigned int fb_cap, unsigned int s,
                                         unsigned int len) {
@@ -656,14 +658,31 @@ __device__ __forceinline__ TileGeom tile_geom(const DevGrid &g, double r0, int c
   return tg;
 }
 
+// Per-block state of the tile kernels' staging: the mbarrier the bulk copies
+// complete on and the phase of the next tile.
+struct TileSync {
+  unsigned long long *bar;
+  uint32_t phase;
+  bool abort;  // a staging wait ran out: the block stops
+};
+
 // One tile (see above): stage its halo, run its queries.  Returns this
 // thread's largest encoded a^2 over its queries.  All threads of the block
 // call it together.
+//   1. halo table: every halo cell's first sorted slot and count;
+//   2. warp 0: exclusive scan of the counts (shared-memory offsets), then the
+//      halo's records as bulk asynchronous copies, one per contiguous run of
+//      cells (the cells of one halo row inside one tile are consecutive ids,
+//      so their records are one global range) and record array, completing
+//      on the block's mbarrier; meanwhile the other threads map each query of
+//      the tile to its halo cell;
+//   3. after the (bounded) wait, each query walks its stencil rows.
 template <int KERNEL, bool XSPH, bool SUMDENS>
 __device__ __forceinline__ unsigned long long tile_process(const StepArgs &a, const PairPtrs &P, const TileGeom &tg,
                                                            const MixedConsts &mc, int t, float4 *h0, float4 *h1,
                                                            float4 *h2, unsigned short (*lists)[kPairBlock],
-                                                           unsigned int *hoff, unsigned int *hgs, DevCtrl *ctrl,
+                                                           unsigned int *hoff, unsigned int *hgs,
+                                                           unsigned char *qmap, TileSync &sync, DevCtrl *ctrl,
                                                            int2 *fb, unsigned int fb_cap) {
   constexpr int kListCap = ListCap<KERNEL>::value;
   const int tid = threadIdx.x;
@@ -672,7 +691,7 @@ __device__ __forceinline__ unsigned long long tile_process(const StepArgs &a, co
   unsigned long long ea = kEncMaxId;
   const unsigned int qs = __ldg(&cst[t << (2 * ts)]), qe = __ldg(&cst[(t + 1) << (2 * ts)]);
   const int ox = (t % ntlx) * T - W, oy = (t / ntlx) * T - W;
-  // halo table: counts and first slots
+  // 1. halo table: counts and first slots
   for (int c = tid; c < HC; c += kPairBlock) {
     const int x = ox + c % HW, y = oy + c / HW;
     unsigned int gs = 0, cnt = 0;
@@ -685,7 +704,7 @@ __device__ __forceinline__ unsigned long long tile_process(const StepArgs &a, co
     hoff[c] = cnt;
   }
   __syncthreads();
-  if (tid < 32) {  // exclusive scan of the counts, kHaloScanPer cells per lane
+  if (tid < 32) {  // 2. exclusive scan of the counts, kHaloScanPer cells per lane
     const int c0 = tid * kHaloScanPer;
     unsigned int v[kHaloScanPer], sum = 0;
 #pragma unroll
@@ -706,41 +725,78 @@ __device__ __forceinline__ unsigned long long tile_process(const StepArgs &a, co
       run += v[u];
     }
     if (tid == 31) hoff[HC] = inc;
+    const unsigned int tot = __shfl_sync(0xffffffffu, inc, 31);
+    __syncwarp();
+    if (tot > 0 && tot <= (unsigned)kHaloCap) {
+      // the previous tile's shared-memory reads (generic proxy) come before
+      // these copies (async proxy)
+      fence_proxy_async_smem();
+      if (tid == 0) mbar_arrive_expect_tx(sync.bar, tot * 48u);
+      __syncwarp();
+      for (int y = tid; y < HW; y += 32) {  // halo row y: runs of cells inside one tile
+        const int gy = oy + y;
+        if (gy < 0 || gy >= tg.nty) continue;
+        int x = ox > 0 ? ox : 0;
+        const int xe = ox + HW < tg.ntx ? ox + HW : tg.ntx;
+        while (x < xe) {
+          const int tile_end = ((x >> ts) + 1) << ts;
+          const int re = tile_end < xe ? tile_end : xe;
+          const int ca = y * HW + (x - ox), cb = y * HW + (re - ox);
+          const unsigned int s0 = hoff[ca], n = hoff[cb] - s0;
+          if (n) {
+            const unsigned int g0 = hgs[ca];
+            bulk_copy_g2s(h0 + s0, P.rec0 + g0, n * 16u, sync.bar);
+            bulk_copy_g2s(h1 + s0, P.rec1 + g0, n * 16u, sync.bar);
+            bulk_copy_g2s(h2 + s0, P.rec2 + g0, n * 16u, sync.bar);
+          }
+          x = re;
+        }
+      }
+    }
   }
   __syncthreads();
   const unsigned int total = hoff[HC];
+  if (total == 0) {  // nothing staged (a listed tile holds particles)
+    __syncthreads();
+    return ea;
+  }
   if (total > (unsigned)kHaloCap) {  // halo does not fit: global path
     if (tid == 0)
       for (unsigned int s = qs; s < qe; s += kPairBlock) fb_push(ctrl, fb, fb_cap, s, min((unsigned)kPairBlock, qe - s));
     __syncthreads();
     return ea;
   }
-  // stage the halo's records: slot s belongs to the last cell whose offset is <= s
-  for (unsigned int s = tid; s < total; s += kPairBlock) {
-    int lo = 0, hi = HC;
-    while (hi - lo > 1) {
-      const int mid = (lo + hi) >> 1;
-      if (hoff[mid] <= s) lo = mid;
-      else hi = mid;
-    }
-    const unsigned int gsl = hgs[lo] + (s - hoff[lo]);
-    h0[s] = P.rec0[gsl];
-    h1[s] = P.rec1[gsl];
-    h2[s] = P.rec2[gsl];
+  // query -> halo cell, for the tile's own cells (their sorted slots are the
+  // tile's query range, in cell order)
+  for (int c = tid; c < T * T; c += kPairBlock) {
+    const int hc = (W + c / T) * HW + W + c % T;
+    const unsigned int cnt = hoff[hc + 1] - hoff[hc], base = hgs[hc] - qs;
+    for (unsigned int u = 0; u < cnt; u++) qmap[base + u] = (unsigned char)hc;
   }
-  __syncthreads();
-  // per-query candidate radius: the padded reach of the largest pair h
+  const uint32_t parity = sync.phase & 1u;
+  sync.phase++;
+  const bool ok = mbar_wait_bounded(sync.bar, parity);
+  if (__syncthreads_or(!ok)) {  // the copies did not land: flag, drain, stop this block
+    if (tid == 0) atomicOr(&ctrl->status, (unsigned)SPH_STATUS_STAGING_TIMEOUT);
+    mbar_wait_bounded(sync.bar, parity);
+    sync.abort = true;
+    __syncthreads();
+    return ea;
+  }
+  // 3. queries.  Candidate radius: the padded reach of the largest pair h
   // (every |h| <= hmaxf), so that one compare per candidate suffices
   const float SK = (float)Support<KERNEL>::q * 1.000002f;  // support / h, padded
-  for (unsigned int k = qs + tid; k < qe; k += kPairBlock) {
-    int cx, cy;
-    tiled_cell(P.keys_sorted[k] - tg.cell0, ts, ntlx, cx, cy);
-    const int hx = cx - ox, hy = cy - oy, hc = hy * HW + hx;
+  const unsigned int nq = qe - qs;
+  for (unsigned int q = tid; q < nq; q += kPairBlock) {
+    const int hc = qmap[q];
+    const int hx = hc % HW, hy = hc / HW;
+    const unsigned int k = qs + q;
     const unsigned int sq = hoff[hc] + (k - hgs[hc]);  // the query's own shared-memory slot
     const float4 Qi = h0[sq];
     const float hif = Qi.z;
     if (signbit(hif)) continue;  // queries are fluid
-    if (P.meta[k].x >= tg.ncx || !(hif > 0.f)) {  // aliased query or h <= 0
+    // an x-overflow alias (reference cells only) or h <= 0: global path
+    if ((tg.W == 1 && P.meta[k].x >= tg.ncx) || !(hif > 0.f)) {
       fb_push(ctrl, fb, fb_cap, k, 1u);
       continue;
     }
@@ -760,23 +816,29 @@ __device__ __forceinline__ unsigned long long tile_process(const StepArgs &a, co
     int nl = 0;
     for (int r = -W; r <= W; r++) {
       const unsigned int *row = hoff + (hy + r) * HW + hx;
-      const unsigned int s1 = row[W + 1];
+      unsigned int j = row[-W];
+      const unsigned int e = row[W + 1];
+      while (j < e) {
+        if (nl == kListCap) {
+          physics(nl);
+          nl = 0;
+        }
+        // a chunk that cannot overflow the list: every candidate is written
+        // and kept (counted) when inside the radius; j == sq, the particle
+        // itself, contributes zero
+        const unsigned int ce = min(e, j + (unsigned int)(kListCap - nl));
 #pragma unroll kTileUnrollCands
-      for (unsigned int j = row[-W]; j < s1; j++) {
-        const float4 qj = h0[j];
-        const float dx = Qi.x - qj.x, dy = Qi.y - qj.y;
-        if (fmaf(dx, dx, dy * dy) <= rq2 && j != sq) {  // j == sq: the particle itself contributes zero
+        for (; j < ce; j++) {
+          const float2 p = *reinterpret_cast<const float2 *>(h0 + j);
+          const float dx = Qi.x - p.x, dy = Qi.y - p.y;
           lists[nl][tid] = (unsigned short)j;
-          if (++nl == kListCap) {
-            physics(nl);
-            nl = 0;
-          }
+          nl += (fmaf(dx, dx, dy * dy) <= rq2 && j != sq) ? 1 : 0;
         }
       }
     }
     physics(nl);
-    const unsigned long long q = mixed_store<XSPH, SUMDENS>(acc, a, i);
-    ea = q > ea ? q : ea;
+    const unsigned long long qa = mixed_store<XSPH, SUMDENS>(acc, a, i);
+    ea = qa > ea ? qa : ea;
   }
   __syncthreads();
   return ea;
@@ -801,6 +863,8 @@ struct TileShared {
   unsigned short lists[ListCap<KERNEL>::value][kPairBlock];
   unsigned int hoff[kHaloCellsMax + 1];  // shared-memory offset of each halo cell, then the total
   unsigned int hgs[kHaloCellsMax];       // its first sorted slot
+  unsigned char qmap[kHaloCap];          // halo cell of each query of the tile
+  unsigned long long bar;                // completion of the staging copies
   int s_tile[2];                         // this and the next claimed tile (-1: none left)
   int s_inst[2];                         // their instances (batched form)
   unsigned long long red[kPairBlock / 32];
@@ -818,6 +882,9 @@ __global__ void __launch_bounds__(kPairBlock, kTileBlocks)
   const bool filter = gp->mode == 1 && (gp->need_filter || ctrl->alias_count > 0);
   const MixedConsts mc = mixed_consts<KERNEL>(pp);
   unsigned long long ea = kEncMaxId;
+  if (tid == 0) mbar_init(&sm.bar, 1);
+  __syncthreads();
+  TileSync sync{&sm.bar, 0u, false};
 
   if (filter || tg.HC > kHaloCellsMax) {
     // everything on the global path, in 128-slot chunks
@@ -845,8 +912,10 @@ __global__ void __launch_bounds__(kPairBlock, kTileBlocks)
         sm.s_tile[(it + 1) & 1] = c < ntl ? tiles[c] : -1;
       }
       const unsigned long long q = tile_process<KERNEL, XSPH, SUMDENS>(a, P, tg, mc, t, sm.h0, sm.h1, sm.h2, sm.lists,
-                                                                        sm.hoff, sm.hgs, ctrl, fb, fb_cap);
+                                                                        sm.hoff, sm.hgs, sm.qmap, sync, ctrl, fb,
+                                                                        fb_cap);
       ea = q > ea ? q : ea;
+      if (sync.abort) break;
     }
   }
   // this block's max a^2 (the list kernel finishes the TimeStep reduction);
@@ -876,6 +945,8 @@ __global__ void __launch_bounds__(kPairBlock, kTileBlocks)
   const int tid = threadIdx.x;
   DevCtrl *ctrl = P.ctrl;
   const unsigned int ntl = ctrl->tl_count;
+  if (tid == 0) mbar_init(&sm.bar, 1);
+  TileSync sync{&sm.bar, 0u, false};
   if (tid == 0) {
     if (blockIdx.x == 0)  // every instance's dump cell (reference-OOB particles) is in no tile
       for (int b = 0; b < B.n_inst; b++) {
@@ -913,9 +984,11 @@ __global__ void __launch_bounds__(kPairBlock, kTileBlocks)
     }
     const MixedConsts mc = mixed_consts<KERNEL>(pp);
     const unsigned long long ea = tile_process<KERNEL, XSPH, SUMDENS>(a, P, tg, mc, t, sm.h0, sm.h1, sm.h2, sm.lists,
-                                                                       sm.hoff, sm.hgs, ctrl, fb, fb_cap);
+                                                                       sm.hoff, sm.hgs, sm.qmap, sync, ctrl, fb,
+                                                                       fb_cap);
     const unsigned long long ba = block_max_u64(ea, sm.red);
     if (tid == 0 && ba != kEncMaxId) atomicMax(&B.sl[b].pd_a2max, ba);
+    if (sync.abort) break;
   }
   if (tid == 0) {
     __threadfence();

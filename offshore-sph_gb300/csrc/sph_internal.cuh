@@ -367,6 +367,54 @@ __device__ __forceinline__ unsigned long long warp_max_u64(unsigned long long v)
   return ((unsigned long long)mh << 32) | ml;
 }
 
+// ---------------------------------------------------------------------------
+// Bulk asynchronous copies global -> shared (cp.async.bulk, the TMA engine's
+// 1D form) completing on a shared-memory mbarrier.  Addresses 16-byte
+// aligned, sizes multiples of 16 bytes.
+// ---------------------------------------------------------------------------
+__device__ __forceinline__ uint32_t smem_addr(const void *p) { return (uint32_t)__cvta_generic_to_shared(p); }
+
+__device__ __forceinline__ void mbar_init(unsigned long long *bar, uint32_t count) {
+  asm volatile("mbarrier.init.shared::cta.b64 [%0], %1;" ::"r"(smem_addr(bar)), "r"(count) : "memory");
+  asm volatile("fence.mbarrier_init.release.cluster;" ::: "memory");
+}
+
+// orders this thread's earlier generic-proxy shared-memory accesses before
+// its later async-proxy (bulk copy) ones
+__device__ __forceinline__ void fence_proxy_async_smem() {
+  asm volatile("fence.proxy.async.shared::cta;" ::: "memory");
+}
+
+__device__ __forceinline__ void mbar_arrive_expect_tx(unsigned long long *bar, uint32_t bytes) {
+  asm volatile("mbarrier.arrive.expect_tx.shared::cta.b64 _, [%0], %1;" ::"r"(smem_addr(bar)), "r"(bytes)
+               : "memory");
+}
+
+__device__ __forceinline__ void bulk_copy_g2s(void *dst, const void *src, uint32_t bytes, unsigned long long *bar) {
+  asm volatile("cp.async.bulk.shared::cluster.global.mbarrier::complete_tx::bytes [%0], [%1], %2, [%3];" ::"r"(
+                   smem_addr(dst)),
+               "l"(src), "r"(bytes), "r"(smem_addr(bar))
+               : "memory");
+}
+
+__device__ __forceinline__ bool mbar_try_wait(unsigned long long *bar, uint32_t parity) {
+  uint32_t ok;
+  asm volatile(
+      "{\n .reg .pred p;\n mbarrier.try_wait.parity.shared::cta.b64 p, [%1], %2;\n selp.u32 %0, 1, 0, p;\n}"
+      : "=r"(ok)
+      : "r"(smem_addr(bar)), "r"(parity)
+      : "memory");
+  return ok != 0;
+}
+
+// Bounded wait for phase `parity` of bar; false when the limit ran out.
+constexpr int kMbarWaitLimit = 1 << 22;
+__device__ __forceinline__ bool mbar_wait_bounded(unsigned long long *bar, uint32_t parity) {
+  for (int it = 0; it < kMbarWaitLimit; it++)
+    if (mbar_try_wait(bar, parity)) return true;
+  return false;
+}
+
 // 32-bit signed saturation for cell coordinates
 __device__ __forceinline__ int sat_i32(long long v) {
   return v > (1ll << 30) ? (1 << 30) : (v < -(1ll << 30) ? -(1 << 30) : (int)v);

@@ -22,6 +22,10 @@ SOURCES = ["nn_build.cu", "pair.cu", "integrate.cu", "capi.cu", "static_ws.cu", 
 ARCH = ["-gencode", "arch=compute_103a,code=sm_103a"]
 FLAGS = ["-O3", "-std=c++17", "-lineinfo", "-Xcompiler", "-fPIC", "--expt-relaxed-constexpr",
          "-I", INCLUDE, "-I", CSRC]
+# the mixed-form pair arithmetic flushes FP32 denormals: its reciprocals and
+# square roots then take the plain hardware approximations (the FP64 form is
+# unaffected; every FP32 pair operand of a real scene is far from 1e-38)
+SOURCE_FLAGS = {"pair.cu": ["-ftz=true"]}
 
 
 def nvcc():
@@ -50,7 +54,8 @@ def build(force=False, verbose=False, extra_flags=()):
 
     def compile_one(src):
         obj = os.path.join(OBJDIR, os.path.splitext(src)[0] + ".o")
-        cmd = [nv, "-c", os.path.join(CSRC, src), "-o", obj] + ARCH + FLAGS + list(extra_flags)
+        cmd = [nv, "-c", os.path.join(CSRC, src), "-o", obj] + ARCH + FLAGS + SOURCE_FLAGS.get(src, []) + \
+            list(extra_flags)
         r = subprocess.run(cmd, capture_output=True, text=True)
         if r.returncode != 0:
             raise RuntimeError("nvcc failed on %s:\n%s\n%s" % (src, " ".join(cmd), r.stderr))
