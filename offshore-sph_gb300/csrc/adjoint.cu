@@ -376,7 +376,7 @@ void launch_adjoint_step(const StepArgs &s, const StepArgs &h, const WsPtrs &w, 
   if (!adj.reuse_build) {
     k_adj_half<<<nb, kBlock, 0, st>>>(s, h, dt);
     // neighbour build and FP64 records of the half state (the forward's own passes)
-    launch_bounds(h, w, cfg, kStageNone, true, nullptr, nullptr, st);
+    launch_bounds(h, w, cfg, wc, kStageNone, true, nullptr, nullptr, st);
     launch_build(h, w, cfg, wc, st);
     sph_config_t c64 = cfg;
     c64.precision = SPH_PREC_FP64;

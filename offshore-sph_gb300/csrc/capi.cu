@@ -24,6 +24,7 @@ WsLayout make_layout(long long n_cap, long long max_cells) {
   L.grid = take(sizeof(DevGrid));
   L.keys = take(n * 4);
   L.refcell = take(n * 8);
+  L.crank = take(n * 4);
   L.perm_tmp = take(n * 4);
   L.keys_sorted = take(n * 4);
   L.perm = take(n * 4);
@@ -53,6 +54,7 @@ WsPtrs ws_ptrs(const sph_workspace_t *ws) {
   p.grid = (DevGrid *)(b + L.grid);
   p.keys = (int *)(b + L.keys);
   p.refcell = (int2 *)(b + L.refcell);
+  p.crank = (unsigned int *)(b + L.crank);
   p.perm_tmp = (int *)(b + L.perm_tmp);
   p.keys_sorted = (int *)(b + L.keys_sorted);
   p.perm = (int *)(b + L.perm);
@@ -85,6 +87,7 @@ __global__ void k_ctrl_init(DevCtrl *c) {
 // zero cell counters, zero grid, control block at its identities
 void init_workspace(const WsPtrs &w, cudaStream_t st) {
   cudaMemsetAsync(w.counts, 0, (size_t)(w.max_cells + 1) * 4, st);
+  cudaMemsetAsync(w.scan_part, 0, (size_t)w.n_parts * 4, st);
   cudaMemsetAsync(w.grid, 0, sizeof(DevGrid), st);
   k_ctrl_init<<<1, 32, 0, st>>>(w.ctrl);
 }
@@ -248,7 +251,7 @@ int sph_nn_update(const sph_particles_t *pa, const sph_config_t *cfg, const sph_
   WsPtrs w = ws_ptrs(ws);
   sph_wcsph_t wc;
   memset(&wc, 0, sizeof(wc));
-  launch_bounds(a, w, *cfg, kStageNone, false, nullptr, nullptr, st);
+  launch_bounds(a, w, *cfg, wc, kStageNone, false, nullptr, nullptr, st);
   launch_build(a, w, *cfg, wc, st);
   return check_launch();
 }
@@ -314,8 +317,8 @@ int sph_probe_density(const sph_particles_t *pa, const sph_wcsph_t *w, int kerne
 static void compute_body(const StepArgs &a, const WsPtrs &w, const sph_wcsph_t &wc, const sph_config_t &cfg,
                          double *dt_out, double *dt_hist, cudaStream_t st, const WallLoad *wall = nullptr) {
   const bool do_dt = dt_out != nullptr || dt_hist != nullptr;
-  launch_build(a, w, cfg, wc, st);
-  launch_records(a, w, cfg, wc, true, false, do_dt, st);
+  const RecParams rp = rec_params(cfg, wc, true, false, do_dt);
+  launch_build(a, w, cfg, wc, st, &rp);
   if (wc.use_summation_density) {
     launch_sumdens(a, w, cfg, wc, st);
     launch_records(a, w, cfg, wc, false, true, false, st);
@@ -332,7 +335,7 @@ int sph_compute(sph_particles_t *pa, const sph_wcsph_t *w, const sph_config_t *c
   cudaStream_t st = (cudaStream_t)stream;
   StepArgs a = step_args(pa);
   WsPtrs wp = ws_ptrs(ws);
-  launch_bounds(a, wp, *cfg, kStageNone, true, nullptr, nullptr, st);
+  launch_bounds(a, wp, *cfg, *w, kStageNone, true, nullptr, nullptr, st);
   compute_body(a, wp, *w, *cfg, nullptr, nullptr, st);
   return check_launch();
 }
@@ -382,7 +385,7 @@ int sph_run(sph_particles_t *pa, const sph_wcsph_t *w, const sph_config_t *cfg, 
     double *prev = ring + 3 * ((s + 1) & 1);
     double *cur = ring + 3 * (s & 1);
     double *nxt = ring + 3 * ((s + 1) & 1);
-    launch_bounds(a, wp, *cfg, s == 0 ? kStagePredict : kStageCorrectPredict, true, prev, cur, st);
+    launch_bounds(a, wp, *cfg, *w, s == 0 ? kStagePredict : kStageCorrectPredict, true, prev, cur, st);
     double *hist_next = (dt_hist && !fixed && s + 1 < nsteps) ? dt_hist + 3 * (s + 1) : nullptr;
     compute_body(a, wp, *w, *cfg, fixed ? nullptr : nxt, hist_next, st);
   }
@@ -416,7 +419,7 @@ int sph_run_wall_load(sph_particles_t *pa, const sph_wcsph_t *w, const sph_confi
   for (int64_t s = 0; s < nsteps; s++) {
     double *prev = ring + 3 * ((s + 1) & 1);
     double *cur = ring + 3 * (s & 1);
-    launch_bounds(a, wp, *cfg, s == 0 ? kStagePredict : kStageCorrectPredict, true, prev, cur, st);
+    launch_bounds(a, wp, *cfg, *w, s == 0 ? kStagePredict : kStageCorrectPredict, true, prev, cur, st);
     compute_body(a, wp, *w, *cfg, nullptr, nullptr, st, &wall);
     launch_sum_fixed(fr, a.n, load_hist + s, st);
   }
@@ -473,11 +476,11 @@ int sph_run_profiled(sph_particles_t *pa, const sph_wcsph_t *w, const sph_config
     double *cur = ring + 3 * (s & 1);
     double *nxt = ring + 3 * ((s + 1) & 1);
     cudaEventRecord(ev[0], st);
-    launch_bounds(a, wp, *cfg, s == 0 ? kStagePredict : kStageCorrectPredict, true, prev, cur, st);
+    launch_bounds(a, wp, *cfg, *w, s == 0 ? kStagePredict : kStageCorrectPredict, true, prev, cur, st);
     lap(SPH_STAGE_PREDICT, 0);
-    launch_build(a, wp, *cfg, *w, st);
+    const RecParams rp = rec_params(*cfg, *w, true, false, !fixed);
+    launch_build(a, wp, *cfg, *w, st, &rp);  // the records pass is fused into the build's last kernel
     lap(SPH_STAGE_BUILD, SPH_STAGE_PREDICT + 1);
-    launch_records(a, wp, *cfg, *w, true, false, !fixed, st);
     if (w->use_summation_density) {
       launch_sumdens(a, wp, *cfg, *w, st);
       launch_records(a, wp, *cfg, *w, false, true, false, st);

@@ -16,6 +16,8 @@
 // (aliased cells, or a grid coarsened to fit the cell capacity).
 #include <math.h>
 
+#include <string.h>
+
 #include "sph_internal.cuh"
 
 namespace sph {
@@ -36,69 +38,88 @@ struct BoundsParams {
   const double *dt_prev, *dt_cur;  // device dt of the previous / current step
 };
 
-// The integrator work in front of a neighbour build, on one fluid particle:
-// [the previous step's corrector: PEC.correct (src/Integrators/PEC.py:61-89)
-// in its reduced form x0 + dt v, or Euler.correct (Euler.py:17-27)] then
-// [this step's PEC.predict (PEC.py:32-59)].  Uniform conditions arrive as
-// ints and the half step is an exponent decrement, so the FP64 pipe only
-// sees the fused multiply-adds of the updates.
-__device__ __forceinline__ void integrate_front(const StepArgs &a, long long i, const BoundsParams &bp, double &x,
-                                                double &y, double &rho) {
+// The integrator work in front of a neighbour build, on one particle (stored
+// only when it is fluid): [the previous step's corrector: PEC.correct
+// (src/Integrators/PEC.py:61-89) in its reduced form x0 + dt v, or
+// Euler.correct (Euler.py:17-27)] then [this step's PEC.predict
+// (PEC.py:32-59)].  Uniform conditions arrive as ints and the half step is
+// an exponent decrement, so the FP64 pipe only sees the fused multiply-adds
+// of the updates.  Every input is loaded before anything depends on the
+// label, so a particle costs one memory round trip.
+__device__ __forceinline__ void integrate_front(const StepArgs &a, long long i, const BoundsParams &bp, bool fl,
+                                                double &x, double &y, double &rho) {
+  const bool cp = bp.stage == kStageCorrectPredict;
+  const double hdt = half_exact(bp.dt_fixed_on ? bp.dt_fixed : bp.dt_cur[0]);
+  const double dtc = cp ? (bp.dt_fixed_on ? bp.dt_fixed : bp.dt_prev[0]) : 0.0;
+  const double vxc = a.vx[i], vyc = a.vy[i];
   if (bp.verlet) {
     // [Verlet.correct (src/Integrators/Verlet.py:37-53): kick, second half
     // drift with the new velocity or XSPH] then [Verlet.predict (:28-35):
     // half drift]; the density is not integrated
-    double vx = a.vx[i], vy = a.vy[i];
-    if (bp.stage == kStageCorrectPredict) {
-      const double dtc = bp.dt_fixed_on ? bp.dt_fixed : bp.dt_prev[0];
-      const double hc = half_exact(dtc);
-      vx = fma(dtc, a.ax[i], vx);
-      vy = fma(dtc, a.ay[i], vy);
+    double vx = vxc, vy = vyc, nx = x, ny = y;
+    if (cp) {
+      const double axv = a.ax[i], ayv = a.ay[i];
+      double xs = 0.0, ys = 0.0;
       if (bp.use_xsph) {
-        x = fma(hc, a.xsphx[i], x);
-        y = fma(hc, a.xsphy[i], y);
-      } else {
-        x = fma(hc, vx, x);
-        y = fma(hc, vy, y);
+        xs = a.xsphx[i];
+        ys = a.xsphy[i];
       }
-      a.vx[i] = vx;
-      a.vy[i] = vy;
-    }
-    const double hdt = half_exact(bp.dt_fixed_on ? bp.dt_fixed : bp.dt_cur[0]);
-    x = fma(hdt, vx, x);
-    y = fma(hdt, vy, y);
-    a.x[i] = x;
-    a.y[i] = y;
-    return;
-  }
-  double vx, vy;
-  const double axv = a.ax[i], ayv = a.ay[i], drho = a.drho[i];
-  if (bp.stage == kStageCorrectPredict) {
-    const double dtc = bp.dt_fixed_on ? bp.dt_fixed : bp.dt_prev[0];
-    if (bp.euler) {
-      vx = a.vx[i];
-      vy = a.vy[i];
-      const double hdt2 = half_exact(dtc * dtc);
-      x = fma(hdt2, axv, fma(dtc, vx, x));
-      y = fma(hdt2, ayv, fma(dtc, vy, y));
+      const double hc = half_exact(dtc);
       vx = fma(dtc, axv, vx);
       vy = fma(dtc, ayv, vy);
-      rho = fma(dtc, drho, rho);
-      a.x[i] = x;
-      a.y[i] = y;
-      a.vx[i] = vx;
-      a.vy[i] = vy;
-      a.rho[i] = rho;
+      nx = fma(hc, bp.use_xsph ? xs : vx, nx);
+      ny = fma(hc, bp.use_xsph ? ys : vy, ny);
+      if (fl) {
+        a.vx[i] = vx;
+        a.vy[i] = vy;
+      }
+    }
+    nx = fma(hdt, vx, nx);
+    ny = fma(hdt, vy, ny);
+    if (fl) {
+      a.x[i] = nx;
+      a.y[i] = ny;
+      x = nx;
+      y = ny;
+    }
+    return;
+  }
+  const double axv = a.ax[i], ayv = a.ay[i], drho = a.drho[i];
+  double x0 = 0.0, y0 = 0.0, vx0 = 0.0, vy0 = 0.0, rho0 = 0.0, xs = 0.0, ys = 0.0;
+  if (cp && !bp.euler) {
+    x0 = a.x0[i];
+    y0 = a.y0[i];
+    vx0 = a.vx0[i];
+    vy0 = a.vy0[i];
+    rho0 = a.rho0[i];
+  }
+  if (bp.use_xsph && !bp.euler) {
+    xs = a.xsphx[i];
+    ys = a.xsphy[i];
+  }
+  double nx = x, ny = y, nrho = rho, vx = vxc, vy = vyc;
+  if (cp) {
+    if (bp.euler) {
+      const double hdt2 = half_exact(dtc * dtc);
+      nx = fma(hdt2, axv, fma(dtc, vxc, x));
+      ny = fma(hdt2, ayv, fma(dtc, vyc, y));
+      vx = fma(dtc, axv, vxc);
+      vy = fma(dtc, ayv, vyc);
+      nrho = fma(dtc, drho, rho);
+      if (fl) {
+        a.x[i] = nx;
+        a.y[i] = ny;
+        a.vx[i] = vx;
+        a.vy[i] = vy;
+        a.rho[i] = nrho;
+        x = nx;
+        y = ny;
+        rho = nrho;
+      }
       return;  // Euler.predict is a no-op
     }
-    const double x0 = a.x0[i], y0 = a.y0[i], vx0 = a.vx0[i], vy0 = a.vy0[i], rho0 = a.rho0[i];
-    if (bp.use_xsph) {
-      x = fma(dtc, a.xsphx[i], x0);
-      y = fma(dtc, a.xsphy[i], y0);
-    } else {
-      x = fma(dtc, a.vx[i], x0);
-      y = fma(dtc, a.vy[i], y0);
-    }
+    nx = fma(dtc, bp.use_xsph ? xs : vxc, x0);
+    ny = fma(dtc, bp.use_xsph ? ys : vyc, y0);
     if (bp.damped) {
       const double c1 = dtc * bp.inv_damp;
       vx = fma(c1, axv, bp.c0 * vx0);
@@ -107,76 +128,89 @@ __device__ __forceinline__ void integrate_front(const StepArgs &a, long long i, 
       vx = fma(dtc, axv, vx0);
       vy = fma(dtc, ayv, vy0);
     }
-    rho = fma(dtc, drho, rho0);
-    if (bp.strict && negative_bits(rho)) rho = 0.0;
-  } else {
-    vx = a.vx[i];
-    vy = a.vy[i];
+    nrho = fma(dtc, drho, rho0);
+    if (bp.strict && negative_bits(nrho)) nrho = 0.0;
   }
   // PEC.predict with this step's dt
-  const double hdt = half_exact(bp.dt_fixed_on ? bp.dt_fixed : bp.dt_cur[0]);
-  a.x0[i] = x;
-  a.y0[i] = y;
-  a.vx0[i] = vx;
-  a.vy0[i] = vy;
-  a.rho0[i] = rho;
+  double px, py;
   if (bp.use_xsph) {
-    x = fma(hdt, a.xsphx[i], x);
-    y = fma(hdt, a.xsphy[i], y);
+    px = fma(hdt, xs, nx);
+    py = fma(hdt, ys, ny);
   } else {
-    x = fma(hdt, vx, x);
-    y = fma(hdt, vy, y);
+    px = fma(hdt, vx, nx);
+    py = fma(hdt, vy, ny);
   }
   double nvx = fma(hdt, axv, vx), nvy = fma(hdt, ayv, vy);
   if (bp.damped) {
     nvx *= bp.inv_damp;
     nvy *= bp.inv_damp;
   }
-  rho = fma(hdt, drho, rho);
-  if (bp.strict && negative_bits(rho)) rho = 0.0;
-  a.x[i] = x;
-  a.y[i] = y;
-  a.vx[i] = nvx;
-  a.vy[i] = nvy;
-  a.rho[i] = rho;
-}
-
-// One particle's part of k_bounds: the integrator work in front of the build
-// and its six bound values (minima; maxima as minima of the complement).
-__device__ __forceinline__ void bounds_one(const StepArgs &a, long long i, const BoundsParams &bp,
-                                           unsigned long long (&v)[6], bool &bad) {
-  {
-    const int8_t lab = a.label[i];
-    double x = a.x[i], y = a.y[i];
-    const double h = a.h[i];
-    double hn = h;
-    if (is_fluid(lab)) {
-      if (bp.stage != kStageNone || (bp.h_reset && !bp.h_fixed_on)) {
-        double rho = a.rho[i];
-        if (bp.stage != kStageNone) integrate_front(a, i, bp, x, y, rho);
-        if (bp.h_reset) hn = bp.h_fixed_on ? bp.h_fixed : compute_h(a.m[i], rho);
-      } else if (bp.h_reset) {
-        hn = bp.h_fixed;
-      }
-    }
-    bad = !(finite_bits(x) && finite_bits(y) && finite_bits(h));
-    if (!bad) {
-      v[0] = enc_d(x);
-      v[1] = ~v[0];
-      v[2] = enc_d(y);
-      v[3] = ~v[2];
-      v[4] = enc_d(h);
-      v[5] = ~enc_d(hn);
-    }
+  double prho = fma(hdt, drho, nrho);
+  if (bp.strict && negative_bits(prho)) prho = 0.0;
+  if (fl) {
+    a.x0[i] = nx;
+    a.y0[i] = ny;
+    a.vx0[i] = vx;
+    a.vy0[i] = vy;
+    a.rho0[i] = nrho;
+    a.x[i] = px;
+    a.y[i] = py;
+    a.vx[i] = nvx;
+    a.vy[i] = nvy;
+    a.rho[i] = prho;
+    x = px;
+    y = py;
+    rho = prho;
   }
 }
 
-__global__ void __launch_bounds__(kBlock) k_bounds(StepArgs a, DevCtrl *ctrl, BoundsParams bp) {
+// One particle's part of k_bounds: the integrator work in front of the build
+// and its six bound values (minima; maxima as minima of the complement),
+// folded into v.
+__device__ __forceinline__ void bounds_one(const StepArgs &a, long long i, const BoundsParams &bp,
+                                           unsigned long long (&v)[6], bool &bad) {
+  const int8_t lab = a.label[i];
+  double x = a.x[i], y = a.y[i];
+  const double h = a.h[i];
+  const bool fl = is_fluid(lab);
+  const bool front = bp.stage != kStageNone;
+  const bool hcomp = bp.h_reset && !bp.h_fixed_on;
+  double rho = (front || hcomp) ? a.rho[i] : 0.0;
+  const double m = hcomp ? a.m[i] : 0.0;
+  if (front) integrate_front(a, i, bp, fl, x, y, rho);
+  double hn = h;
+  if (fl && bp.h_reset) hn = bp.h_fixed_on ? bp.h_fixed : compute_h(m, rho);
+  if (!(finite_bits(x) && finite_bits(y) && finite_bits(h))) {
+    bad = true;
+    return;
+  }
+  const unsigned long long ex = enc_d(x), ey = enc_d(y), eh = enc_d(h), en = ~enc_d(hn);
+  v[0] = ex < v[0] ? ex : v[0];
+  v[1] = ~ex < v[1] ? ~ex : v[1];
+  v[2] = ey < v[2] ? ey : v[2];
+  v[3] = ~ey < v[3] ? ~ey : v[3];
+  v[4] = eh < v[4] ? eh : v[4];
+  v[5] = en < v[5] ? en : v[5];
+}
+
+__device__ void grid_from_bounds(DevCtrl *ctrl, DevGrid *g, const GridParams &gp);
+
+// Persistent grid-stride blocks (a few per SM), so that the block
+// reductions end in few atomics on the shared bound slots.  The last block
+// to finish sets the grid of the next build from the reduced bounds.
+#ifndef SPH_BOUNDS_BLOCKS
+#define SPH_BOUNDS_BLOCKS 4
+#endif
+constexpr int kBoundsBlocks = SPH_BOUNDS_BLOCKS;  // resident blocks per SM
+__global__ void __launch_bounds__(kBlock, kBoundsBlocks) k_bounds(StepArgs a, DevCtrl *ctrl, BoundsParams bp,
+                                                                  DevGrid *g, GridParams gp) {
   __shared__ unsigned long long red[kBlock / 32][6];
-  const long long i = (long long)blockIdx.x * blockDim.x + threadIdx.x;
+  __shared__ bool last;
   unsigned long long v[6] = {kEncMinId, kEncMinId, kEncMinId, kEncMinId, kEncMinId, kEncMinId};
   bool bad = false;
-  if (i < a.n) bounds_one(a, i, bp, v, bad);
+  const long long stride = (long long)gridDim.x * blockDim.x;
+  for (long long i = (long long)blockIdx.x * blockDim.x + threadIdx.x; i < a.n; i += stride)
+    bounds_one(a, i, bp, v, bad);
   if (__syncthreads_or(bad) && threadIdx.x == 0) atomicOr(&ctrl->status, (unsigned)SPH_STATUS_NONFINITE);
   const int lane = threadIdx.x & 31, wid = threadIdx.x >> 5;
 #pragma unroll
@@ -196,10 +230,32 @@ __global__ void __launch_bounds__(kBlock) k_bounds(StepArgs a, DevCtrl *ctrl, Bo
       else atomicMin(slot[q], m);
     }
   }
+  __syncthreads();
+  if (threadIdx.x == 0) {
+    __threadfence();
+    last = atomicAdd(&ctrl->bounds_done, 1u) == gridDim.x - 1;
+  }
+  __syncthreads();
+  if (last && threadIdx.x == 0) {
+    __threadfence();
+    ctrl->bounds_done = 0;
+    grid_from_bounds(ctrl, g, gp);
+  }
 }
 
-void launch_bounds(const StepArgs &a, const WsPtrs &w, const sph_config_t &cfg, int stage, bool h_reset,
-                   const double *dt_prev, const double *dt_cur, cudaStream_t st) {
+static GridParams grid_params(const WsPtrs &w, const sph_config_t &cfg, const sph_wcsph_t &wc) {
+  GridParams gp;
+  gp.scale = cfg.nn_scale;
+  gp.r0 = wc.r0;
+  gp.kernel = cfg.kernel;
+  gp.max_cells = w.max_cells;
+  gp.ts_ref_max = SPH_TILE_SHIFT_REF;
+  gp.ts_own_max = SPH_TILE_SHIFT_OWN;
+  return gp;
+}
+
+void launch_bounds(const StepArgs &a, const WsPtrs &w, const sph_config_t &cfg, const sph_wcsph_t &wc, int stage,
+                   bool h_reset, const double *dt_prev, const double *dt_cur, cudaStream_t st) {
   BoundsParams bp;
   bp.stage = stage;
   bp.euler = cfg.integrator == SPH_INTEGRATOR_EULER ? 1 : 0;
@@ -217,7 +273,7 @@ void launch_bounds(const StepArgs &a, const WsPtrs &w, const sph_config_t &cfg, 
   bp.damped = cfg.damping != 0.0 ? 1 : 0;
   bp.use_xsph = cfg.pec_use_xsph;
   bp.strict = cfg.pec_strict;
-  k_bounds<<<nblocks(a.n), kBlock, 0, st>>>(a, w.ctrl, bp);
+  k_bounds<<<persist_blocks(a.n, kBoundsBlocks), kBlock, 0, st>>>(a, w.ctrl, bp, w.grid, grid_params(w, cfg, wc));
 }
 
 
@@ -335,11 +391,12 @@ __device__ unsigned grid_setup(double xmin, double xmax, double ymin, double yma
   return status;
 }
 
-__global__ void k_grid(DevCtrl *ctrl, DevGrid *g, GridParams gp) {
-  if (threadIdx.x != 0 || blockIdx.x != 0) return;
-  const double xmin = dec_d(ctrl->xmin), xmax = dec_d(ctrl->xmax);
-  const double ymin = dec_d(ctrl->ymin), ymax = dec_d(ctrl->ymax);
-  const double hmin = dec_d(ctrl->hmin_all), hmax = dec_d(ctrl->hmax_new);
+// The grid of the next build from the reduced bounds (one thread); the bound
+// slots return to their identities.  Runs in the last block of k_bounds.
+__device__ void grid_from_bounds(DevCtrl *ctrl, DevGrid *g, const GridParams &gp) {
+  const double xmin = dec_d(__ldcg(&ctrl->xmin)), xmax = dec_d(__ldcg(&ctrl->xmax));
+  const double ymin = dec_d(__ldcg(&ctrl->ymin)), ymax = dec_d(__ldcg(&ctrl->ymax));
+  const double hmin = dec_d(__ldcg(&ctrl->hmin_all)), hmax = dec_d(__ldcg(&ctrl->hmax_new));
   ctrl->xmin = kEncMinId; ctrl->xmax = kEncMaxId; ctrl->ymin = kEncMinId; ctrl->ymax = kEncMaxId;
   ctrl->hmin_all = kEncMinId; ctrl->hmax_new = kEncMaxId;
   ctrl->alias_count = 0;
@@ -384,22 +441,39 @@ __device__ __forceinline__ int cell_key(const DevGrid &g, double xi, double yi, 
   }
 }
 
+// Keys of the single-scene build: traversal and reference cells, the
+// particle's arrival rank in its cell and the cell totals of the scan tiles.
+// Lanes of a warp that share a cell (or a scan tile) take one atomic
+// together, so most warps issue a handful.
 __global__ void __launch_bounds__(kBlock) k_keys(const double *__restrict__ x, const double *__restrict__ y,
                                                  long long n, const DevGrid *__restrict__ gp, DevCtrl *ctrl,
                                                  int *__restrict__ keys, int2 *__restrict__ refcell,
-                                                 unsigned int *__restrict__ counts) {
-  long long i = (long long)blockIdx.x * blockDim.x + threadIdx.x;
+                                                 unsigned int *__restrict__ crank, unsigned int *__restrict__ counts,
+                                                 unsigned int *__restrict__ part) {
+  const long long i = (long long)blockIdx.x * blockDim.x + threadIdx.x;
+  const int lane = threadIdx.x & 31;
+  const bool act = i < n;
   bool alias = false, overflow = false;
-  if (i < n) {
+  int key = -1 - lane;  // inactive lanes: keys that match no other lane
+  if (act) {
     int2 ref;
-    const int key = cell_key(*gp, x[i], y[i], ref, alias, overflow);
+    key = cell_key(*gp, x[i], y[i], ref, alias, overflow);
     refcell[i] = ref;
     keys[i] = key;
-    atomicAdd(&counts[key], 1u);
   }
-  unsigned am = __ballot_sync(0xffffffffu, alias);
-  unsigned om = __ballot_sync(0xffffffffu, overflow);
-  if ((threadIdx.x & 31) == 0) {
+  const unsigned int below = (1u << lane) - 1u;
+  const unsigned int peers = __match_any_sync(0xffffffffu, key);
+  const int leader = __ffs(peers) - 1;
+  unsigned int base = 0;
+  if (act && lane == leader) base = atomicAdd(&counts[key], (unsigned int)__popc(peers));
+  base = __shfl_sync(0xffffffffu, base, leader);
+  if (act) crank[i] = base + (unsigned int)__popc(peers & below);
+  const int pt = act ? key / kScanTile : -1 - lane;
+  const unsigned int tpeers = __match_any_sync(0xffffffffu, pt);
+  if (act && lane == __ffs(tpeers) - 1) atomicAdd(&part[pt], (unsigned int)__popc(tpeers));
+  const unsigned am = __ballot_sync(0xffffffffu, alias);
+  const unsigned om = __ballot_sync(0xffffffffu, overflow);
+  if (lane == 0) {
     if (am) atomicAdd(&ctrl->alias_count, (unsigned)__popc(am));
     if (om) atomicOr(&ctrl->status, (unsigned)SPH_STATUS_CELL_OVERFLOW);
   }
@@ -516,14 +590,95 @@ __global__ void __launch_bounds__(kScanThreads) k_scan_apply(const unsigned int 
   }
 }
 
+// The single-scene scan: scan tile b's offset is the sum of the totals of
+// tiles 0 .. b-1 (counted by k_keys), so one pass writes cstart.
+__global__ void __launch_bounds__(kScanThreads) k_scan_cells(const unsigned int *__restrict__ counts,
+                                                             const DevGrid *__restrict__ g,
+                                                             const unsigned int *__restrict__ part,
+                                                             unsigned int *__restrict__ cstart) {
+  __shared__ unsigned int warp_tot[32];
+  __shared__ unsigned int red[32];
+  __shared__ unsigned int s_pre;
+  const long long m = (long long)g->ncells + 1;
+  const long long base = (long long)blockIdx.x * kScanTile;
+  if (base >= m) return;
+  unsigned int pre = 0;
+  for (int t = threadIdx.x; t < (int)blockIdx.x; t += kScanThreads) pre += part[t];
+  pre = block_reduce(pre, AddU32(), 0u, red);
+  if (threadIdx.x == 0) s_pre = pre;
+  const long long c0 = base + (long long)threadIdx.x * kScanPer;
+  unsigned int v[kScanPer];
+  if (c0 + 3 < m) {
+    const uint4 q = *(const uint4 *)(counts + c0);
+    v[0] = q.x; v[1] = q.y; v[2] = q.z; v[3] = q.w;
+  } else {
+#pragma unroll
+    for (int t = 0; t < kScanPer; t++) v[t] = (c0 + t < m) ? counts[c0 + t] : 0u;
+  }
+  const unsigned int loc = v[0] + v[1] + v[2] + v[3];
+  const int lane = threadIdx.x & 31, wid = threadIdx.x >> 5;
+  unsigned int inc = loc;
+#pragma unroll
+  for (int o = 1; o < 32; o <<= 1) {
+    unsigned int u = __shfl_up_sync(0xffffffffu, inc, o);
+    if (lane >= o) inc += u;
+  }
+  if (lane == 31) warp_tot[wid] = inc;
+  __syncthreads();
+  if (wid == 0) {
+    unsigned int t = warp_tot[lane];
+#pragma unroll
+    for (int o = 1; o < 32; o <<= 1) {
+      unsigned int u = __shfl_up_sync(0xffffffffu, t, o);
+      if (lane >= o) t += u;
+    }
+    warp_tot[lane] = t;  // inclusive over warps
+  }
+  __syncthreads();
+  const unsigned int run = s_pre + (wid ? warp_tot[wid - 1] : 0u) + inc - loc;
+  const unsigned int r0 = run, r1 = r0 + v[0], r2 = r1 + v[1], r3 = r2 + v[2], r4 = r3 + v[3];
+  if (c0 + 3 < m) {
+    *(uint4 *)(cstart + c0) = make_uint4(r0, r1, r2, r3);
+  } else {
+    const unsigned int rr[4] = {r0, r1, r2, r3};
+#pragma unroll
+    for (int t = 0; t < kScanPer; t++)
+      if (c0 + t < m) cstart[c0 + t] = rr[t];
+  }
+  if (c0 <= m - 1 && m - 1 <= c0 + 3) {
+    const unsigned int rr[5] = {r0, r1, r2, r3, r4};
+    cstart[m] = rr[m - c0];  // total
+  }
+}
+
+// Single-scene scatter: each particle to its cell's range at its arrival
+// rank (no atomics); cell counters and scan-tile totals return to zero.
+__global__ void __launch_bounds__(kBlock) k_scatter_rank(const int *__restrict__ keys,
+                                                         const unsigned int *__restrict__ crank, long long n,
+                                                         unsigned int *__restrict__ counts,
+                                                         const unsigned int *__restrict__ cstart,
+                                                         int *__restrict__ perm_tmp, int *__restrict__ keys_sorted,
+                                                         unsigned int *__restrict__ part, long long n_parts) {
+  const long long i = (long long)blockIdx.x * blockDim.x + threadIdx.x;
+  for (long long t = i; t < n_parts; t += (long long)gridDim.x * blockDim.x) part[t] = 0u;
+  if (i >= n) return;
+  const int key = keys[i];
+  const unsigned int slot = cstart[key] + crank[i];
+  perm_tmp[slot] = (int)i;
+  keys_sorted[slot] = key;
+  counts[key] = 0u;
+}
+
 // ---------------------------------------------------------------------------
 // Scatter (counts return to zero) and in-cell rank by particle index
 // ---------------------------------------------------------------------------
 __global__ void __launch_bounds__(kBlock) k_scatter(const int *__restrict__ keys, long long n,
                                                     unsigned int *__restrict__ counts,
                                                     const unsigned int *__restrict__ cstart,
-                                                    int *__restrict__ perm_tmp, int *__restrict__ keys_sorted) {
+                                                    int *__restrict__ perm_tmp, int *__restrict__ keys_sorted,
+                                                    unsigned int *__restrict__ part, long long n_parts) {
   long long i = (long long)blockIdx.x * blockDim.x + threadIdx.x;
+  for (long long t = i; t < n_parts; t += (long long)gridDim.x * blockDim.x) part[t] = 0u;
   if (i >= n) return;
   int key = keys[i];
   unsigned int old = atomicSub(&counts[key], 1u);
@@ -531,55 +686,6 @@ __global__ void __launch_bounds__(kBlock) k_scatter(const int *__restrict__ keys
   perm_tmp[slot] = (int)i;
   keys_sorted[slot] = key;
 }
-
-// In-cell order by particle index (deterministic); the first particle of each
-// non-empty tile also lists its tile for the tile pair kernel.
-__global__ void __launch_bounds__(kBlock) k_cellsort(const int *__restrict__ perm_tmp,
-                                                     const int *__restrict__ keys_sorted,
-                                                     const unsigned int *__restrict__ cstart,
-                                                     const int2 *__restrict__ refcell, long long n,
-                                                     const DevGrid *__restrict__ gp, DevCtrl *ctrl,
-                                                     int *__restrict__ perm, int2 *__restrict__ meta,
-                                                     int *__restrict__ tiles) {
-  long long k = (long long)blockIdx.x * blockDim.x + threadIdx.x;
-  if (k >= n) return;
-  int key = keys_sorted[k];
-  unsigned int s = cstart[key], e = cstart[key + 1];
-  const int ts2 = 2 * gp->ts;
-  if (key < gp->ncells && (unsigned)k == __ldg(&cstart[(key >> ts2) << ts2]))
-    tiles[atomicAdd(&ctrl->tl_count, 1u)] = key >> ts2;
-  int v = perm_tmp[k];
-  unsigned int rank = 0;
-  for (unsigned int t = s; t < e; t++) rank += (unsigned)(perm_tmp[t] < v);
-  perm[s + rank] = v;
-  meta[s + rank] = refcell[v];
-}
-
-void launch_build(const StepArgs &a, const WsPtrs &w, const sph_config_t &cfg, const sph_wcsph_t &wc,
-                  cudaStream_t st) {
-  GridParams gp;
-  gp.scale = cfg.nn_scale;
-  gp.r0 = wc.r0;
-  gp.kernel = cfg.kernel;
-  gp.max_cells = w.max_cells;
-  gp.ts_ref_max = SPH_TILE_SHIFT_REF;
-  gp.ts_own_max = SPH_TILE_SHIFT_OWN;
-  k_grid<<<1, 32, 0, st>>>(w.ctrl, w.grid, gp);
-  unsigned nb = nblocks(a.n);
-  k_keys<<<nb, kBlock, 0, st>>>(a.x, a.y, a.n, w.grid, w.ctrl, w.keys, w.refcell, w.counts);
-  k_scan_tiles<<<(unsigned)w.n_parts, kScanThreads, 0, st>>>(w.counts, w.grid, w.scan_part);
-  k_scan_top<<<1, 1024, 0, st>>>(w.scan_part, (int)w.n_parts);
-  k_scan_apply<<<(unsigned)w.n_parts, kScanThreads, 0, st>>>(w.counts, w.grid, w.scan_part, w.cstart);
-  k_scatter<<<nb, kBlock, 0, st>>>(w.keys, a.n, w.counts, w.cstart, w.perm_tmp, w.keys_sorted);
-  k_cellsort<<<nb, kBlock, 0, st>>>(w.perm_tmp, w.keys_sorted, w.cstart, w.refcell, a.n, w.grid, w.ctrl, w.perm,
-                                    w.meta, w.tiles);
-}
-
-// ---------------------------------------------------------------------------
-// Sorted pair records.  The h reset and the Tait EOS of _loop's first pass
-// (SolverTools.py:122-127) are fused here; p, c and the fluid h go back to
-// the caller's arrays.
-// ---------------------------------------------------------------------------
 
 // The mixed form's records of slot k (particle i): FP32 pair records, the h
 // reset and the Tait EOS on the relative density (no FP64 arithmetic); p, c
@@ -636,82 +742,113 @@ __device__ __forceinline__ void record_mixed(const StepArgs &a, long long k, int
     if (fl) a.h[i] = hd;
   }
   if (fl) {
-    eh = enc_d(hd);
-    nf = 1;
+    const unsigned long long e = enc_d(hd);
+    eh = e < eh ? e : eh;
+    nf++;
   }
 }
 
-template <bool MIXED>
-__global__ void __launch_bounds__(kBlock) k_records(StepArgs a, const int *__restrict__ perm, RecParams rp,
-                                                    DevCtrl *ctrl, float4 *__restrict__ rec0,
-                                                    float4 *__restrict__ rec1, float4 *__restrict__ rec2,
-                                                    double4_32a *__restrict__ r64a,
-                                                    double4_32a *__restrict__ r64b) {
+// The FP64 form's records of slot k (particle i), the reference's arithmetic.
+__device__ __forceinline__ void record_fp64(const StepArgs &a, long long k, int i, const RecParams &rp,
+                                            float4 *__restrict__ rec0, double4_32a *__restrict__ r64a,
+                                            double4_32a *__restrict__ r64b, unsigned long long &eh,
+                                            unsigned int &nf) {
+  const int8_t lab = a.label[i];
+  const bool fl = is_fluid(lab);
+  const double m = a.m[i], rho = a.rho[i];
+  const double x = a.x[i], y = a.y[i];
+  float xh, xl, yh, yl;
+  split_df(x, xh, xl);
+  split_df(y, yh, yl);
+  const float mf = d2f_trunc(m);
+  double h = a.h[i];
+  if (fl && !rp.from_state) h = rp.h_fixed_on ? rp.h_fixed : compute_h(m, rho);
+  const double p = rp.from_state ? a.p[i] : tait_p(rho, lab, rp.gamma, rp.B, rp.inv_rho0, rp.Pb);
+  const double othr = p / (rho * rho);
+  const double hs = fl ? h : -h;
+  r64a[k] = make_double4_32a(x, y, a.vx[i], a.vy[i]);
+  r64b[k] = make_double4_32a(m, rho, othr, (!fl && h == 0.0) ? -0.0 : hs);
+  const float hf = d2f_trunc(h);
+  rec0[k] = make_float4(xh, yh, fl ? hf : -hf, mf);
+  if (rp.write_state) {
+    a.p[i] = p;
+    a.c[i] = rp.co;
+    if (fl) a.h[i] = h;
+  }
+  if (fl) {
+    const unsigned long long e = enc_d(h);
+    eh = e < eh ? e : eh;
+    nf++;
+  }
+}
+
+// Block minimum of the fluid h and count of fluid particles into the step's
+// TimeStep slots (all threads call it).
+__device__ __forceinline__ void reduce_h_block(unsigned long long eh, unsigned int nf, unsigned long long *red,
+                                               unsigned int *redn, DevCtrl *ctrl) {
+  const unsigned long long wm = warp_min_u64(eh);
+  const unsigned int wn = __reduce_add_sync(0xffffffffu, nf);
+  const int lane = threadIdx.x & 31, wid = threadIdx.x >> 5;
+  if (lane == 0) {
+    red[wid] = wm;
+    redn[wid] = wn;
+  }
+  __syncthreads();
+  if (threadIdx.x == 0) {
+    unsigned long long bh = kEncMinId;
+    unsigned int bn = 0;
+    for (int w = 0; w < kBlock / 32; w++) {
+      bh = red[w] < bh ? red[w] : bh;
+      bn += redn[w];
+    }
+    if (bn) {
+      atomicMin(&ctrl->pd_hmin, bh);
+      atomicAdd(&ctrl->pd_nfluid, bn);
+    }
+  }
+}
+
+// In-cell order by particle index (deterministic); the first particle of each
+// non-empty tile also lists its tile for the tile pair kernel.  With REC the
+// same thread then writes the pair records of its final slot (the records
+// pass fused in: kRecMixed FP32 records, kRecFp64 FP64 records).
+enum { kRecNone = 0, kRecMixed = 1, kRecFp64 = 2 };
+template <int REC>
+__global__ void __launch_bounds__(kBlock) k_cellsort(const int *__restrict__ perm_tmp,
+                                                     const int *__restrict__ keys_sorted,
+                                                     const unsigned int *__restrict__ cstart,
+                                                     const int2 *__restrict__ refcell, long long n,
+                                                     const DevGrid *__restrict__ gp, DevCtrl *ctrl,
+                                                     int *__restrict__ perm, int2 *__restrict__ meta,
+                                                     int *__restrict__ tiles, StepArgs a, RecParams rp,
+                                                     float4 *__restrict__ rec0, float4 *__restrict__ rec1,
+                                                     float4 *__restrict__ rec2, double4_32a *__restrict__ r64a,
+                                                     double4_32a *__restrict__ r64b) {
   __shared__ unsigned long long red[kBlock / 32];
   __shared__ unsigned int redn[kBlock / 32];
   const long long k = (long long)blockIdx.x * blockDim.x + threadIdx.x;
   unsigned long long eh = kEncMinId;
   unsigned int nf = 0;
-  if (k < a.n) {
-    const int i = perm[k];
-    const int8_t lab = a.label[i];
-    const bool fl = is_fluid(lab);
-    const double m = a.m[i], rho = a.rho[i];
-    const double x = a.x[i], y = a.y[i];
-    float xh, xl, yh, yl;
-    split_df(x, xh, xl);
-    split_df(y, yh, yl);
-    const float mf = d2f_trunc(m);
-    if (MIXED) {
-      record_mixed(a, k, i, rp, rec0, rec1, rec2, eh, nf);
-    } else {
-      // FP64 record, the reference's arithmetic
-      double h = a.h[i];
-      if (fl && !rp.from_state) h = rp.h_fixed_on ? rp.h_fixed : compute_h(m, rho);
-      const double p = rp.from_state ? a.p[i] : tait_p(rho, lab, rp.gamma, rp.B, rp.inv_rho0, rp.Pb);
-      const double othr = p / (rho * rho);
-      const double hs = fl ? h : -h;
-      r64a[k] = make_double4_32a(x, y, a.vx[i], a.vy[i]);
-      r64b[k] = make_double4_32a(m, rho, othr, (!fl && h == 0.0) ? -0.0 : hs);
-      const float hf = d2f_trunc(h);
-      rec0[k] = make_float4(xh, yh, fl ? hf : -hf, mf);
-      if (rp.write_state) {
-        a.p[i] = p;
-        a.c[i] = rp.co;
-        if (fl) a.h[i] = h;
-      }
-      if (fl) {
-        eh = enc_d(h);
-        nf = 1;
-      }
-    }
+  if (k < n) {
+    const int key = keys_sorted[k];
+    const unsigned int s = cstart[key], e = cstart[key + 1];
+    const int ts2 = 2 * gp->ts;
+    if (key < gp->ncells && (unsigned)k == __ldg(&cstart[(key >> ts2) << ts2]))
+      tiles[atomicAdd(&ctrl->tl_count, 1u)] = key >> ts2;
+    const int v = perm_tmp[k];
+    unsigned int rank = 0;
+    for (unsigned int t = s; t < e; t++) rank += (unsigned)(perm_tmp[t] < v);
+    const unsigned int slot = s + rank;
+    perm[slot] = v;
+    meta[slot] = refcell[v];
+    if (REC == kRecMixed) record_mixed(a, slot, v, rp, rec0, rec1, rec2, eh, nf);
+    if (REC == kRecFp64) record_fp64(a, slot, v, rp, rec0, r64a, r64b, eh, nf);
   }
-  if (rp.reduce_h) {
-    const unsigned long long wm = warp_min_u64(eh);
-    const unsigned int wn = __reduce_add_sync(0xffffffffu, nf);
-    const int lane = threadIdx.x & 31, wid = threadIdx.x >> 5;
-    if (lane == 0) {
-      red[wid] = wm;
-      redn[wid] = wn;
-    }
-    __syncthreads();
-    if (threadIdx.x == 0) {
-      unsigned long long bh = kEncMinId;
-      unsigned int bn = 0;
-      for (int w = 0; w < kBlock / 32; w++) {
-        bh = red[w] < bh ? red[w] : bh;
-        bn += redn[w];
-      }
-      if (bn) {
-        atomicMin(&ctrl->pd_hmin, bh);
-        atomicAdd(&ctrl->pd_nfluid, bn);
-      }
-    }
-  }
+  if (REC != kRecNone && rp.reduce_h) reduce_h_block(eh, nf, red, redn, ctrl);
 }
 
-void launch_records(const StepArgs &a, const WsPtrs &w, const sph_config_t &cfg, const sph_wcsph_t &wc,
-                    bool write_state, bool p_from_state, bool reduce_h, cudaStream_t st) {
+RecParams rec_params(const sph_config_t &cfg, const sph_wcsph_t &wc, bool write_state, bool p_from_state,
+                     bool reduce_h) {
   RecParams rp;
   rp.h_fixed = cfg.h_fixed;
   rp.gamma = wc.gamma; rp.B = wc.B; rp.inv_rho0 = 1.0 / wc.rho0; rp.Pb = wc.Pb; rp.co = wc.co;
@@ -727,6 +864,60 @@ void launch_records(const StepArgs &a, const WsPtrs &w, const sph_config_t &cfg,
   rp.write_state = write_state ? 1 : 0;
   rp.from_state = p_from_state ? 1 : 0;
   rp.reduce_h = reduce_h ? 1 : 0;
+  return rp;
+}
+
+// The build after k_bounds (which set the grid): keys and ranks, scan,
+// scatter, in-cell order.  With rp, the pair records of the form cfg names
+// are written by the in-cell-order pass (launch_records' work, fused).
+void launch_build(const StepArgs &a, const WsPtrs &w, const sph_config_t &cfg, const sph_wcsph_t &wc,
+                  cudaStream_t st, const RecParams *rp) {
+  (void)wc;
+  const unsigned nb = nblocks(a.n);
+  k_keys<<<nb, kBlock, 0, st>>>(a.x, a.y, a.n, w.grid, w.ctrl, w.keys, w.refcell, w.crank, w.counts, w.scan_part);
+  k_scan_cells<<<(unsigned)w.n_parts, kScanThreads, 0, st>>>(w.counts, w.grid, w.scan_part, w.cstart);
+  k_scatter_rank<<<nb, kBlock, 0, st>>>(w.keys, w.crank, a.n, w.counts, w.cstart, w.perm_tmp, w.keys_sorted,
+                                        w.scan_part, w.n_parts);
+  RecParams none;
+  memset(&none, 0, sizeof(none));
+#define SPH_CELLSORT(R, P)                                                                                   \
+  k_cellsort<R><<<nb, kBlock, 0, st>>>(w.perm_tmp, w.keys_sorted, w.cstart, w.refcell, a.n, w.grid, w.ctrl, \
+                                       w.perm, w.meta, w.tiles, a, P, w.rec0, w.rec1, w.rec2, w.rec64a, w.rec64b)
+  if (!rp) SPH_CELLSORT(kRecNone, none);
+  else if (cfg.precision == SPH_PREC_MIXED) SPH_CELLSORT(kRecMixed, *rp);
+  else SPH_CELLSORT(kRecFp64, *rp);
+#undef SPH_CELLSORT
+}
+
+// ---------------------------------------------------------------------------
+// Sorted pair records.  The h reset and the Tait EOS of _loop's first pass
+// (SolverTools.py:122-127) are fused here; p, c and the fluid h go back to
+// the caller's arrays.
+// ---------------------------------------------------------------------------
+
+
+template <bool MIXED>
+__global__ void __launch_bounds__(kBlock) k_records(StepArgs a, const int *__restrict__ perm, RecParams rp,
+                                                    DevCtrl *ctrl, float4 *__restrict__ rec0,
+                                                    float4 *__restrict__ rec1, float4 *__restrict__ rec2,
+                                                    double4_32a *__restrict__ r64a,
+                                                    double4_32a *__restrict__ r64b) {
+  __shared__ unsigned long long red[kBlock / 32];
+  __shared__ unsigned int redn[kBlock / 32];
+  const long long k = (long long)blockIdx.x * blockDim.x + threadIdx.x;
+  unsigned long long eh = kEncMinId;
+  unsigned int nf = 0;
+  if (k < a.n) {
+    const int i = perm[k];
+    if (MIXED) record_mixed(a, k, i, rp, rec0, rec1, rec2, eh, nf);
+    else record_fp64(a, k, i, rp, rec0, r64a, r64b, eh, nf);
+  }
+  if (rp.reduce_h) reduce_h_block(eh, nf, red, redn, ctrl);
+}
+
+void launch_records(const StepArgs &a, const WsPtrs &w, const sph_config_t &cfg, const sph_wcsph_t &wc,
+                    bool write_state, bool p_from_state, bool reduce_h, cudaStream_t st) {
+  const RecParams rp = rec_params(cfg, wc, write_state, p_from_state, reduce_h);
   if (cfg.precision == SPH_PREC_MIXED)
     k_records<true><<<nblocks(a.n), kBlock, 0, st>>>(a, w.perm, rp, w.ctrl, w.rec0, w.rec1, w.rec2, w.rec64a,
                                                      w.rec64b);
@@ -887,7 +1078,8 @@ void launch_bt_build(const StepArgs &a, const WsPtrs &w, const BatchPtrs &B, cud
   k_scan_tiles<<<(unsigned)w.n_parts, kScanThreads, 0, st>>>(w.counts, B.scan, w.scan_part);
   k_scan_top<<<1, 1024, 0, st>>>(w.scan_part, (int)w.n_parts);
   k_scan_apply<<<(unsigned)w.n_parts, kScanThreads, 0, st>>>(w.counts, B.scan, w.scan_part, w.cstart);
-  k_scatter<<<nb, kBlock, 0, st>>>(w.keys, a.n, w.counts, w.cstart, w.perm_tmp, w.keys_sorted);
+  k_scatter<<<nb, kBlock, 0, st>>>(w.keys, a.n, w.counts, w.cstart, w.perm_tmp, w.keys_sorted, w.scan_part,
+                                   w.n_parts);
   k_bt_cellsort<<<nb, kBlock, 0, st>>>(w.perm_tmp, w.keys_sorted, w.cstart, w.refcell, a.n, B, w.ctrl, w.perm, w.meta);
 }
 

@@ -1195,8 +1195,7 @@ static PairParams pair_params(const StepArgs &a, const sph_config_t &cfg, const 
   return pp;
 }
 
-// SMs of the current device (cached per device)
-static int sm_count() {
+int sm_count() {
   static int cache[64] = {0};
   int dev = 0;
   cudaGetDevice(&dev);

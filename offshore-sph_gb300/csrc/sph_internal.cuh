@@ -150,6 +150,7 @@ struct DevCtrl {
   unsigned int tile_next, tile_done;
   unsigned int fb_count, fb_done;
   unsigned int tl_count;  // non-empty tiles listed by the build
+  unsigned int bounds_done;  // finished blocks of the bounds pass (its last block sets the grid)
   double dt_ring[2][3];  // {dt, dt_c, dt_f} of the step with that parity
 };
 
@@ -179,8 +180,8 @@ struct DevGrid {
 
 // Byte offsets of the workspace regions (computed on the host).
 struct WsLayout {
-  size_t ctrl, grid, keys, refcell, perm_tmp, keys_sorted, perm, meta, counts, cstart, scan_part, rec0, rec1,
-      rec2, rec64a, rec64b, fb, tiles, total;
+  size_t ctrl, grid, keys, refcell, crank, perm_tmp, keys_sorted, perm, meta, counts, cstart, scan_part, rec0,
+      rec1, rec2, rec64a, rec64b, fb, tiles, total;
   long long n_cap, max_cells, n_parts, fb_cap;
 };
 
@@ -288,13 +289,14 @@ struct WsPtrs {
   DevGrid *grid;
   int *keys;          // traversal cell of particle i (caller order)
   int2 *refcell;      // raw reference cell (cx, cy) of particle i
+  unsigned int *crank;  // arrival rank of particle i in its cell (this build)
   int *perm_tmp;      // unsorted-within-cell permutation
   int *keys_sorted;   // traversal cell of sorted slot k
   int *perm;          // sorted slot -> particle index
   int2 *meta;         // raw reference cell of sorted slot k
   unsigned int *counts;  // per cell counters (zero between builds)
   unsigned int *cstart;  // exclusive prefix of counts, cstart[ncells + 1] = n
-  unsigned int *scan_part;
+  unsigned int *scan_part;  // cell total of each scan tile (zero between builds)
   float4 *rec0, *rec1, *rec2;
   double4_32a *rec64a, *rec64b;
   int2 *fb;  // fallback list of the tile pair kernel: (first slot, count <= 128)
@@ -693,6 +695,16 @@ inline unsigned int nblocks(long long n, int bs = kBlock) {
   return (unsigned int)(b < 1 ? 1 : b);
 }
 
+// SMs of the current device (cached per device; pair.cu)
+int sm_count();
+
+// Blocks of a persistent grid-stride launch over n items: per_sm blocks of
+// bs threads on every SM, fewer when n is small.
+inline unsigned int persist_blocks(long long n, int per_sm = 8, int bs = kBlock) {
+  const unsigned int nb = nblocks(n, bs), cap = (unsigned int)(sm_count() * per_sm);
+  return nb < cap ? nb : cap;
+}
+
 struct StepArgs {
   // state (caller order)
   long long n;
@@ -717,10 +729,13 @@ inline StepArgs step_args(const sph_particles_t *pa) {
 // of the first step, or the previous step's corrector followed by this
 // step's predictor.  h_reset: take hmax over the h the evaluation will set.
 enum IntStage { kStageNone = 0, kStagePredict = 1, kStageCorrectPredict = 2 };
-void launch_bounds(const StepArgs &a, const WsPtrs &w, const sph_config_t &cfg, int stage, bool h_reset,
-                   const double *dt_prev, const double *dt_cur, cudaStream_t st);
+void launch_bounds(const StepArgs &a, const WsPtrs &w, const sph_config_t &cfg, const sph_wcsph_t &wc, int stage,
+                   bool h_reset, const double *dt_prev, const double *dt_cur, cudaStream_t st);
+RecParams rec_params(const sph_config_t &cfg, const sph_wcsph_t &wc, bool write_state, bool p_from_state,
+                     bool reduce_h);
+// neighbour build after launch_bounds; with rp the records pass is fused in
 void launch_build(const StepArgs &a, const WsPtrs &w, const sph_config_t &cfg, const sph_wcsph_t &wc,
-                  cudaStream_t st);
+                  cudaStream_t st, const RecParams *rp = nullptr);
 // Sorted pair records (h reset + Tait EOS fused).  write_state: write p, c
 // and the fluid h back; p_from_state: take p from the caller's array (second
 // records pass of summation density); reduce_h: feed the step's TimeStep.

@@ -71,6 +71,7 @@ extern "C" int sph_compute_static(sph_particles_t *pa, const sph_wcsph_t *w, con
   sph::WsPtrs p = sph::ws_ptrs(&ws);
   // counters and control block start from zero on every call
   if (cudaMemsetAsync(p.counts, 0, (size_t)(ws.max_cells + 1) * 4, st) != cudaSuccess) return SPH_ERR_CUDA;
+  if (cudaMemsetAsync(p.scan_part, 0, (size_t)p.n_parts * 4, st) != cudaSuccess) return SPH_ERR_CUDA;
   k_static_ctrl_init<<<1, 32, 0, st>>>(p.ctrl);
   if (cudaGetLastError() != cudaSuccess) return SPH_ERR_CUDA;
   e = sph_compute(pa, w, cfg, &ws, stream);
