@@ -41,8 +41,7 @@ STEP_BYTES = 385    # algorithmic bytes of one PEC step per particle (dt 32 + pr
 # DRAM bytes (read + write) per particle of one pair launch, from the ncu
 # captures summarised in profiles/ (dram__bytes_read.sum + dram__bytes_write.sum
 # of k_pair_tiles over its particle count)
-TRAFFIC_PER_PARTICLE = {("dambreak1m", "mixed"): 77.0,  # profiles/k_pair_tiles_dambreak1m.md
-                        ("lattice1m", "mixed"): 76.5}
+TRAFFIC_PER_PARTICLE = {("dambreak1m", "mixed"): 62.5}  # profiles/k_pair_tiles_dambreak1m.md
 
 
 def workload(name):
@@ -570,7 +569,9 @@ def main():
     # per step: bounds/predict, grid, keys, 3 scan passes, scatter, cellsort,
     # records, pair tiles, pair fallback list (mixed) or one FP64 pair kernel;
     # per sph_run call also the initial TimeStep and the last corrector
-    launches_per_step = 11 if args.precision == "mixed" else 10
+    # k_bounds, k_keys, k_scan_cells, k_scatter_rank, k_cellsort, then
+    # k_pair_tiles + k_pair_list (mixed) or k_pair (FP64)
+    launches_per_step = 7 if args.precision == "mixed" else 6
     gsteps, reps, rem = graph_plan(args.steps)
     launches = launches_per_step * args.steps + 2 * (reps + (1 if rem else 0))
     out = {"metric": METRIC, "value": value, "unit": UNIT, "n_gpus": world, "steps": args.steps,

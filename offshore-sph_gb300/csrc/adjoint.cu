@@ -32,7 +32,9 @@
 
 namespace sph {
 
-constexpr int kAdjBlock = 128;
+// one-warp blocks: the kernel is FP64-bound and a small case has few warps
+// per SM, so small blocks spread them evenly
+constexpr int kAdjBlock = 32;
 constexpr int kAdjSplit = 1;  // lanes per query
 
 struct AdjParams {
@@ -254,7 +256,7 @@ __device__ __forceinline__ void adjoint_query(const AdjPtrs &P, const AdjParams 
 }
 
 template <int KERNEL>
-__global__ void __launch_bounds__(kAdjBlock, 2) k_pair_adjoint(AdjPtrs P, AdjParams ap) {
+__global__ void __launch_bounds__(kAdjBlock, 12) k_pair_adjoint(AdjPtrs P, AdjParams ap) {
   // kAdjSplit adjacent lanes share a query and take every kAdjSplit-th
   // candidate of its stencil; their sums are combined with shuffles
   const long long t = (long long)blockIdx.x * blockDim.x + threadIdx.x;

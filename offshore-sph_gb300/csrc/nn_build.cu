@@ -328,10 +328,13 @@ __device__ unsigned grid_setup(double xmin, double xmax, double ymin, double yma
   // support radius contribute nothing; the Gaussian is cut at q <= 3 inclusive
   const bool trunc_free = cubic ? (cs >= R) : (cs >= R * (1.0 + 1e-9));
   // the largest tile shift (up to ts_max) whose padded cell count fits
+  // (integer arithmetic: nx, ny are whole numbers below 2^31 here)
   auto tile_fit = [&](double nx, double ny, int ts_max, int &ts_out) {
+    const unsigned long long ix = (unsigned long long)nx, iy = (unsigned long long)ny;
     for (int ts = ts_max; ts >= 0; ts--) {
-      const double T = (double)(1 << ts);
-      if (ceil(nx / T) * ceil(ny / T) * T * T <= (double)gp.max_cells) {
+      const unsigned long long T = 1ull << ts;
+      const unsigned long long tx = (ix + T - 1) >> ts, ty = (iy + T - 1) >> ts;
+      if (tx * ty <= ((unsigned long long)gp.max_cells >> (2 * ts))) {
         ts_out = ts;
         return true;
       }

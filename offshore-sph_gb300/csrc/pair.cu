@@ -66,7 +66,8 @@ __device__ int exact_count(const StepArgs &a, const int *__restrict__ perm, cons
 // {dt, dt_courant, dt_force} (TimeStep.py:7-56) from the min h the records
 // pass gathered, and resets the slots.
 __device__ __forceinline__ void timestep_epilogue(DevCtrl *ctrl, unsigned long long ea, double co, double cfl_c,
-                                                  double cfl_f, double *dt_out, double *dt_hist) {
+                                                  double cfl_f, double *dt_out, double *dt_hist,
+                                                  unsigned int *zero_on_last = nullptr) {
   __shared__ unsigned long long red[kPairBlock / 32];
   __shared__ bool last;
   const unsigned long long wm = warp_max_u64(ea);
@@ -74,7 +75,7 @@ __device__ __forceinline__ void timestep_epilogue(DevCtrl *ctrl, unsigned long l
   __syncthreads();
   if (threadIdx.x == 0) {
     unsigned long long ba = kEncMaxId;
-    for (int w = 0; w < kPairBlock / 32; w++) ba = red[w] > ba ? red[w] : ba;
+    for (int w = 0; w < (int)(blockDim.x >> 5); w++) ba = red[w] > ba ? red[w] : ba;
     if (ba != kEncMaxId) atomicMax(&ctrl->pd_a2max, ba);
     __threadfence();
     last = atomicAdd(&ctrl->done_pair, 1u) == gridDim.x - 1;
@@ -86,6 +87,7 @@ __device__ __forceinline__ void timestep_epilogue(DevCtrl *ctrl, unsigned long l
     const double max_a2 = dec_d(atomicExch(&ctrl->pd_a2max, kEncMaxId));
     const unsigned int cnt = atomicExch(&ctrl->pd_nfluid, 0u);
     atomicExch(&ctrl->done_pair, 0u);
+    if (zero_on_last) *zero_on_last = 0u;
     const double max_c = co;  // compute_speed_of_sound gives co to every particle (WCSPH.py:110-129)
     double dc = __ddiv_rn(__dmul_rn(cfl_c, min_h), max_c);
     double df = max_a2 < 1e-12 ? 1e10 : __dmul_rn(cfl_f, __dsqrt_rn(__ddiv_rn(min_h, max_a2)));
@@ -443,28 +445,32 @@ __global__ void __launch_bounds__(kPairBlock, kListBlocks)
     k_pair_list(StepArgs a, PairPtrs P, PairParams pp, const int2 *__restrict__ fb, double *dt_out,
                 double *dt_hist) {
   __shared__ unsigned int lists[ListCap<KERNEL>::value][kPairBlock];
-  __shared__ bool last;
-  const DevGrid g = *P.grid;
-  const bool filter = g.mode == 1 && (g.need_filter || P.ctrl->alias_count > 0);
   const unsigned int cnt = *(volatile unsigned int *)&P.ctrl->fb_count;
   unsigned long long ea = kEncMaxId;
-  for (unsigned int e = blockIdx.x; e < cnt; e += gridDim.x) {
-    const int2 r = fb[e];
-    if ((int)threadIdx.x < r.y) {
-      const unsigned long long q = pair_query<KERNEL, XSPH, SUMDENS, true>(a, P, pp, g, filter, r.x + threadIdx.x, lists);
-      ea = q > ea ? q : ea;
+  if (blockIdx.x < cnt) {
+    const DevGrid g = *P.grid;
+    const bool filter = g.mode == 1 && (g.need_filter || P.ctrl->alias_count > 0);
+    for (unsigned int e = blockIdx.x; e < cnt; e += gridDim.x) {
+      const int2 r = fb[e];
+      if ((int)threadIdx.x < r.y) {
+        const unsigned long long q =
+            pair_query<KERNEL, XSPH, SUMDENS, true>(a, P, pp, g, filter, r.x + threadIdx.x, lists);
+        ea = q > ea ? q : ea;
+      }
     }
   }
   __syncthreads();
-  if (threadIdx.x == 0) {
+  // the last block to finish empties the fallback list (with the TimeStep
+  // epilogue when there is one)
+  if (pp.do_dt) {
+    timestep_epilogue(P.ctrl, ea, pp.co, pp.cfl_c, pp.cfl_f, dt_out, dt_hist, &P.ctrl->fb_count);
+  } else if (threadIdx.x == 0) {
     __threadfence();
-    last = atomicAdd(&P.ctrl->fb_done, 1u) == gridDim.x - 1;
-    if (last) {
+    if (atomicAdd(&P.ctrl->fb_done, 1u) == gridDim.x - 1) {
       P.ctrl->fb_count = 0;
       P.ctrl->fb_done = 0;
     }
   }
-  if (pp.do_dt) timestep_epilogue(P.ctrl, ea, pp.co, pp.cfl_c, pp.cfl_f, dt_out, dt_hist);
 }
 
 // ---------------------------------------------------------------------------
@@ -1219,8 +1225,10 @@ static void pair_dispatch(const StepArgs &a, const WsPtrs &w, const sph_config_t
     k_pair_list<KERNEL, XSPH, SUMDENS><<<sms * kListBlocks, kPairBlock, 0, st>>>(a, pair_ptrs(w), pp, w.fb,
                                                                                           dt_out, dt_hist);
   } else {
-    k_pair<KERNEL, XSPH, SUMDENS, false><<<nblocks(a.n, kPairBlock), kPairBlock, 0, st>>>(a, pair_ptrs(w), pp, dt_out,
-                                                                                          dt_hist);
+    // one query per thread; below a few blocks per SM, one-warp blocks so
+    // that the FP64-bound work spreads evenly over the SMs
+    const int bs = a.n < (long long)sm_count() * kPairBlock * 8 ? 32 : kPairBlock;
+    k_pair<KERNEL, XSPH, SUMDENS, false><<<nblocks(a.n, bs), bs, 0, st>>>(a, pair_ptrs(w), pp, dt_out, dt_hist);
   }
 }
 
