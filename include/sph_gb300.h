@@ -161,6 +161,13 @@ const char *sph_status_string(int code);
 /* Human-readable name of a single device status bit (SPH_STATUS_*). */
 const char *sph_status_bit_string(uint32_t bit);
 
+/* Self-test of the pair kernel's staging primitives (bulk asynchronous copy
+ * completing on an mbarrier, and the bounded wait): src64 is 64 bytes of
+ * device memory, 16-byte aligned; result (device, 2 x uint32) receives
+ * {1 if the copy landed intact, 2 if a wait on bytes that never arrive gave
+ * up after its bound}.  No host synchronisation. */
+int sph_selftest_staging(const void *src64, uint32_t *result, sph_stream_t stream);
+
 /* WCSPH.initialize + the fluid part of Solver.setup
  * (src/Methods/WCSPH.py:82-108, src/Solver.py:184-196): for fluid particles
  * set h (fixed or computeH), rho = TaitEOS_height(y), p = TaitEOS(rho) + Pb,

@@ -15,7 +15,6 @@ namespace sph {
 void launch_bt_bounds(const StepArgs &a, const WsPtrs &w, const BatchPtrs &B, const sph_config_t &cfg, int stage,
                       int prev, int cur, cudaStream_t st);
 void launch_bt_build(const StepArgs &a, const WsPtrs &w, const BatchPtrs &B, cudaStream_t st);
-void launch_bt_records(const StepArgs &a, const WsPtrs &w, const BatchPtrs &B, cudaStream_t st);
 void launch_bt_pair(const StepArgs &a, const WsPtrs &w, const BatchPtrs &B, int kernel, bool xsph, int tile_blocks,
                     cudaStream_t st);
 void launch_bt_timestep(const StepArgs &a, const WsPtrs &w, const BatchPtrs &B, int slot, double *dt_hist,
@@ -200,8 +199,7 @@ int sph_batch_run(sph_particles_t *pa, const sph_config_t *cfg, const sph_worksp
   for (int64_t s = 0; s < nsteps; s++) {
     const int prev = (int)((s + 1) & 1), cur = (int)(s & 1), nxt = (int)((s + 1) & 1);
     launch_bt_bounds(a, wp, B, *cfg, s == 0 ? kStagePredict : kStageCorrectPredict, prev, cur, st);
-    launch_bt_build(a, wp, B, st);
-    launch_bt_records(a, wp, B, st);
+    launch_bt_build(a, wp, B, st);  // with the records
     launch_bt_pair(a, wp, B, cfg->kernel, false, tile_blocks, st);
     launch_bt_dt_finish(wp, B, nxt, (dt_hist && s + 1 < nsteps) ? dt_hist + 3 * ni * (s + 1) : nullptr, st);
   }

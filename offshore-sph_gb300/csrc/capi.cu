@@ -92,6 +92,37 @@ void init_workspace(const WsPtrs &w, cudaStream_t st) {
   k_ctrl_init<<<1, 32, 0, st>>>(w.ctrl);
 }
 
+// Self-test of the staging primitives of the pair tile kernel: a 64-byte
+// bulk copy completing on an mbarrier, and a wait on bytes that never come,
+// which must give up after its bound.  result[0] = 1 when the copy landed
+// intact, result[1] = 2 when the second wait ran out (1 if it completed).
+__global__ void k_selftest_staging(const float4 *src, unsigned int *result) {
+  __shared__ float4 buf[4];
+  __shared__ unsigned long long bar[2];
+  if (threadIdx.x == 0) {
+    mbar_init(&bar[0], 1);
+    mbar_init(&bar[1], 1);
+  }
+  __syncthreads();
+  if (threadIdx.x == 0) {
+    fence_proxy_async_smem();
+    mbar_arrive_expect_tx(&bar[0], 64u);
+    bulk_copy_g2s(buf, src, 64u, &bar[0]);
+    mbar_arrive_expect_tx(&bar[1], 16u);  // nothing is sent
+  }
+  bool ok0 = mbar_wait_bounded(&bar[0], 0u);
+  if (!ok0) mbar_wait_bounded(&bar[0], 0u);  // never leave with the copy in flight
+  const bool ok1 = mbar_wait_bounded(&bar[1], 0u, 256);
+  __syncthreads();
+  if (threadIdx.x == 0) {
+    bool same = ok0;
+    for (int q = 0; q < 4 && same; q++)
+      same = buf[q].x == src[q].x && buf[q].y == src[q].y && buf[q].z == src[q].z && buf[q].w == src[q].w;
+    result[0] = same ? 1u : 0u;
+    result[1] = ok1 ? 1u : 2u;
+  }
+}
+
 __global__ void k_fill_dt(double *dt_hist, long long nsteps, double dt) {
   long long s = (long long)blockIdx.x * blockDim.x + threadIdx.x;
   if (s >= nsteps) return;
@@ -185,6 +216,12 @@ const char *sph_status_string(int code) {
     case SPH_ERR_STATIC_LIMIT: return "more particles than the static scratch of sph_compute_static holds";
     default: return "unknown";
   }
+}
+
+int sph_selftest_staging(const void *src64, uint32_t *result, sph_stream_t stream) {
+  if (!src64 || !result || ((uintptr_t)src64 & 15u)) return SPH_ERR_INVALID_ARGUMENT;
+  k_selftest_staging<<<1, 32, 0, (cudaStream_t)stream>>>((const float4 *)src64, result);
+  return check_launch();
 }
 
 const char *sph_status_bit_string(uint32_t bit) {

@@ -484,114 +484,11 @@ __global__ void __launch_bounds__(kBlock) k_keys(const double *__restrict__ x, c
 
 // ---------------------------------------------------------------------------
 // Exclusive scan of counts[0 .. ncells] (ncells + 1 entries, the last is the
-// dump cell) into cstart[0 .. ncells + 1].  Three phases over tiles of
+// dump cell) into cstart[0 .. ncells + 1], in one pass over tiles of
 // kScanTile cells; launch sizes depend only on the capacity.
 // ---------------------------------------------------------------------------
 constexpr int kScanThreads = 1024;
 constexpr int kScanPer = kScanTile / kScanThreads;
-
-__global__ void __launch_bounds__(kScanThreads) k_scan_tiles(const unsigned int *__restrict__ counts,
-                                                             const DevGrid *__restrict__ g,
-                                                             unsigned int *__restrict__ part) {
-  __shared__ unsigned int red[32];
-  const long long m = (long long)g->ncells + 1;
-  const long long base = (long long)blockIdx.x * kScanTile;
-  unsigned int s = 0;
-  if (base < m) {
-    const uint4 *c4 = (const uint4 *)(counts + base);
-    for (int t = threadIdx.x; t < kScanTile / 4; t += kScanThreads) {
-      long long c = base + 4ll * t;
-      if (c + 3 < m) {
-        uint4 v = c4[t];
-        s += v.x + v.y + v.z + v.w;
-      } else {
-        for (int q = 0; q < 4; q++)
-          if (c + q < m) s += counts[c + q];
-      }
-    }
-  }
-  s = block_reduce(s, AddU32(), 0u, red);
-  if (threadIdx.x == 0) part[blockIdx.x] = s;
-}
-
-__global__ void __launch_bounds__(1024) k_scan_top(unsigned int *part, int nparts) {
-  __shared__ unsigned int sh[1024];
-  int per = (nparts + 1023) / 1024;
-  int b = threadIdx.x * per;
-  unsigned int loc = 0;
-  for (int t = 0; t < per; t++)
-    if (b + t < nparts) loc += part[b + t];
-  sh[threadIdx.x] = loc;
-  __syncthreads();
-  for (int o = 1; o < 1024; o <<= 1) {
-    unsigned int v = threadIdx.x >= o ? sh[threadIdx.x - o] : 0u;
-    __syncthreads();
-    sh[threadIdx.x] += v;
-    __syncthreads();
-  }
-  unsigned int run = sh[threadIdx.x] - loc;  // exclusive
-  for (int t = 0; t < per; t++)
-    if (b + t < nparts) {
-      unsigned int v = part[b + t];
-      part[b + t] = run;
-      run += v;
-    }
-}
-
-__global__ void __launch_bounds__(kScanThreads) k_scan_apply(const unsigned int *__restrict__ counts,
-                                                             const DevGrid *__restrict__ g,
-                                                             const unsigned int *__restrict__ part,
-                                                             unsigned int *__restrict__ cstart) {
-  __shared__ unsigned int warp_tot[32];
-  const long long m = (long long)g->ncells + 1;
-  const long long base = (long long)blockIdx.x * kScanTile;
-  if (base >= m) return;
-  static_assert(kScanPer == 4, "one uint4 per thread");
-  const long long c0 = base + (long long)threadIdx.x * kScanPer;
-  unsigned int v[kScanPer];
-  if (c0 + 3 < m) {
-    const uint4 q = *(const uint4 *)(counts + c0);
-    v[0] = q.x; v[1] = q.y; v[2] = q.z; v[3] = q.w;
-  } else {
-#pragma unroll
-    for (int t = 0; t < kScanPer; t++) v[t] = (c0 + t < m) ? counts[c0 + t] : 0u;
-  }
-  const unsigned int loc = v[0] + v[1] + v[2] + v[3];
-  // block exclusive scan of loc: warp scan + scan of warp totals
-  const int lane = threadIdx.x & 31, wid = threadIdx.x >> 5;
-  unsigned int inc = loc;
-#pragma unroll
-  for (int o = 1; o < 32; o <<= 1) {
-    unsigned int u = __shfl_up_sync(0xffffffffu, inc, o);
-    if (lane >= o) inc += u;
-  }
-  if (lane == 31) warp_tot[wid] = inc;
-  __syncthreads();
-  if (wid == 0) {
-    unsigned int t = warp_tot[lane];
-#pragma unroll
-    for (int o = 1; o < 32; o <<= 1) {
-      unsigned int u = __shfl_up_sync(0xffffffffu, t, o);
-      if (lane >= o) t += u;
-    }
-    warp_tot[lane] = t;  // inclusive over warps
-  }
-  __syncthreads();
-  const unsigned int run = part[blockIdx.x] + (wid ? warp_tot[wid - 1] : 0u) + inc - loc;
-  const unsigned int r0 = run, r1 = r0 + v[0], r2 = r1 + v[1], r3 = r2 + v[2], r4 = r3 + v[3];
-  if (c0 + 3 < m) {
-    *(uint4 *)(cstart + c0) = make_uint4(r0, r1, r2, r3);
-  } else {
-    const unsigned int rr[4] = {r0, r1, r2, r3};
-#pragma unroll
-    for (int t = 0; t < kScanPer; t++)
-      if (c0 + t < m) cstart[c0 + t] = rr[t];
-  }
-  if (c0 <= m - 1 && m - 1 <= c0 + 3) {
-    const unsigned int rr[5] = {r0, r1, r2, r3, r4};
-    cstart[m] = rr[m - c0];  // total
-  }
-}
 
 // The single-scene scan: scan tile b's offset is the sum of the totals of
 // tiles 0 .. b-1 (counted by k_keys), so one pass writes cstart.
@@ -673,23 +570,8 @@ __global__ void __launch_bounds__(kBlock) k_scatter_rank(const int *__restrict__
 }
 
 // ---------------------------------------------------------------------------
-// Scatter (counts return to zero) and in-cell rank by particle index
+// Pair records and in-cell rank by particle index
 // ---------------------------------------------------------------------------
-__global__ void __launch_bounds__(kBlock) k_scatter(const int *__restrict__ keys, long long n,
-                                                    unsigned int *__restrict__ counts,
-                                                    const unsigned int *__restrict__ cstart,
-                                                    int *__restrict__ perm_tmp, int *__restrict__ keys_sorted,
-                                                    unsigned int *__restrict__ part, long long n_parts) {
-  long long i = (long long)blockIdx.x * blockDim.x + threadIdx.x;
-  for (long long t = i; t < n_parts; t += (long long)gridDim.x * blockDim.x) part[t] = 0u;
-  if (i >= n) return;
-  int key = keys[i];
-  unsigned int old = atomicSub(&counts[key], 1u);
-  unsigned int slot = cstart[key] + old - 1u;
-  perm_tmp[slot] = (int)i;
-  keys_sorted[slot] = key;
-}
-
 // The mixed form's records of slot k (particle i): FP32 pair records, the h
 // reset and the Tait EOS on the relative density (no FP64 arithmetic); p, c
 // and the fluid h go back to the caller's arrays when asked.  eh / nf: the
@@ -991,61 +873,71 @@ __global__ void k_bt_grid(BatchPtrs B, DevCtrl *ctrl) {
   }
 }
 
+// k_keys over every instance: cell ids offset by the instance's first cell;
+// arrival ranks and scan-tile totals as in k_keys.
 __global__ void __launch_bounds__(kBlock) k_bt_keys(const double *__restrict__ x, const double *__restrict__ y,
                                                     long long n, BatchPtrs B, DevCtrl *ctrl, int *__restrict__ keys,
-                                                    int2 *__restrict__ refcell, unsigned int *__restrict__ counts) {
+                                                    int2 *__restrict__ refcell, unsigned int *__restrict__ crank,
+                                                    unsigned int *__restrict__ counts,
+                                                    unsigned int *__restrict__ part) {
   const long long i = (long long)blockIdx.x * blockDim.x + threadIdx.x;
+  const int lane = threadIdx.x & 31;
+  const bool act = i < n;
   bool alias = false, overflow = false;
-  if (i < n) {
+  int key = -1 - lane;
+  if (act) {
     const int b = B.inst[i];
     int2 ref;
-    const int key = B.coff[b] + cell_key(B.grids[b], x[i], y[i], ref, alias, overflow);
+    key = B.coff[b] + cell_key(B.grids[b], x[i], y[i], ref, alias, overflow);
     refcell[i] = ref;
     keys[i] = key;
-    atomicAdd(&counts[key], 1u);
     if (alias) atomicAdd(&B.sl[b].alias_count, 1u);
   }
+  const unsigned int below = (1u << lane) - 1u;
+  const unsigned int peers = __match_any_sync(0xffffffffu, key);
+  const int leader = __ffs(peers) - 1;
+  unsigned int base = 0;
+  if (act && lane == leader) base = atomicAdd(&counts[key], (unsigned int)__popc(peers));
+  base = __shfl_sync(0xffffffffu, base, leader);
+  if (act) crank[i] = base + (unsigned int)__popc(peers & below);
+  const int pt = act ? key / kScanTile : -1 - lane;
+  const unsigned int tpeers = __match_any_sync(0xffffffffu, pt);
+  if (act && lane == __ffs(tpeers) - 1) atomicAdd(&part[pt], (unsigned int)__popc(tpeers));
   const unsigned om = __ballot_sync(0xffffffffu, overflow);
-  if ((threadIdx.x & 31) == 0 && om) atomicOr(&ctrl->status, (unsigned)SPH_STATUS_CELL_OVERFLOW);
+  if (lane == 0 && om) atomicOr(&ctrl->status, (unsigned)SPH_STATUS_CELL_OVERFLOW);
 }
 
-// k_cellsort with the tile list of every instance: entries (instance, tile)
+// k_cellsort with the tile list of every instance (entries (instance, tile))
+// and the mixed-form records of each final slot with its instance's
+// constants; the TimeStep's min h and fluid count per instance.
 __global__ void __launch_bounds__(kBlock) k_bt_cellsort(const int *__restrict__ perm_tmp,
                                                         const int *__restrict__ keys_sorted,
                                                         const unsigned int *__restrict__ cstart,
                                                         const int2 *__restrict__ refcell, long long n, BatchPtrs B,
                                                         DevCtrl *ctrl, int *__restrict__ perm,
-                                                        int2 *__restrict__ meta) {
-  const long long k = (long long)blockIdx.x * blockDim.x + threadIdx.x;
-  if (k >= n) return;
-  const int key = keys_sorted[k];
-  const unsigned int s = cstart[key], e = cstart[key + 1];
-  const int v = perm_tmp[k];
-  unsigned int rank = 0;
-  for (unsigned int t = s; t < e; t++) rank += (unsigned)(perm_tmp[t] < v);
-  perm[s + rank] = v;
-  meta[s + rank] = refcell[v];
-  const int b = B.inst[v];
-  const int c0 = B.coff[b], lk = key - c0;
-  const DevGrid &g = B.grids[b];
-  const int ts2 = 2 * g.ts;
-  if (lk < g.ncells && (unsigned)k == __ldg(&cstart[c0 + ((lk >> ts2) << ts2)]))
-    B.tiles[atomicAdd(&ctrl->tl_count, 1u)] = make_int2(b, lk >> ts2);
-}
-
-// mixed-form records with each instance's constants; the TimeStep's min h
-// and fluid count per instance
-__global__ void __launch_bounds__(kBlock) k_bt_records(StepArgs a, const int *__restrict__ perm, BatchPtrs B,
-                                                       float4 *__restrict__ rec0, float4 *__restrict__ rec1,
-                                                       float4 *__restrict__ rec2) {
+                                                        int2 *__restrict__ meta, StepArgs a,
+                                                        float4 *__restrict__ rec0, float4 *__restrict__ rec1,
+                                                        float4 *__restrict__ rec2) {
   const long long k = (long long)blockIdx.x * blockDim.x + threadIdx.x;
   unsigned long long eh = kEncMinId;
   unsigned int nf = 0;
   int b = -1;
-  if (k < a.n) {
-    const int i = perm[k];
-    b = B.inst[i];
-    record_mixed(a, k, i, B.ip[b].rp, rec0, rec1, rec2, eh, nf);
+  if (k < n) {
+    const int key = keys_sorted[k];
+    const unsigned int s = cstart[key], e = cstart[key + 1];
+    const int v = perm_tmp[k];
+    unsigned int rank = 0;
+    for (unsigned int t = s; t < e; t++) rank += (unsigned)(perm_tmp[t] < v);
+    const unsigned int slot = s + rank;
+    perm[slot] = v;
+    meta[slot] = refcell[v];
+    b = B.inst[v];
+    const int c0 = B.coff[b], lk = key - c0;
+    const DevGrid &g = B.grids[b];
+    const int ts2 = 2 * g.ts;
+    if (lk < g.ncells && (unsigned)k == __ldg(&cstart[c0 + ((lk >> ts2) << ts2)]))
+      B.tiles[atomicAdd(&ctrl->tl_count, 1u)] = make_int2(b, lk >> ts2);
+    record_mixed(a, slot, v, B.ip[b].rp, rec0, rec1, rec2, eh, nf);
   }
   InstSlots *sl = B.sl;
   seg_min_u64(eh, b, [&](int q, unsigned long long m) { atomicMin(&sl[q].pd_hmin, m); });
@@ -1074,20 +966,16 @@ void launch_bt_bounds(const StepArgs &a, const WsPtrs &w, const BatchPtrs &B, co
   k_bt_bounds<<<nblocks(a.n), kBlock, 0, st>>>(a, B, bp, prev, cur, w.ctrl);
 }
 
+// the batched build with the records fused into the in-cell sort
 void launch_bt_build(const StepArgs &a, const WsPtrs &w, const BatchPtrs &B, cudaStream_t st) {
   const unsigned nb = nblocks(a.n);
   k_bt_grid<<<1, 256, 0, st>>>(B, w.ctrl);
-  k_bt_keys<<<nb, kBlock, 0, st>>>(a.x, a.y, a.n, B, w.ctrl, w.keys, w.refcell, w.counts);
-  k_scan_tiles<<<(unsigned)w.n_parts, kScanThreads, 0, st>>>(w.counts, B.scan, w.scan_part);
-  k_scan_top<<<1, 1024, 0, st>>>(w.scan_part, (int)w.n_parts);
-  k_scan_apply<<<(unsigned)w.n_parts, kScanThreads, 0, st>>>(w.counts, B.scan, w.scan_part, w.cstart);
-  k_scatter<<<nb, kBlock, 0, st>>>(w.keys, a.n, w.counts, w.cstart, w.perm_tmp, w.keys_sorted, w.scan_part,
-                                   w.n_parts);
-  k_bt_cellsort<<<nb, kBlock, 0, st>>>(w.perm_tmp, w.keys_sorted, w.cstart, w.refcell, a.n, B, w.ctrl, w.perm, w.meta);
-}
-
-void launch_bt_records(const StepArgs &a, const WsPtrs &w, const BatchPtrs &B, cudaStream_t st) {
-  k_bt_records<<<nblocks(a.n), kBlock, 0, st>>>(a, w.perm, B, w.rec0, w.rec1, w.rec2);
+  k_bt_keys<<<nb, kBlock, 0, st>>>(a.x, a.y, a.n, B, w.ctrl, w.keys, w.refcell, w.crank, w.counts, w.scan_part);
+  k_scan_cells<<<(unsigned)w.n_parts, kScanThreads, 0, st>>>(w.counts, B.scan, w.scan_part, w.cstart);
+  k_scatter_rank<<<nb, kBlock, 0, st>>>(w.keys, w.crank, a.n, w.counts, w.cstart, w.perm_tmp, w.keys_sorted,
+                                        w.scan_part, w.n_parts);
+  k_bt_cellsort<<<nb, kBlock, 0, st>>>(w.perm_tmp, w.keys_sorted, w.cstart, w.refcell, a.n, B, w.ctrl, w.perm, w.meta,
+                                       a, w.rec0, w.rec1, w.rec2);
 }
 
 }  // namespace sph

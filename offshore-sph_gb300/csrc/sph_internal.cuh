@@ -411,8 +411,9 @@ __device__ __forceinline__ bool mbar_try_wait(unsigned long long *bar, uint32_t 
 
 // Bounded wait for phase `parity` of bar; false when the limit ran out.
 constexpr int kMbarWaitLimit = 1 << 22;
-__device__ __forceinline__ bool mbar_wait_bounded(unsigned long long *bar, uint32_t parity) {
-  for (int it = 0; it < kMbarWaitLimit; it++)
+__device__ __forceinline__ bool mbar_wait_bounded(unsigned long long *bar, uint32_t parity,
+                                                  int limit = kMbarWaitLimit) {
+  for (int it = 0; it < limit; it++)
     if (mbar_try_wait(bar, parity)) return true;
   return false;
 }

@@ -51,6 +51,7 @@ def test_host_only_calls(lib):
     assert lib.sph_status_string(0) == b"ok"
     assert b"non-finite" in lib.sph_status_bit_string(4)
     assert b"coarsened" in lib.sph_status_bit_string(2)
+    assert b"staging" in lib.sph_status_bit_string(64)
     assert b"workspace" in lib.sph_status_string(2)
 
 
