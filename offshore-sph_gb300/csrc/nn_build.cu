@@ -46,29 +46,33 @@ struct BoundsParams {
 // an exponent decrement, so the FP64 pipe only sees the fused multiply-adds
 // of the updates.  Every input is loaded before anything depends on the
 // label, so a particle costs one memory round trip.
+// The configuration is a compile-time form (integrator, stage, damping,
+// XSPH), so that no path that a uniform flag switches off is if-converted
+// into every particle's FP64 issue.
+template <int INTEG, int STAGE, bool DAMPED, bool XSPH>
 __device__ __forceinline__ void integrate_front(const StepArgs &a, long long i, const BoundsParams &bp, bool fl,
                                                 double &x, double &y, double &rho) {
-  const bool cp = bp.stage == kStageCorrectPredict;
+  constexpr bool cp = STAGE == kStageCorrectPredict;
   const double hdt = half_exact(bp.dt_fixed_on ? bp.dt_fixed : bp.dt_cur[0]);
   const double dtc = cp ? (bp.dt_fixed_on ? bp.dt_fixed : bp.dt_prev[0]) : 0.0;
   const double vxc = a.vx[i], vyc = a.vy[i];
-  if (bp.verlet) {
+  if constexpr (INTEG == SPH_INTEGRATOR_VERLET) {
     // [Verlet.correct (src/Integrators/Verlet.py:37-53): kick, second half
     // drift with the new velocity or XSPH] then [Verlet.predict (:28-35):
     // half drift]; the density is not integrated
     double vx = vxc, vy = vyc, nx = x, ny = y;
-    if (cp) {
+    if constexpr (cp) {
       const double axv = a.ax[i], ayv = a.ay[i];
       double xs = 0.0, ys = 0.0;
-      if (bp.use_xsph) {
+      if constexpr (XSPH) {
         xs = a.xsphx[i];
         ys = a.xsphy[i];
       }
       const double hc = half_exact(dtc);
       vx = fma(dtc, axv, vx);
       vy = fma(dtc, ayv, vy);
-      nx = fma(hc, bp.use_xsph ? xs : vx, nx);
-      ny = fma(hc, bp.use_xsph ? ys : vy, ny);
+      nx = fma(hc, XSPH ? xs : vx, nx);
+      ny = fma(hc, XSPH ? ys : vy, ny);
       if (fl) {
         a.vx[i] = vx;
         a.vy[i] = vy;
@@ -86,20 +90,20 @@ __device__ __forceinline__ void integrate_front(const StepArgs &a, long long i, 
   }
   const double axv = a.ax[i], ayv = a.ay[i], drho = a.drho[i];
   double x0 = 0.0, y0 = 0.0, vx0 = 0.0, vy0 = 0.0, rho0 = 0.0, xs = 0.0, ys = 0.0;
-  if (cp && !bp.euler) {
+  if constexpr (cp && INTEG != SPH_INTEGRATOR_EULER) {
     x0 = a.x0[i];
     y0 = a.y0[i];
     vx0 = a.vx0[i];
     vy0 = a.vy0[i];
     rho0 = a.rho0[i];
   }
-  if (bp.use_xsph && !bp.euler) {
+  if constexpr (XSPH && INTEG != SPH_INTEGRATOR_EULER) {
     xs = a.xsphx[i];
     ys = a.xsphy[i];
   }
   double nx = x, ny = y, nrho = rho, vx = vxc, vy = vyc;
-  if (cp) {
-    if (bp.euler) {
+  if constexpr (cp) {
+    if constexpr (INTEG == SPH_INTEGRATOR_EULER) {
       const double hdt2 = half_exact(dtc * dtc);
       nx = fma(hdt2, axv, fma(dtc, vxc, x));
       ny = fma(hdt2, ayv, fma(dtc, vyc, y));
@@ -118,9 +122,9 @@ __device__ __forceinline__ void integrate_front(const StepArgs &a, long long i, 
       }
       return;  // Euler.predict is a no-op
     }
-    nx = fma(dtc, bp.use_xsph ? xs : vxc, x0);
-    ny = fma(dtc, bp.use_xsph ? ys : vyc, y0);
-    if (bp.damped) {
+    nx = fma(dtc, XSPH ? xs : vxc, x0);
+    ny = fma(dtc, XSPH ? ys : vyc, y0);
+    if constexpr (DAMPED) {
       const double c1 = dtc * bp.inv_damp;
       vx = fma(c1, axv, bp.c0 * vx0);
       vy = fma(c1, ayv, bp.c0 * vy0);
@@ -133,7 +137,7 @@ __device__ __forceinline__ void integrate_front(const StepArgs &a, long long i, 
   }
   // PEC.predict with this step's dt
   double px, py;
-  if (bp.use_xsph) {
+  if constexpr (XSPH) {
     px = fma(hdt, xs, nx);
     py = fma(hdt, ys, ny);
   } else {
@@ -141,7 +145,7 @@ __device__ __forceinline__ void integrate_front(const StepArgs &a, long long i, 
     py = fma(hdt, vy, ny);
   }
   double nvx = fma(hdt, axv, vx), nvy = fma(hdt, ayv, vy);
-  if (bp.damped) {
+  if constexpr (DAMPED) {
     nvx *= bp.inv_damp;
     nvy *= bp.inv_damp;
   }
@@ -167,19 +171,20 @@ __device__ __forceinline__ void integrate_front(const StepArgs &a, long long i, 
 // One particle's part of k_bounds: the integrator work in front of the build
 // and its six bound values (minima; maxima as minima of the complement),
 // folded into v.
+template <int INTEG, int STAGE, bool DAMPED, bool XSPH>
 __device__ __forceinline__ void bounds_one(const StepArgs &a, long long i, const BoundsParams &bp,
                                            unsigned long long (&v)[6], bool &bad) {
   const int8_t lab = a.label[i];
   double x = a.x[i], y = a.y[i];
   const double h = a.h[i];
   const bool fl = is_fluid(lab);
-  const bool front = bp.stage != kStageNone;
+  constexpr bool front = STAGE != kStageNone;
   const bool hcomp = bp.h_reset && !bp.h_fixed_on;
   double rho = (front || hcomp) ? a.rho[i] : 0.0;
   const double m = hcomp ? a.m[i] : 0.0;
-  if (front) integrate_front(a, i, bp, fl, x, y, rho);
+  if constexpr (front) integrate_front<INTEG, STAGE, DAMPED, XSPH>(a, i, bp, fl, x, y, rho);
   double hn = h;
-  if (fl && bp.h_reset) hn = bp.h_fixed_on ? bp.h_fixed : compute_h(m, rho);
+  if (fl && bp.h_reset) hn = bp.h_fixed_on ? bp.h_fixed : compute_h_call(m, rho);
   if (!(finite_bits(x) && finite_bits(y) && finite_bits(h))) {
     bad = true;
     return;
@@ -202,6 +207,7 @@ __device__ void grid_from_bounds(DevCtrl *ctrl, DevGrid *g, const GridParams &gp
 #define SPH_BOUNDS_BLOCKS 4
 #endif
 constexpr int kBoundsBlocks = SPH_BOUNDS_BLOCKS;  // resident blocks per SM
+template <int INTEG, int STAGE, bool DAMPED, bool XSPH>
 __global__ void __launch_bounds__(kBlock, kBoundsBlocks) k_bounds(StepArgs a, DevCtrl *ctrl, BoundsParams bp,
                                                                   DevGrid *g, GridParams gp) {
   __shared__ unsigned long long red[kBlock / 32][6];
@@ -210,7 +216,7 @@ __global__ void __launch_bounds__(kBlock, kBoundsBlocks) k_bounds(StepArgs a, De
   bool bad = false;
   const long long stride = (long long)gridDim.x * blockDim.x;
   for (long long i = (long long)blockIdx.x * blockDim.x + threadIdx.x; i < a.n; i += stride)
-    bounds_one(a, i, bp, v, bad);
+    bounds_one<INTEG, STAGE, DAMPED, XSPH>(a, i, bp, v, bad);
   if (__syncthreads_or(bad) && threadIdx.x == 0) atomicOr(&ctrl->status, (unsigned)SPH_STATUS_NONFINITE);
   const int lane = threadIdx.x & 31, wid = threadIdx.x >> 5;
 #pragma unroll
@@ -224,10 +230,9 @@ __global__ void __launch_bounds__(kBlock, kBoundsBlocks) k_bounds(StepArgs a, De
     unsigned long long m = kEncMinId;
     for (int w = 0; w < kBlock / 32; w++) m = red[w][q] < m ? red[w][q] : m;
     if (m != kEncMinId) {
-      unsigned long long *slot[6] = {&ctrl->xmin, &ctrl->xmax, &ctrl->ymin, &ctrl->ymax, &ctrl->hmin_all,
-                                     &ctrl->hmax_new};
-      if (q & 1) atomicMax(slot[q], ~m);
-      else atomicMin(slot[q], m);
+      unsigned long long *slot = &ctrl->xmin + q;  // xmin, xmax, ymin, ymax, hmin_all, hmax_new
+      if (q & 1) atomicMax(slot, ~m);
+      else atomicMin(slot, m);
     }
   }
   __syncthreads();
@@ -240,6 +245,42 @@ __global__ void __launch_bounds__(kBlock, kBoundsBlocks) k_bounds(StepArgs a, De
     __threadfence();
     ctrl->bounds_done = 0;
     grid_from_bounds(ctrl, g, gp);
+  }
+}
+
+// Calls f.template operator()<INTEG, STAGE, DAMPED, XSPH>() for the compile-
+// time form of bp (the combinations the integrators use).
+template <typename F>
+static void front_dispatch(const BoundsParams &bp, F &&f) {
+  const bool d = bp.damped != 0, x = bp.use_xsph != 0;
+  if (bp.stage == kStageNone) {
+    f.template operator()<SPH_INTEGRATOR_PEC, kStageNone, false, false>();
+  } else if (bp.euler) {  // Euler.predict is a no-op: only the corrector stage reaches here
+    f.template operator()<SPH_INTEGRATOR_EULER, kStageCorrectPredict, false, false>();
+  } else if (bp.verlet) {
+    if (bp.stage == kStagePredict) {
+      if (x) f.template operator()<SPH_INTEGRATOR_VERLET, kStagePredict, false, true>();
+      else f.template operator()<SPH_INTEGRATOR_VERLET, kStagePredict, false, false>();
+    } else {
+      if (x) f.template operator()<SPH_INTEGRATOR_VERLET, kStageCorrectPredict, false, true>();
+      else f.template operator()<SPH_INTEGRATOR_VERLET, kStageCorrectPredict, false, false>();
+    }
+  } else if (bp.stage == kStagePredict) {
+    if (d) {
+      if (x) f.template operator()<SPH_INTEGRATOR_PEC, kStagePredict, true, true>();
+      else f.template operator()<SPH_INTEGRATOR_PEC, kStagePredict, true, false>();
+    } else {
+      if (x) f.template operator()<SPH_INTEGRATOR_PEC, kStagePredict, false, true>();
+      else f.template operator()<SPH_INTEGRATOR_PEC, kStagePredict, false, false>();
+    }
+  } else {
+    if (d) {
+      if (x) f.template operator()<SPH_INTEGRATOR_PEC, kStageCorrectPredict, true, true>();
+      else f.template operator()<SPH_INTEGRATOR_PEC, kStageCorrectPredict, true, false>();
+    } else {
+      if (x) f.template operator()<SPH_INTEGRATOR_PEC, kStageCorrectPredict, false, true>();
+      else f.template operator()<SPH_INTEGRATOR_PEC, kStageCorrectPredict, false, false>();
+    }
   }
 }
 
@@ -273,7 +314,11 @@ void launch_bounds(const StepArgs &a, const WsPtrs &w, const sph_config_t &cfg, 
   bp.damped = cfg.damping != 0.0 ? 1 : 0;
   bp.use_xsph = cfg.pec_use_xsph;
   bp.strict = cfg.pec_strict;
-  k_bounds<<<persist_blocks(a.n, kBoundsBlocks), kBlock, 0, st>>>(a, w.ctrl, bp, w.grid, grid_params(w, cfg, wc));
+  const GridParams gp = grid_params(w, cfg, wc);
+  const unsigned nb = persist_blocks(a.n, kBoundsBlocks);
+  front_dispatch(bp, [&]<int I, int S, bool D, bool X>() {
+    k_bounds<I, S, D, X><<<nb, kBlock, 0, st>>>(a, w.ctrl, bp, w.grid, gp);
+  });
 }
 
 
@@ -647,7 +692,7 @@ __device__ __forceinline__ void record_fp64(const StepArgs &a, long long k, int 
   split_df(y, yh, yl);
   const float mf = d2f_trunc(m);
   double h = a.h[i];
-  if (fl && !rp.from_state) h = rp.h_fixed_on ? rp.h_fixed : compute_h(m, rho);
+  if (fl && !rp.from_state) h = rp.h_fixed_on ? rp.h_fixed : compute_h_call(m, rho);
   const double p = rp.from_state ? a.p[i] : tait_p(rho, lab, rp.gamma, rp.B, rp.inv_rho0, rp.Pb);
   const double othr = p / (rho * rho);
   const double hs = fl ? h : -h;
@@ -819,6 +864,7 @@ void launch_records(const StepArgs &a, const WsPtrs &w, const sph_config_t &cfg,
 // global ids sorts every instance at once and keeps each instance's slots in
 // its particle range.
 // ---------------------------------------------------------------------------
+template <int INTEG, int STAGE, bool DAMPED, bool XSPH>
 __global__ void __launch_bounds__(kBlock) k_bt_bounds(StepArgs a, BatchPtrs B, BoundsParams bp, int prev, int cur,
                                                       DevCtrl *ctrl) {
   const long long i = (long long)blockIdx.x * blockDim.x + threadIdx.x;
@@ -833,7 +879,7 @@ __global__ void __launch_bounds__(kBlock) k_bt_bounds(StepArgs a, BatchPtrs B, B
     bi.h_fixed_on = rp.h_fixed_on;
     bi.dt_prev = B.sl[b].dt_ring[prev];
     bi.dt_cur = B.sl[b].dt_ring[cur];
-    bounds_one(a, i, bi, v, bad);
+    bounds_one<INTEG, STAGE, DAMPED, XSPH>(a, i, bi, v, bad);
   }
   if (__syncthreads_or(bad) && threadIdx.x == 0) atomicOr(&ctrl->status, (unsigned)SPH_STATUS_NONFINITE);
   InstSlots *sl = B.sl;
@@ -963,7 +1009,9 @@ void launch_bt_bounds(const StepArgs &a, const WsPtrs &w, const BatchPtrs &B, co
   bp.damped = cfg.damping != 0.0 ? 1 : 0;
   bp.use_xsph = cfg.pec_use_xsph;
   bp.strict = cfg.pec_strict;
-  k_bt_bounds<<<nblocks(a.n), kBlock, 0, st>>>(a, B, bp, prev, cur, w.ctrl);
+  front_dispatch(bp, [&]<int I, int S, bool D, bool X>() {
+    k_bt_bounds<I, S, D, X><<<nblocks(a.n), kBlock, 0, st>>>(a, B, bp, prev, cur, w.ctrl);
+  });
 }
 
 // the batched build with the records fused into the in-cell sort

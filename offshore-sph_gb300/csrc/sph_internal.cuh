@@ -10,6 +10,7 @@
 
 #include <cuda_runtime.h>
 #include <math.h>
+#include <stddef.h>
 #include <stdint.h>
 
 #include "sph_gb300.h"
@@ -50,13 +51,15 @@ __device__ __forceinline__ bool finite_bits(double v) {
 // ---------------------------------------------------------------------------
 // double <-> float on the integer pipe
 // ---------------------------------------------------------------------------
-// float -> double, exact
+// float -> double, exact; denormals through an out-of-line conversion, so
+// that the compiler cannot if-convert it into every thread's path
+static __device__ __noinline__ double f2d_slow(float f) { return (double)f; }
 __device__ __forceinline__ double f2d(float f) {
   unsigned u = __float_as_uint(f);
   unsigned s = u & 0x80000000u, e = (u >> 23) & 0xffu, m = u & 0x7fffffu;
   unsigned long long r;
   if (e == 0u) {
-    if (m != 0u) return (double)f;  // denormal (never in practice)
+    if (m != 0u) return f2d_slow(f);  // denormal (never in practice)
     r = (unsigned long long)s << 32;
   } else if (e == 0xffu) {
     r = ((unsigned long long)(s | 0x7ff00000u | (m >> 3)) << 32) | ((unsigned long long)(m & 7u) << 29);
@@ -153,6 +156,14 @@ struct DevCtrl {
   unsigned int bounds_done;  // finished blocks of the bounds pass (its last block sets the grid)
   double dt_ring[2][3];  // {dt, dt_c, dt_f} of the step with that parity
 };
+
+// the bound slots are consecutive (k_bounds indexes them from xmin)
+static_assert(offsetof(DevCtrl, xmax) == offsetof(DevCtrl, xmin) + 8 &&
+                  offsetof(DevCtrl, ymin) == offsetof(DevCtrl, xmin) + 16 &&
+                  offsetof(DevCtrl, ymax) == offsetof(DevCtrl, xmin) + 24 &&
+                  offsetof(DevCtrl, hmin_all) == offsetof(DevCtrl, xmin) + 32 &&
+                  offsetof(DevCtrl, hmax_new) == offsetof(DevCtrl, xmin) + 40,
+              "bound slots of DevCtrl");
 
 // Search grid, written by the grid kernel of each neighbour build.
 struct DevGrid {
@@ -566,9 +577,14 @@ __device__ __forceinline__ double compute_h(double m, double rho) {
   return rho > 1e-12 ? 1.3 * sqrt(m / rho) : 0.0;
 }
 
+// computeH out of line: a path that selects it by a uniform flag calls it
+// only when taken (inlined, the compiler evaluates both sides of the select,
+// and its division and square root then cost every particle FP64 issue)
+static __device__ __noinline__ double compute_h_call(double m, double rho) { return compute_h(m, rho); }
+
 // The fluid h of the h reset (Solver.py:242-246)
 __device__ __forceinline__ double reset_h(double h_fixed, double m, double rho) {
-  return h_fixed > 0.0 ? h_fixed : compute_h(m, rho);
+  return h_fixed > 0.0 ? h_fixed : compute_h_call(m, rho);
 }
 
 // ---------------------------------------------------------------------------

@@ -20,7 +20,7 @@ LIB = os.path.join(LIBDIR, "libsph_gb300.so")
 
 SOURCES = ["nn_build.cu", "pair.cu", "integrate.cu", "capi.cu", "static_ws.cu", "adjoint.cu", "batch.cu", "newmark.cu"]
 ARCH = ["-gencode", "arch=compute_103a,code=sm_103a"]
-FLAGS = ["-O3", "-std=c++17", "-lineinfo", "-Xcompiler", "-fPIC", "--expt-relaxed-constexpr",
+FLAGS = ["-O3", "-std=c++20", "-lineinfo", "-Xcompiler", "-fPIC", "--expt-relaxed-constexpr",
          "-I", INCLUDE, "-I", CSRC]
 # the mixed-form pair arithmetic flushes FP32 denormals: its reciprocals and
 # square roots then take the plain hardware approximations (the FP64 form is
