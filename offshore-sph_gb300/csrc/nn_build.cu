@@ -621,9 +621,16 @@ __global__ void __launch_bounds__(kBlock) k_scatter_rank(const int *__restrict__
 // reset and the Tait EOS on the relative density (no FP64 arithmetic); p, c
 // and the fluid h go back to the caller's arrays when asked.  eh / nf: the
 // fluid h for the TimeStep reduction.
-__device__ __forceinline__ void record_mixed(const StepArgs &a, long long k, int i, const RecParams &rp,
-                                             float4 *__restrict__ rec0, float4 *__restrict__ rec1,
-                                             float4 *__restrict__ rec2, unsigned long long &eh, unsigned int &nf) {
+// HSRC: where the fluid h and p come from (kHState: the caller's arrays, the
+// second summation-density pass; kHFixed: the fixed h; kHCompute: computeH
+// in FP32); PB: a nonzero background pressure.  Compile-time, so that the
+// paths a run does not take are not if-converted into every particle.
+enum { kHState = 0, kHFixed = 1, kHCompute = 2 };
+template <int HSRC, bool PB>
+__device__ __forceinline__ void record_mixed_t(const StepArgs &a, long long k, int i, const RecParams &rp,
+                                               float4 *__restrict__ rec0, float4 *__restrict__ rec1,
+                                               float4 *__restrict__ rec2, unsigned long long &eh,
+                                               unsigned int &nf) {
   const int8_t lab = a.label[i];
   const bool fl = is_fluid(lab);
   const double m = a.m[i], rho = a.rho[i];
@@ -637,10 +644,10 @@ __device__ __forceinline__ void record_mixed(const StepArgs &a, long long k, int
   split_df(rho, rh, rl);
   float hf;
   double hd;
-  if (rp.from_state || !fl) {
+  if (HSRC == kHState || !fl) {
     hd = a.h[i];
     hf = d2f_trunc(hd);
-  } else if (rp.h_fixed_on) {
+  } else if (HSRC == kHFixed) {
     hd = rp.h_fixed;
     hf = rp.h_fixed_f;
   } else {
@@ -649,14 +656,14 @@ __device__ __forceinline__ void record_mixed(const StepArgs &a, long long k, int
   }
   float pf;  // gauge pressure B ((rho/rho0)^gamma - 1), FP32
   double pd;
-  if (rp.from_state) {
+  if constexpr (HSRC == kHState) {
     pd = a.p[i];
     pf = d2f_trunc(pd) - rp.Pb_f;
   } else {
     const float d = ((rh - rp.rho0_hi) + (rl - rp.rho0_lo)) * rp.inv_rho0_f;
     pf = fl ? rp.B_f * tait_ratio_m1_f(d, rp.gamma_f) : 0.f;
     pd = f2d(pf);
-    if (rp.Pb_on) pd += rp.Pb;
+    if constexpr (PB) pd += rp.Pb;
   }
   const float ir = rh != 0.f ? __frcp_rn(rh) : 0.f;
   const float othr = (pf + rp.Pb_f) * ir * ir;
@@ -675,6 +682,22 @@ __device__ __forceinline__ void record_mixed(const StepArgs &a, long long k, int
     const unsigned long long e = enc_d(hd);
     eh = e < eh ? e : eh;
     nf++;
+  }
+}
+
+// record_mixed_t for the flags of rp (runtime form)
+__device__ __forceinline__ void record_mixed(const StepArgs &a, long long k, int i, const RecParams &rp,
+                                             float4 *__restrict__ rec0, float4 *__restrict__ rec1,
+                                             float4 *__restrict__ rec2, unsigned long long &eh, unsigned int &nf) {
+  if (rp.from_state) {
+    if (rp.Pb_on) record_mixed_t<kHState, true>(a, k, i, rp, rec0, rec1, rec2, eh, nf);
+    else record_mixed_t<kHState, false>(a, k, i, rp, rec0, rec1, rec2, eh, nf);
+  } else if (rp.h_fixed_on) {
+    if (rp.Pb_on) record_mixed_t<kHFixed, true>(a, k, i, rp, rec0, rec1, rec2, eh, nf);
+    else record_mixed_t<kHFixed, false>(a, k, i, rp, rec0, rec1, rec2, eh, nf);
+  } else {
+    if (rp.Pb_on) record_mixed_t<kHCompute, true>(a, k, i, rp, rec0, rec1, rec2, eh, nf);
+    else record_mixed_t<kHCompute, false>(a, k, i, rp, rec0, rec1, rec2, eh, nf);
   }
 }
 
@@ -743,7 +766,7 @@ __device__ __forceinline__ void reduce_h_block(unsigned long long eh, unsigned i
 // same thread then writes the pair records of its final slot (the records
 // pass fused in: kRecMixed FP32 records, kRecFp64 FP64 records).
 enum { kRecNone = 0, kRecMixed = 1, kRecFp64 = 2 };
-template <int REC>
+template <int REC, int HSRC = kHFixed, bool PB = false>
 __global__ void __launch_bounds__(kBlock) k_cellsort(const int *__restrict__ perm_tmp,
                                                      const int *__restrict__ keys_sorted,
                                                      const unsigned int *__restrict__ cstart,
@@ -771,7 +794,7 @@ __global__ void __launch_bounds__(kBlock) k_cellsort(const int *__restrict__ per
     const unsigned int slot = s + rank;
     perm[slot] = v;
     meta[slot] = refcell[v];
-    if (REC == kRecMixed) record_mixed(a, slot, v, rp, rec0, rec1, rec2, eh, nf);
+    if (REC == kRecMixed) record_mixed_t<HSRC, PB>(a, slot, v, rp, rec0, rec1, rec2, eh, nf);
     if (REC == kRecFp64) record_fp64(a, slot, v, rp, rec0, r64a, r64b, eh, nf);
   }
   if (REC != kRecNone && rp.reduce_h) reduce_h_block(eh, nf, red, redn, ctrl);
@@ -810,12 +833,28 @@ void launch_build(const StepArgs &a, const WsPtrs &w, const sph_config_t &cfg, c
                                         w.scan_part, w.n_parts);
   RecParams none;
   memset(&none, 0, sizeof(none));
-#define SPH_CELLSORT(R, P)                                                                                   \
-  k_cellsort<R><<<nb, kBlock, 0, st>>>(w.perm_tmp, w.keys_sorted, w.cstart, w.refcell, a.n, w.grid, w.ctrl, \
-                                       w.perm, w.meta, w.tiles, a, P, w.rec0, w.rec1, w.rec2, w.rec64a, w.rec64b)
-  if (!rp) SPH_CELLSORT(kRecNone, none);
-  else if (cfg.precision == SPH_PREC_MIXED) SPH_CELLSORT(kRecMixed, *rp);
-  else SPH_CELLSORT(kRecFp64, *rp);
+#define SPH_CELLSORT(P, ...)                                                                                   \
+  k_cellsort<__VA_ARGS__><<<nb, kBlock, 0, st>>>(w.perm_tmp, w.keys_sorted, w.cstart, w.refcell, a.n, w.grid,   \
+                                                 w.ctrl, w.perm, w.meta, w.tiles, a, P, w.rec0, w.rec1, w.rec2, \
+                                                 w.rec64a, w.rec64b)
+  if (!rp) {
+    SPH_CELLSORT(none, kRecNone);
+  } else if (cfg.precision == SPH_PREC_MIXED) {
+    const int hs = rp->from_state ? kHState : (rp->h_fixed_on ? kHFixed : kHCompute);
+    const bool pb = rp->Pb_on != 0;
+    if (hs == kHState) {
+      if (pb) SPH_CELLSORT(*rp, kRecMixed, kHState, true);
+      else SPH_CELLSORT(*rp, kRecMixed, kHState, false);
+    } else if (hs == kHFixed) {
+      if (pb) SPH_CELLSORT(*rp, kRecMixed, kHFixed, true);
+      else SPH_CELLSORT(*rp, kRecMixed, kHFixed, false);
+    } else {
+      if (pb) SPH_CELLSORT(*rp, kRecMixed, kHCompute, true);
+      else SPH_CELLSORT(*rp, kRecMixed, kHCompute, false);
+    }
+  } else {
+    SPH_CELLSORT(*rp, kRecFp64);
+  }
 #undef SPH_CELLSORT
 }
 
