@@ -859,12 +859,12 @@ void launch_build(const StepArgs &a, const WsPtrs &w, const sph_config_t &cfg, c
 }
 
 // ---------------------------------------------------------------------------
-// Sorted pair records.  The h reset and the Tait EOS of _loop's first pass
-// (SolverTools.py:122-127) are fused here; p, c and the fluid h go back to
-// the caller's arrays.
+// Sorted pair records as a pass of their own, for the builds whose in-cell
+// sort did not write them (the second summation-density pass, the adjoint's
+// half state).  The h reset and the Tait EOS of _loop's first pass
+// (SolverTools.py:122-127) are done here; p, c and the fluid h go back to the
+// caller's arrays.
 // ---------------------------------------------------------------------------
-
-
 template <bool MIXED>
 __global__ void __launch_bounds__(kBlock) k_records(StepArgs a, const int *__restrict__ perm, RecParams rp,
                                                     DevCtrl *ctrl, float4 *__restrict__ rec0,

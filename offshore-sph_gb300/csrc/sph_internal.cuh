@@ -165,7 +165,8 @@ static_assert(offsetof(DevCtrl, xmax) == offsetof(DevCtrl, xmin) + 8 &&
                   offsetof(DevCtrl, hmax_new) == offsetof(DevCtrl, xmin) + 40,
               "bound slots of DevCtrl");
 
-// Search grid, written by the grid kernel of each neighbour build.
+// Search grid, written by the last block of the bounds pass of each
+// neighbour build (the batched form: by its grid kernel, per instance).
 struct DevGrid {
   // reference grid (src/Tools/NNLinkedList.py:86-127)
   double xmin, xmax, ymin, ymax, cs, inv_cs;
