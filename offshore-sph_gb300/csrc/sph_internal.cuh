@@ -339,15 +339,24 @@ static __device__ __noinline__ long long ref_floor_div_slow(double a, double o, 
 }
 
 // The same binning with an FP32 fast path: the FP32 estimate decides unless
-// it lands within 1e-3 cells of a cell edge (then the exact FP64 test does).
+// it lands within its error bound of a cell edge (then the exact FP64 test
+// does).  With af = a truncated to FP32 (relative error 2^-23), of = o and
+// inv_sf = 1/s rounded (2^-24 each) and two rounded FP32 operations, the
+// estimate t is within ((|af| + |of|) inv_sf + t) 2^-22 of the exact
+// (a - o) / s; the margin doubles that, and the FP64 quotient of the
+// reference is within 2^-52 t of the exact one, far inside it.  So the few
+// particles in the margin are the only ones that take the FP64 division (a
+// lane or two of a warp, each costing the warp the slow FP64 pipe).
 __device__ __forceinline__ long long ref_cell(double a, double o, double s, double inv_s, float of, float inv_sf) {
   const float af = d2f_trunc(a);
   const float t = (af - of) * inv_sf;
-  const bool range = t >= 0.f && t < 1e6f && (fabsf(af) + fabsf(of)) * inv_sf < 4000.f;
+  const float span = (fabsf(af) + fabsf(of)) * inv_sf;
+  const bool range = t >= 0.f && t < 1e6f && span < 4000.f;
   float f;
   const int c = floor_small(range ? t : 0.f, f);
   const float fr = t - f;
-  if (range && fr > 1e-3f && fr < 1.0f - 1e-3f) return c;
+  const float mg = (span + t) * 4.76837158e-7f + 9.5367432e-7f;  // 2^-21 (span + t) + 2^-20
+  if (range && fr > mg && fr < 1.0f - mg) return c;
   return ref_floor_div_slow(a, o, s, inv_s);
 }
 
