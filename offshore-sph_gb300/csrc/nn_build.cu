@@ -435,6 +435,8 @@ __device__ unsigned grid_setup(double xmin, double xmax, double ymin, double yma
     int wd = (int)ceil(3.0 * hmax * (1.0 + 1e-6) / ct) + 1;
     g->wide = wd < 2 ? 2 : (wd > 1024 ? 1024 : wd);
   }
+  g->txmaxf = (float)(g->ntx - 1);
+  g->tymaxf = (float)(g->nty - 1);
   g->valid = 1;
   return status;
 }
@@ -477,8 +479,8 @@ __device__ __forceinline__ int cell_key(const DevGrid &g, double xi, double yi, 
     } else {
       // FP32 binning, monotone in the position (query and candidates agree)
       float ft;
-      const float tx = fminf(fmaxf((d2f_trunc(xi) - g.oxf) * g.inv_ctf, 0.f), (float)(g.ntx - 1));
-      const float ty = fminf(fmaxf((d2f_trunc(yi) - g.oyf) * g.inv_ctf, 0.f), (float)(g.nty - 1));
+      const float tx = fminf(fmaxf((d2f_trunc(xi) - g.oxf) * g.inv_ctf, 0.f), g.txmaxf);
+      const float ty = fminf(fmaxf((d2f_trunc(yi) - g.oyf) * g.inv_ctf, 0.f), g.tymaxf);
       if (g.ntx < (1 << 22) && g.nty < (1 << 22))
         key = tiled_key(floor_small(tx, ft), floor_small(ty, ft), g.ts, g.ntlx);
       else
@@ -547,10 +549,7 @@ __global__ void __launch_bounds__(kScanThreads) k_scan_cells(const unsigned int 
   const long long m = (long long)g->ncells + 1;
   const long long base = (long long)blockIdx.x * kScanTile;
   if (base >= m) return;
-  unsigned int pre = 0;
-  for (int t = threadIdx.x; t < (int)blockIdx.x; t += kScanThreads) pre += part[t];
-  pre = block_reduce(pre, AddU32(), 0u, red);
-  if (threadIdx.x == 0) s_pre = pre;
+  // the tile's counts and the earlier tiles' totals load together
   const long long c0 = base + (long long)threadIdx.x * kScanPer;
   unsigned int v[kScanPer];
   if (c0 + 3 < m) {
@@ -560,6 +559,10 @@ __global__ void __launch_bounds__(kScanThreads) k_scan_cells(const unsigned int 
 #pragma unroll
     for (int t = 0; t < kScanPer; t++) v[t] = (c0 + t < m) ? counts[c0 + t] : 0u;
   }
+  unsigned int pre = 0;
+  for (int t = threadIdx.x; t < (int)blockIdx.x; t += kScanThreads) pre += part[t];
+  pre = block_reduce(pre, AddU32(), 0u, red);
+  if (threadIdx.x == 0) s_pre = pre;
   const unsigned int loc = v[0] + v[1] + v[2] + v[3];
   const int lane = threadIdx.x & 31, wid = threadIdx.x >> 5;
   unsigned int inc = loc;

@@ -1050,8 +1050,8 @@ __device__ __forceinline__ int probe_cell(const DevGrid &g, double x, double y, 
     W = 1;
     return 0;
   }
-  const float tx = fminf(fmaxf((d2f_trunc(x) - g.oxf) * g.inv_ctf, 0.f), (float)(g.ntx - 1));
-  const float ty = fminf(fmaxf((d2f_trunc(y) - g.oyf) * g.inv_ctf, 0.f), (float)(g.nty - 1));
+  const float tx = fminf(fmaxf((d2f_trunc(x) - g.oxf) * g.inv_ctf, 0.f), g.txmaxf);
+  const float ty = fminf(fmaxf((d2f_trunc(y) - g.oyf) * g.inv_ctf, 0.f), g.tymaxf);
   const int kx = min(max((int)floorf(tx), 0), g.ntx - 1), ky = min(max((int)floorf(ty), 0), g.nty - 1);
   const double reach = 1.5 * (h + g.hmax) * (1.0 + 1e-6);
   const double wd = ceil(reach / g.ct) + 1.0;

@@ -180,6 +180,7 @@ struct DevGrid {
   int ts;      // cells are numbered in tiles of 2^ts x 2^ts, row-major inside a tile
   int ntlx;    // tiles per row
   float oxf, oyf, inv_ctf;  // mode 1 binning (FP32, monotone)
+  float txmaxf, tymaxf;     // ntx - 1, nty - 1 in FP32 (the binning's clamps)
   int wt;           // stencil half-width of the pair kernels
   int need_filter;  // mode 1: candidates must pass the reference-stencil test
   int wide;         // mode 1: half-width covering q <= 3 at hmax (export, aliased queries)
