@@ -223,7 +223,7 @@ def time_graph_steps(graphs):
     return s.elapsed_time(e) / 1e3
 
 
-def e2e_steps(core, dp, wc, cfg, ws, k, pa):
+def e2e_steps(core, dp, wc, cfg, ws, k, pa, result=None):
     """Steps through the C ABI with the particle state on the HOST: each step
     copies its inputs host -> device (pinned) and its results back, and the
     next step starts from the host's copy.  The host link carries about
@@ -233,7 +233,8 @@ def e2e_steps(core, dp, wc, cfg, ws, k, pa):
       while step s computes;
     - each result field goes up for step s + 1 as soon as its download of
       step s has finished, while the next field comes down.
-    Returns (seconds, bytes in per step, bytes out per step)."""
+    Returns (seconds, bytes in per step, bytes out per step); with a dict
+    `result`, also the host copy of the last step's results in it."""
     import torch
     from sph import state
     fconst = ("m", "h", "c")
@@ -284,6 +285,8 @@ def e2e_steps(core, dp, wc, cfg, ws, k, pa):
     e.record(comp)
     torch.cuda.synchronize()
     del other
+    if result is not None:
+        result.update({f: host[f].numpy().copy() for f in fout})
     return s.elapsed_time(e) / 1e3, h2d, d2h
 
 
