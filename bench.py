@@ -607,11 +607,10 @@ def main():
     clk = clocks.stop()
     ws.check()
     el, value = replica_value(el, nfluid, args.steps, world, "cuda")
-    # per step: bounds/predict, grid, keys, 3 scan passes, scatter, cellsort,
-    # records, pair tiles, pair fallback list (mixed) or one FP64 pair kernel;
-    # per sph_run call also the initial TimeStep and the last corrector
-    # k_bounds, k_keys, k_scan_cells, k_scatter_rank, k_cellsort, then
-    # k_pair_tiles + k_pair_list (mixed) or k_pair (FP64)
+    # per step: k_bounds (corrector + predictor + bounds + grid), k_keys,
+    # k_scan_cells, k_scatter_rank, k_cellsort (+ records), then
+    # k_pair_tiles + k_pair_list (mixed) or k_pair (FP64); per sph_run call
+    # also the initial TimeStep and the last corrector
     launches_per_step = 7 if args.precision == "mixed" else 6
     gsteps, reps, rem = graph_plan(args.steps)
     launches = launches_per_step * args.steps + 2 * (reps + (1 if rem else 0))
