@@ -42,6 +42,11 @@ STEP_BYTES = 385    # algorithmic bytes of one PEC step per particle (dt 32 + pr
 # captures summarised in profiles/ (dram__bytes_read.sum + dram__bytes_write.sum
 # of k_pair_tiles over its particle count)
 TRAFFIC_PER_PARTICLE = {("dambreak1m", "mixed"): 62.5}  # profiles/k_pair_tiles_dambreak1m.md
+# what bounds the pair kernel instead of HBM, from the same captures
+LIMITER = {"mixed": "instruction issue: 70.6% of cycles issue, DRAM 4.2% of peak "
+                    "(profiles/k_pair_tiles_dambreak1m.md)",
+           "fp64": "FP64 pipe: busy 86.5% of active cycles, DRAM 0.5% of peak "
+                   "(profiles/k_pair_fp64_dambreak1m.md)"}
 
 
 def workload(name):
@@ -642,7 +647,8 @@ def main():
                            "achieved": ach, "peak": hbm, "unit": "GB/s", "frac": ach / hbm,
                            "peak_kind": peak_kind, "traffic": traffic * dp.n if traffic else None,
                            "algorithmic_bytes_per_launch": dp.n * PAIR_BYTES,
-                           "step_achieved_gbs": dp.n * STEP_BYTES / step_s / 1e9}
+                           "step_achieved_gbs": dp.n * STEP_BYTES / step_s / 1e9,
+                           "limiter": LIMITER.get(args.precision)}
         # the GPU's own FP64 path on the same workload
         if args.precision == "mixed":
             dp64, wc64, cfg64, ws64 = prepare(wl, "fp64")
