@@ -176,6 +176,44 @@ def test_step_sequence_matches_oracle_dam_break(sph):
     assert not bad, bad
 
 
+@pytest.mark.parametrize("xsph", [False, True])
+def test_damped_steps_match_oracle(sph, xsph):
+    """20 damped PEC steps (damping 0.05, the Solver's default while it
+    settles; with and without XSPH) of the 3200-fluid dam break, FP64,
+    against the oracle. This runs the damped forms of the fused
+    corrector + predictor."""
+    import oracle
+    import torch
+    from sph import scenarios as S
+    core, state = sph
+    pa = S.cfg_dam_break_small()
+    dx, damping = 0.025, 0.05
+    P = oracle.Particles(arrays={k: pa[k] for k in pa.dtype.names if k != "deleted"})
+    par = oracle.wcsph_params(2.0, dx, 1000.0, use_xsph=xsph)
+    oracle.setup(P, par, 2.0, 1.3 * dx)
+    init = P.as_dict()
+    dp = state.DeviceParticles.from_array(_to_array(init))
+    wc = core.wcsph_struct(2.0, dx, 1000.0, use_xsph=xsph)
+    cfg = core.config_struct(precision="fp64", pec_use_xsph=xsph, pec_strict=True, h_fixed=1.3 * dx, cfl_c=0.3,
+                             cfl_f=0.25, damping=damping)
+    ws = state.DeviceWorkspace(dp.n)
+    nsteps = 20
+    hist = torch.zeros((nsteps, 3), dtype=torch.float64, device="cuda")
+    core.run(dp, wc, cfg, ws, nsteps, hist)
+    ws.check()
+    dts = oracle.run(par, oracle.NN(2.0), P, nsteps, h_fixed=1.3 * dx, gamma_c=0.3, gamma_f=0.25, damping=damping,
+                     pec_use_xsph=xsph, nthreads=8)
+    np.testing.assert_allclose(hist.cpu().numpy(), dts, rtol=1e-9)
+    bad = SC.compare_state(dp.soa(), P.as_dict(), SC.STATE_FIELDS, 1e-8)
+    assert not bad, bad
+    # damping slowed the fluid against the undamped run
+    und = oracle.Particles(arrays={k: v.copy() for k, v in init.items()})
+    oracle.run(par, oracle.NN(2.0), und, nsteps, h_fixed=1.3 * dx, gamma_c=0.3, gamma_f=0.25, pec_use_xsph=xsph,
+               nthreads=8)
+    f = init["label"] == 0
+    assert np.linalg.norm(P.vy[f]) < np.linalg.norm(und.vy[f])
+
+
 def _lattice_state(n, kernel, seed=0):
     from sph import scenarios as S
     import oracle
