@@ -69,6 +69,47 @@ def test_invalid_arguments_rejected_on_host(lib):
     assert lib.sph_compute(C.byref(pa), C.byref(wc), C.byref(bad), C.byref(ws), None) == 1
 
 
+def test_empty_inputs_return_before_any_device_work(lib):
+    """n = 0 (no active particles, or an empty map) is valid and returns ok
+    from the argument checks, before anything touches the device; a negative
+    size, an unknown kernel or too small a workspace is refused."""
+    from sph import _lib, core
+    wc = core.wcsph_struct(1.0, 0.01, 1000.0)
+    cfg = core.config_struct()
+    empty = _lib.Particles()
+    empty.n = 0
+    nbytes = C.c_size_t()
+    assert lib.sph_workspace_size(0, 0, C.byref(nbytes)) == 0
+    ws = _lib.Workspace()
+    ws.ptr = 256  # never dereferenced: every call below returns on the host
+    ws.bytes = nbytes.value
+    ws.n_cap = 0
+    ws.max_cells = lib.sph_default_max_cells(0)
+    dt = C.c_double(1e-4)
+    stages = (C.c_double * 16)()
+    assert lib.sph_initialize(C.byref(empty), C.byref(wc), C.byref(cfg), None) == 0
+    assert lib.sph_eos(C.byref(empty), C.byref(wc), None) == 0
+    assert lib.sph_predict(C.byref(empty), C.byref(cfg), C.byref(dt), None) == 0
+    assert lib.sph_correct(C.byref(empty), C.byref(cfg), C.byref(dt), None) == 0
+    assert lib.sph_nn_update(C.byref(empty), C.byref(cfg), C.byref(ws), None) == 0
+    assert lib.sph_compute(C.byref(empty), C.byref(wc), C.byref(cfg), C.byref(ws), None) == 0
+    assert lib.sph_run(C.byref(empty), C.byref(wc), C.byref(cfg), C.byref(ws), 5, None, None) == 0
+    assert lib.sph_run_profiled(C.byref(empty), C.byref(wc), C.byref(cfg), C.byref(ws), 5, stages, None) == 0
+    assert all(v == 0.0 for v in stages)
+    for k in (0, 1, 2):
+        assert lib.sph_kernel_eval(k, 0, None, None, None, None) == 0
+        assert lib.sph_kernel_grad(k, 0, None, None, None, None, None) == 0
+    assert lib.sph_gauss_deriv(0, None, None, None, None) == 0
+    # refused
+    assert lib.sph_kernel_eval(7, 0, None, None, None, None) == 1
+    assert lib.sph_kernel_eval(0, -1, None, None, None, None) == 1
+    assert lib.sph_kernel_eval(0, 3, None, None, None, None) == 1
+    assert lib.sph_run(C.byref(empty), C.byref(wc), C.byref(cfg), C.byref(ws), -1, None, None) == 1
+    small = _lib.Workspace()  # bytes below the layout of its own capacity
+    small.ptr, small.bytes, small.n_cap, small.max_cells = 256, 16, 0, 65536
+    assert lib.sph_compute(C.byref(empty), C.byref(wc), C.byref(cfg), C.byref(small), None) != 0
+
+
 def test_newmark_arguments_checked_on_host(lib):
     from sph import _lib
     nbytes = C.c_size_t()
