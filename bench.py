@@ -17,7 +17,8 @@ timed steps (whole job: summed over ranks; N > 1 runs independent replicas).
 
 Lines printed: one JSON object (rank 0).  ``--impl reference`` times the CPU
 reference implementation of the step (the C restatement in oracle/, OpenMP
-over all host cores) on a bounded sample of the same workload.
+over all host cores) on the same workload: ``--warmup`` untimed and
+``--steps`` timed steps.
 """
 import argparse
 import json
@@ -38,15 +39,14 @@ METRIC = "WCSPH particle-steps/s"
 UNIT = "particle-steps/s"
 PAIR_BYTES = 81     # algorithmic bytes of the pair evaluation per particle (x,y,vx,vy,rho,m,h,label in; drho,ax,ay out)
 STEP_BYTES = 385    # algorithmic bytes of one PEC step per particle (dt 32 + predict 144 + build 24 + pair 81 + correct 104)
-# DRAM bytes (read + write) per particle of one pair launch, from the ncu
-# captures summarised in profiles/ (dram__bytes_read.sum + dram__bytes_write.sum
-# of k_pair_tiles over its particle count)
-TRAFFIC_PER_PARTICLE = {("dambreak1m", "mixed"): 62.5}  # profiles/k_pair_tiles_dambreak1m.md
-# what bounds the pair kernel instead of HBM, from the same captures
-LIMITER = {"mixed": "instruction issue: 70.6% of cycles issue, DRAM 4.2% of peak "
-                    "(profiles/k_pair_tiles_dambreak1m.md)",
-           "fp64": "FP64 pipe: busy 86.5% of active cycles, DRAM 0.5% of peak "
-                   "(profiles/k_pair_fp64_dambreak1m.md)"}
+# DRAM bytes (read + write) per particle of one pair launch: not measurable
+# without a profiler, so taken from an ncu capture of the same kernel on the
+# same workload (dram__bytes_read.sum + dram__bytes_write.sum over the
+# particle count), with the capture's date
+TRAFFIC_FROM_PROFILE = {("dambreak1m", "mixed"): (62.5, "2026-12-04, k_pair_tiles, one launch")}
+# what bounds the pair kernel instead of HBM, read off the same captures
+LIMITER_FROM_PROFILE = {"mixed": "instruction issue: 70.6% of cycles issue, DRAM 4.2% of peak (ncu, 2026-12-04)",
+                        "fp64": "FP64 pipe: busy 86.5% of active cycles, DRAM 0.5% of peak (ncu, 2026-12-04)"}
 
 
 def workload(name):
@@ -73,21 +73,6 @@ def workload(name):
         return dict(pa=pa, height=2.0, r0=0.025, h=0.0325, kernel=0, gamma_c=0.3, setup=True,
                     desc="1x2 m column at dx=0.025 (3200 fluid) in a 4x3 m tank, cubic, PEC, Courant 0.3")
     raise SystemExit("unknown workload " + name)
-
-
-def sample(wl_name, wl, size):
-    """A smaller case of the same recipe for the CPU timings: a size x size
-    lattice, or a dam break whose column is size x 2 size particles at the
-    workload's dx (same H scaling: H = column height).  Returns (particles,
-    height, description)."""
-    from sph import scenarios as S
-    if wl_name.startswith("lattice"):
-        return (S.jittered_lattice(size, size, 0.01, seed=0), wl["height"],
-                "%dx%d lattice of the same recipe" % (size, size))
-    dx = wl["r0"]
-    w, h = size * dx, 2 * size * dx
-    return (S.dam_break(w, h, dx, 4.0 * w, 1.5 * h), h,
-            "dam break of the same recipe, %dx%d fluid column" % (size, 2 * size))
 
 
 def oracle_particles(wl, pa, height):
@@ -187,17 +172,6 @@ def prepare(wl, precision):
     return dp, wc, cfg, ws
 
 
-def time_steps(core, dp, wc, cfg, ws, k):
-    import torch
-    s, e = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
-    torch.cuda.synchronize()
-    s.record()
-    core.run(dp, wc, cfg, ws, k)
-    e.record()
-    torch.cuda.synchronize()
-    return s.elapsed_time(e) / 1e3
-
-
 GRAPH_STEPS = 100  # steps per captured CUDA graph in the timed region
 
 
@@ -295,40 +269,54 @@ def e2e_steps(core, dp, wc, cfg, ws, k, pa, result=None):
     return s.elapsed_time(e) / 1e3, h2d, d2h
 
 
-def cpu_baseline(wl_name, wl, budget_s=10.0, budget_1t_s=4.0):
-    """The oracle (C restatement of the reference's step) on a bounded sample
-    of the same recipe, PEC steps, all host threads; then the same sample on
-    one thread, as the reference's numba loop runs (its prange has no
-    parallel=True)."""
+def arm_config(wl_name, wl):
+    """The workload as both arms report it (identical dicts, so that the two
+    lines name the same configuration)."""
+    pa = wl["pa"]
+    return {"workload": wl_name + ": " + wl["desc"], "n_particles": int(len(pa)),
+            "n_fluid": int(np.sum(pa["label"] == 0)), "integrator": "PEC"}
+
+
+def cpu_baseline(wl_name, wl, steps=3, budget_1t_s=8.0):
+    """The oracle (C restatement of the reference's step) on the full
+    workload: `steps` PEC steps on all host threads; then one thread, as the
+    reference's numba loop runs (its prange has no parallel=True), on a
+    bounded sample of one evaluation: _loop's pass over the first fluid
+    particles (about budget_1t_s seconds of work), because a whole
+    single-threaded step of the 1M workload takes minutes."""
     import oracle
     threads = oracle.max_threads()
-    pa, height, what = sample(wl_name, wl, 200 if wl_name.startswith("lattice") else 141)
-    P, par = oracle_particles(wl, pa, height)
+    P, par = oracle_particles(wl, wl["pa"], wl["height"])
     nn = oracle.NN(2.0)
     nf = int(np.sum(P.label == 0))
-
-    def timed(nthreads, budget, warm):
-        if warm:
-            oracle.run(par, nn, P, 1, h_fixed=wl["h"], gamma_c=wl["gamma_c"], nthreads=nthreads)
-        steps, t0 = 0, time.perf_counter()
-        while True:
-            oracle.run(par, nn, P, 1, h_fixed=wl["h"], gamma_c=wl["gamma_c"], nthreads=nthreads)
-            steps += 1
-            el = time.perf_counter() - t0
-            if el >= budget or steps >= 200:
-                return nf * steps / el, steps
-
-    v, steps = timed(threads, budget_s, True)
-    v1, steps1 = timed(1, budget_1t_s, False)  # the threaded steps warmed the sample
-    return {"value": v, "unit": UNIT, "cores": threads, "kind": "port",
-            "sample": "%s (%d fluid), %d PEC steps, OpenMP over particles" % (what, nf, steps),
-            "single_thread": {"value": v1, "unit": UNIT, "cores": 1, "steps": steps1}}
+    t0 = time.perf_counter()
+    oracle.run(par, nn, P, steps, h_fixed=wl["h"], gamma_c=wl["gamma_c"], nthreads=threads)
+    el = time.perf_counter() - t0
+    # single thread: the table of the current state, then a timed probe and
+    # a timed sample sized from it
+    nn.update(P.x, P.y, P.h)
+    fl = np.flatnonzero(P.label == 0)
+    probe = min(len(fl), 512)
+    t0 = time.perf_counter()
+    oracle.loop_range(par, nn, P, int(fl[0]), int(fl[probe - 1]) + 1)
+    per = max((time.perf_counter() - t0) / probe, 1e-9)
+    cnt = int(min(len(fl), max(probe, budget_1t_s / per)))
+    t0 = time.perf_counter()
+    oracle.loop_range(par, nn, P, int(fl[0]), int(fl[cnt - 1]) + 1)
+    el1 = time.perf_counter() - t0
+    return {"value": nf * steps / el, "unit": UNIT, "cores": threads, "kind": "port",
+            "sample": "the full workload (%d fluid), %d PEC steps, OpenMP over particles" % (nf, steps),
+            "single_thread": {"value": cnt / el1, "unit": UNIT, "cores": 1,
+                              "sample": "the pair loop (_loop) of one evaluation over %d of the %d fluid "
+                                        "particles, one thread (neighbour build and integrator, O(N) "
+                                        "and a small share of a step, not included)" % (cnt, nf)}}
 
 
 def run_reference(args, wl_name):
     """--impl reference: the CPU reference implementation of the step (the C
-    restatement in oracle/, all host threads) on a bounded sample of the same
-    workload, sized so that warmup + steps take about a minute."""
+    restatement of the reference's algorithm in oracle/, all host threads)
+    on the same workload and configuration as the GPU arm: `warmup`
+    untimed steps, then `steps` timed ones."""
     import oracle
     rank = int(os.environ.get("RANK", "0"))
     if rank != 0:
@@ -336,38 +324,20 @@ def run_reference(args, wl_name):
     oracle.build()
     wl = workload(wl_name)
     threads = oracle.max_threads()
-    # start small and grow: the reference's cost per step grows faster than
-    # linearly for dam breaks (walls have h = 0, so its cells are 1 m wide)
-    lattice = wl_name.startswith("lattice")
-    size, size_max = (100, 1000) if lattice else (60, 707)
-    total = args.steps + args.warmup
-    target = 60.0 / total
+    P, par = oracle_particles(wl, wl["pa"], wl["height"])
     nn = oracle.NN(2.0)
-    for _ in range(5):
-        pa, height, what = sample(wl_name, wl, size)
-        P, par = oracle_particles(wl, pa, height)
-        t0 = time.perf_counter()
-        oracle.run(par, nn, P, 1, h_fixed=wl["h"], gamma_c=wl["gamma_c"], nthreads=threads)
-        per_step = time.perf_counter() - t0
-        ratio = target / max(per_step, 1e-9)
-        if 0.5 <= ratio <= 2.0:
-            break
-        new = int(min(size_max, max(20, size * ratio ** (0.5 if lattice else 0.25))))
-        if new == size:
-            break
-        size = new
-    for _ in range(args.warmup):
-        oracle.run(par, nn, P, 1, h_fixed=wl["h"], gamma_c=wl["gamma_c"], nthreads=threads)
+    nf = int(np.sum(P.label == 0))
+    oracle.run(par, nn, P, args.warmup, h_fixed=wl["h"], gamma_c=wl["gamma_c"], nthreads=threads)
     t0 = time.perf_counter()
     oracle.run(par, nn, P, args.steps, h_fixed=wl["h"], gamma_c=wl["gamma_c"], nthreads=threads)
     el = time.perf_counter() - t0
-    nf = int(np.sum(P.label == 0))
     v = nf * args.steps / el
-    smp = "%s: %s (%d fluid), PEC steps, OpenMP over particles" % (wl_name, what, nf)
+    smp = "the full workload (%d fluid), %d timed PEC steps after %d untimed, OpenMP over particles" % (
+        nf, args.steps, args.warmup)
     out = {"impl": "reference", "metric": METRIC, "value": v, "unit": UNIT, "n_gpus": args.gpus,
            "steps": args.steps, "warmup": args.warmup, "ms_per_step": el / args.steps * 1e3,
            "higher_is_better": True, "scaling": "weak", "vs_baseline": None, "dtype": "f64", "data": "synthetic",
-           "config": {"workload": wl_name + ": " + wl["desc"], "sample": smp},
+           "config": arm_config(wl_name, wl),
            "cpu_baseline": {"value": v, "unit": UNIT, "cores": threads, "kind": "port", "sample": smp},
            "e2e": {"value": v, "unit": UNIT, "h2d_bytes_per_step": 0, "d2h_bytes_per_step": 0}}
     print(json.dumps(out))
@@ -633,11 +603,11 @@ def main():
            "scaling": "weak", "vs_baseline": None,
            "dtype": "f32 pair / f64 state" if args.precision == "mixed" else "f64",
            "data": "synthetic",
-           "config": {"workload": args.workload + ": " + wl["desc"], "n_particles": int(dp.n), "n_fluid": nfluid,
-                      "precision": args.precision, "integrator": "PEC",
-                      "l2": "inputs larger than L2 (state + records ~%.0f MB per step)"
-                            % ((dp.n * (19 * 8 + 1) + ws.buf.numel()) / 1e6),
-                      "parallelism": "replicas" if world > 1 else "single GPU"},
+           "config": arm_config(args.workload, wl),
+           "precision": args.precision,
+           "l2": "inputs larger than L2 (state + records ~%.0f MB per step)"
+                 % ((dp.n * (19 * 8 + 1) + ws.buf.numel()) / 1e6),
+           "parallelism": "replicas" if world > 1 else "single GPU",
            "clocks": clk, "gpu_launches": launches,
            "timing": "CUDA events around %d replays of a %d-step CUDA graph of sph_run%s"
                      % (reps, gsteps, " and one of %d steps" % rem if rem else "")}
@@ -650,25 +620,31 @@ def main():
         step_s = sum(stages.values()) / 1e3 / kprof
         ach = dp.n * PAIR_BYTES / pair_s / 1e9
         out["stages_ms_per_step"] = {k: v / kprof for k, v in stages.items()}
-        traffic = TRAFFIC_PER_PARTICLE.get((args.workload, args.precision))
+        traffic = TRAFFIC_FROM_PROFILE.get((args.workload, args.precision))
         out["roofline"] = {"bound": "hbm",
                            "kernel": "k_pair_tiles + k_pair_list" if args.precision == "mixed" else "k_pair (FP64)",
                            "achieved": ach, "peak": hbm, "unit": "GB/s", "frac": ach / hbm,
-                           "peak_kind": peak_kind, "traffic": traffic * dp.n if traffic else None,
+                           "peak_kind": peak_kind, "traffic": traffic[0] * dp.n if traffic else None,
+                           "traffic_source": ("from_profile: ncu dram__bytes_read.sum + dram__bytes_write.sum, "
+                                              + traffic[1]) if traffic else None,
                            "algorithmic_bytes_per_launch": dp.n * PAIR_BYTES,
                            "step_achieved_gbs": dp.n * STEP_BYTES / step_s / 1e9,
-                           "limiter": LIMITER.get(args.precision)}
-        # the GPU's own FP64 path on the same workload
+                           "limiter_from_profile": LIMITER_FROM_PROFILE.get(args.precision)}
+        # the GPU's own FP64 path on the same workload, timed the same way
+        # (replays of a captured CUDA graph of sph_run)
         if args.precision == "mixed":
             dp64, wc64, cfg64, ws64 = prepare(wl, "fp64")
             core.run(dp64, wc64, cfg64, ws64, 3)
-            k64 = max(3, min(args.steps // 10, 200))
-            el64 = time_steps(core, dp64, wc64, cfg64, ws64, k64)
+            k64 = max(20, min(args.steps, 100))
+            g64 = make_graphs(core, dp64, wc64, cfg64, ws64, k64)
+            ws64.check()
+            el64 = time_graph_steps(g64)
             ws64.check()
             v64 = nfluid * k64 / el64
             out["fp64"] = {"value": v64, "steps": k64, "ms_per_step": el64 / k64 * 1e3,
+                           "timing": "CUDA events around a graph replay of %d steps of sph_run" % k64,
                            "mixed_over_fp64": value / world / v64}
-            del dp64, ws64
+            del g64, dp64, ws64
         # end to end through host buffers
         ke = max(3, min(args.steps, 100))
         el_e, h2d, d2h = e2e_steps(core, dp, wc, cfg, ws, ke, wl["pa"])

@@ -249,8 +249,10 @@ int sph_compute(sph_particles_t *pa, const sph_wcsph_t *w, const sph_config_t *c
  *    is coarsened beyond that (results unchanged, search slower).
  *  - Every GPU that loads the library holds the SPH_STATIC_WS_BYTES array
  *    until the process exits.  The call itself allocates nothing.
- *  - The first call on a device looks up the array's device address (once per
- *    device); make that first call before any stream capture.
+ *  - The first call in a CUDA context looks up the array's device address
+ *    there (once per context: the device's primary context, a caller's own
+ *    context, and the new primary context after cudaDeviceReset each count as
+ *    one); make that first call before any stream capture in the context.
  *  - All calls share the one array: calls whose work overlaps on the GPU (on
  *    different streams, or from different host threads without ordering) race
  *    on it.  Order them on one stream.

@@ -21,7 +21,6 @@ void launch_bt_timestep(const StepArgs &a, const WsPtrs &w, const BatchPtrs &B, 
                         cudaStream_t st);
 void launch_bt_dt_finish(const WsPtrs &w, const BatchPtrs &B, int slot, double *dt_hist, cudaStream_t st);
 void launch_bt_correct(const StepArgs &a, const BatchPtrs &B, const sph_config_t &cfg, int slot, cudaStream_t st);
-void init_workspace(const WsPtrs &w, cudaStream_t st);
 
 // per-instance tables after the regular workspace
 struct BatchLayout {
@@ -166,7 +165,7 @@ int sph_batch_setup(const sph_workspace_t *ws, int64_t n_inst, const int64_t *of
   }
   cudaStream_t st = (cudaStream_t)stream;
   const BatchPtrs B = batch_ptrs(ws, (int)n_inst);
-  init_workspace(ws_ptrs(ws), st);
+  if (init_workspace(ws_ptrs(ws), st) != cudaSuccess) return SPH_ERR_CUDA;
   if (cudaMemcpyAsync(B.ip, ip.data(), ip.size() * sizeof(InstParams), cudaMemcpyHostToDevice, st) != cudaSuccess)
     return SPH_ERR_CUDA;
   k_bt_inst<<<nblocks(N), kBlock, 0, st>>>(B, N);

@@ -84,12 +84,15 @@ __global__ void k_ctrl_init(DevCtrl *c) {
   c->initialised = 0x53504821u;
 }
 
-// zero cell counters, zero grid, control block at its identities
-void init_workspace(const WsPtrs &w, cudaStream_t st) {
-  cudaMemsetAsync(w.counts, 0, (size_t)(w.max_cells + 1) * 4, st);
-  cudaMemsetAsync(w.scan_part, 0, (size_t)w.n_parts * 4, st);
-  cudaMemsetAsync(w.grid, 0, sizeof(DevGrid), st);
+// zero cell counters, zero grid, control block at its identities; returns
+// the first error of the four stream operations
+cudaError_t init_workspace(const WsPtrs &w, cudaStream_t st) {
+  cudaError_t e = cudaMemsetAsync(w.counts, 0, (size_t)(w.max_cells + 1) * 4, st);
+  if (e == cudaSuccess) e = cudaMemsetAsync(w.scan_part, 0, (size_t)w.n_parts * 4, st);
+  if (e == cudaSuccess) e = cudaMemsetAsync(w.grid, 0, sizeof(DevGrid), st);
+  if (e != cudaSuccess) return e;
   k_ctrl_init<<<1, 32, 0, st>>>(w.ctrl);
+  return cudaGetLastError();
 }
 
 // Self-test of the staging primitives of the pair tile kernel: a 64-byte
@@ -111,7 +114,7 @@ __global__ void k_selftest_staging(const float4 *src, unsigned int *result) {
     mbar_arrive_expect_tx(&bar[1], 16u);  // nothing is sent
   }
   bool ok0 = mbar_wait_bounded(&bar[0], 0u);
-  if (!ok0) mbar_wait_bounded(&bar[0], 0u);  // never leave with the copy in flight
+  if (!ok0) mbar_wait_bounded(&bar[0], 0u, kMbarDrainLimit);  // drain before leaving (bounded)
   const bool ok1 = mbar_wait_bounded(&bar[1], 0u, 256);
   __syncthreads();
   if (threadIdx.x == 0) {
@@ -187,8 +190,7 @@ int sph_workspace_init(sph_workspace_t *ws, sph_stream_t stream) {
   int e = ws_ok(ws, 0);
   if (e) return e;
   cudaStream_t st = (cudaStream_t)stream;
-  init_workspace(ws_ptrs(ws), st);
-  if (check_launch()) return SPH_ERR_CUDA;
+  if (init_workspace(ws_ptrs(ws), st) != cudaSuccess) return SPH_ERR_CUDA;
   return cudaStreamSynchronize(st) == cudaSuccess ? SPH_OK : SPH_ERR_CUDA;
 }
 

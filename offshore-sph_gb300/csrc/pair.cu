@@ -784,7 +784,7 @@ __device__ __forceinline__ unsigned long long tile_process(const StepArgs &a, co
   const bool ok = mbar_wait_bounded(sync.bar, parity);
   if (__syncthreads_or(!ok)) {  // the copies did not land: flag, drain, stop this block
     if (tid == 0) atomicOr(&ctrl->status, (unsigned)SPH_STATUS_STAGING_TIMEOUT);
-    mbar_wait_bounded(sync.bar, parity);
+    mbar_wait_bounded(sync.bar, parity, kMbarDrainLimit);
     sync.abort = true;
     __syncthreads();
     return ea;

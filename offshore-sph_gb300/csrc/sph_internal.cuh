@@ -319,6 +319,11 @@ struct WsPtrs {
 
 WsPtrs ws_ptrs(const sph_workspace_t *ws);
 
+// A workspace's initial state: zero cell counters, scan-tile totals and grid,
+// the control block at its identities (capi.cu); asynchronous on st, returns
+// the first CUDA error.
+cudaError_t init_workspace(const WsPtrs &w, cudaStream_t st);
+
 // ---------------------------------------------------------------------------
 // Small device helpers
 // ---------------------------------------------------------------------------
@@ -432,7 +437,16 @@ __device__ __forceinline__ bool mbar_try_wait(unsigned long long *bar, uint32_t 
 }
 
 // Bounded wait for phase `parity` of bar; false when the limit ran out.
+// kMbarWaitLimit polls take milliseconds, far longer than any staging copy of
+// a few tens of KB.  After a wait ran out, a block drains with the 16x longer
+// kMbarDrainLimit before it leaves, so that it does not exit with copies
+// still writing into its shared memory.  Should the drain run out as well,
+// the block leaves anyway (every wait stays bounded): the copies in flight
+// can then only write shared memory that a later block of the same launch
+// may reuse, and that launch has already set SPH_STATUS_STAGING_TIMEOUT,
+// which marks the whole evaluation as failed.
 constexpr int kMbarWaitLimit = 1 << 22;
+constexpr int kMbarDrainLimit = 1 << 26;
 __device__ __forceinline__ bool mbar_wait_bounded(unsigned long long *bar, uint32_t parity,
                                                   int limit = kMbarWaitLimit) {
   for (int it = 0; it < limit; it++)

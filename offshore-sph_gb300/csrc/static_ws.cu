@@ -11,10 +11,17 @@
 // into the library.
 //
 // The scratch is one file-scope __device__ array of SPH_STATIC_WS_BYTES.  Every
-// GPU that loads the library holds that array until the process exits.  Its
-// device address is looked up once per device with cudaGetSymbolAddress and
-// cached; the host-side symbol itself is only a stand-in and is never passed
-// to a kernel.
+// GPU that loads the library holds that array until the process exits.  Host
+// code never passes the array's host-side symbol to a kernel: the symbol is a
+// stand-in, not a device address.  The device address comes from
+// cudaGetSymbolAddress, called with the device current, once per CUDA
+// context, and is cached under the context's unique id (cuCtxGetId).  A
+// context is what owns the loaded module: after cudaDeviceReset, or in a
+// caller's own (non-primary) context, the module is loaded again at another
+// address, and the new context's id differs from every earlier one, so the
+// first call there looks the address up afresh instead of reusing a stale one.
+#include <cuda.h>
+
 #include <mutex>
 
 #include "sph_internal.cuh"
@@ -22,36 +29,77 @@
 namespace {
 
 constexpr size_t kStaticWsBytes = SPH_STATIC_WS_BYTES;
-constexpr int kMaxDevices = 64;
+constexpr int kMaxContexts = 64;
 
 __device__ __align__(256) unsigned char g_static_ws[kStaticWsBytes];
 
-std::mutex g_mutex;
-void *g_static_ptr[kMaxDevices];
+// driver entry points, resolved once through the runtime (the library does
+// not link libcuda itself)
+typedef CUresult (*ctx_get_current_fn)(CUcontext *);
+typedef CUresult (*ctx_get_id_fn)(CUcontext, unsigned long long *);
+ctx_get_current_fn g_ctx_get_current = nullptr;
+ctx_get_id_fn g_ctx_get_id = nullptr;
+std::once_flag g_entry_once;
 
-// Device address of g_static_ws on the current device (first use on a device
-// resolves and caches it).
-int static_ws_address(void **out) {
-  int dev = -1;
-  if (cudaGetDevice(&dev) != cudaSuccess) return SPH_ERR_CUDA;
-  if (dev < 0 || dev >= kMaxDevices) return SPH_ERR_INVALID_ARGUMENT;
-  std::lock_guard<std::mutex> lock(g_mutex);
-  if (!g_static_ptr[dev]) {
-    void *p = nullptr;
-    if (cudaGetSymbolAddress(&p, g_static_ws) != cudaSuccess || !p) return SPH_ERR_CUDA;
-    g_static_ptr[dev] = p;
-  }
-  *out = g_static_ptr[dev];
-  return SPH_OK;
+void resolve_entry_points() {
+  void *f = nullptr;
+  cudaDriverEntryPointQueryResult q;
+  if (cudaGetDriverEntryPointByVersion("cuCtxGetCurrent", &f, 12000, cudaEnableDefault, &q) == cudaSuccess &&
+      q == cudaDriverEntryPointSuccess)
+    g_ctx_get_current = (ctx_get_current_fn)f;
+  f = nullptr;
+  if (cudaGetDriverEntryPointByVersion("cuCtxGetId", &f, 12000, cudaEnableDefault, &q) == cudaSuccess &&
+      q == cudaDriverEntryPointSuccess)
+    g_ctx_get_id = (ctx_get_id_fn)f;
 }
 
-// The array keeps whatever the previous call left: return the control block
-// (reductions, status word, counters) to its initial state.
-__global__ void k_static_ctrl_init(sph::DevCtrl *c) {
-  if (threadIdx.x != 0) return;
-  memset(c, 0, sizeof(sph::DevCtrl));
-  c->xmin = c->ymin = c->hmin_all = c->ts_hmin = c->pd_hmin = sph::kEncMinId;
-  c->xmax = c->ymax = c->hmax_new = c->ts_cmax = c->ts_a2max = c->pd_a2max = sph::kEncMaxId;
+// unique id of the current context (0 when none is current or the driver
+// does not say)
+unsigned long long current_context_id() {
+  if (!g_ctx_get_current || !g_ctx_get_id) return 0;
+  CUcontext ctx = nullptr;
+  unsigned long long id = 0;
+  if (g_ctx_get_current(&ctx) != CUDA_SUCCESS || !ctx) return 0;
+  if (g_ctx_get_id(ctx, &id) != CUDA_SUCCESS) return 0;
+  return id;
+}
+
+struct CachedAddress {
+  unsigned long long ctx_id;
+  void *ptr;
+};
+std::mutex g_mutex;
+CachedAddress g_cache[kMaxContexts];
+int g_cache_used = 0, g_cache_next = 0;
+
+// Device address of g_static_ws in the current context; the first call in a
+// context resolves it with cudaGetSymbolAddress (which also makes the
+// device's primary context current when no context is) and caches it.
+int static_ws_address(void **out) {
+  std::call_once(g_entry_once, resolve_entry_points);
+  int dev = -1;
+  if (cudaGetDevice(&dev) != cudaSuccess || dev < 0) return SPH_ERR_CUDA;
+  std::lock_guard<std::mutex> lock(g_mutex);
+  const unsigned long long id = current_context_id();
+  if (id) {
+    for (int k = 0; k < g_cache_used; k++)
+      if (g_cache[k].ctx_id == id) {
+        *out = g_cache[k].ptr;
+        return SPH_OK;
+      }
+  }
+  void *p = nullptr;
+  if (cudaGetSymbolAddress(&p, g_static_ws) != cudaSuccess || !p) return SPH_ERR_CUDA;
+  const unsigned long long id_after = id ? id : current_context_id();
+  if (id_after) {  // remember it; the oldest entry gives way when the table is full
+    const int slot = g_cache_next;
+    g_cache_next = (g_cache_next + 1) % kMaxContexts;
+    if (g_cache_used < kMaxContexts) g_cache_used++;
+    g_cache[slot].ctx_id = id_after;
+    g_cache[slot].ptr = p;
+  }
+  *out = p;
+  return SPH_OK;
 }
 
 }  // namespace
@@ -69,11 +117,9 @@ extern "C" int sph_compute_static(sph_particles_t *pa, const sph_wcsph_t *w, con
   if (e) return e;
   cudaStream_t st = (cudaStream_t)stream;
   sph::WsPtrs p = sph::ws_ptrs(&ws);
-  // counters and control block start from zero on every call
-  if (cudaMemsetAsync(p.counts, 0, (size_t)(ws.max_cells + 1) * 4, st) != cudaSuccess) return SPH_ERR_CUDA;
-  if (cudaMemsetAsync(p.scan_part, 0, (size_t)p.n_parts * 4, st) != cudaSuccess) return SPH_ERR_CUDA;
-  k_static_ctrl_init<<<1, 32, 0, st>>>(p.ctrl);
-  if (cudaGetLastError() != cudaSuccess) return SPH_ERR_CUDA;
+  // the array keeps what the previous call left: counters, grid and control
+  // block (reductions, status word) return to a fresh workspace's state
+  if (sph::init_workspace(p, st) != cudaSuccess) return SPH_ERR_CUDA;
   e = sph_compute(pa, w, cfg, &ws, stream);
   if (e) return e;
   if (status &&

@@ -71,6 +71,7 @@ EXPORTS = ("sph_abi_version", "sph_workspace_size", "sph_default_max_cells", "sp
            "sph_newmark_work_size", "sph_newmark_acceleration", "sph_selftest_staging")
 SPH_ERR_STATIC_LIMIT = 5
 STATIC_MAX_PARTICLES = 32768
+STATIC_MAX_CELLS = 131072
 
 STAGES = ("timestep", "predict", "build", "records", "pair", "correct")
 

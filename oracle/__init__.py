@@ -65,6 +65,9 @@ def lib():
         L.or_nn_near.argtypes = [C.c_void_p, C.c_double, C.c_double, C.c_double, dp, dp, dp,
                                  i64p, dp, dp, dp, C.c_int64]
         L.or_nn_all.argtypes = [C.c_void_p, C.c_int64, dp, dp, dp, C.c_void_p, C.c_int, i64p, C.c_void_p]
+        L.or_nn_all_mt.argtypes = [C.c_void_p, C.c_int64, dp, dp, dp, C.c_void_p, C.c_int, i64p, C.c_void_p,
+                                   C.c_int, C.c_int]
+        L.or_loop_range.argtypes = [C.c_void_p, C.c_void_p, C.c_void_p, C.c_int64, C.c_int64]
         L.or_loop.argtypes = [C.c_void_p, C.c_void_p, C.c_void_p, C.c_int]
         L.or_compute.argtypes = [C.c_void_p, C.c_void_p, C.c_void_p, C.c_double, C.c_int]
         L.or_run.argtypes = [C.c_void_p, C.c_void_p, C.c_void_p, C.c_void_p, C.c_int64, C.c_void_p]
@@ -104,7 +107,7 @@ class WCSPHParams(C.Structure):
     _fields_ = [(k, C.c_double) for k in
                 ["gamma", "B", "rho0", "Pb", "co", "alpha", "beta", "epsilon", "r0", "D", "p1", "p2"]] + \
                [("use_xsph", C.c_int32), ("use_summation_density", C.c_int32),
-                ("kernel", C.c_int32), ("pad", C.c_int32)]
+                ("kernel", C.c_int32), ("sum_order", C.c_int32)]
 
 
 class StepOpt(C.Structure):
@@ -118,14 +121,18 @@ class _Particles(C.Structure):
 
 
 def wcsph_params(height, r0, rho0, use_xsph=False, Pb=0.0, use_summation_density=False, kernel=0,
-                 alpha=0.01, beta=0.0):
-    """The constants WCSPH.__init__ derives (WCSPH.py:35-79, TaitEOS.py:33-44)."""
+                 alpha=0.01, beta=0.0, sum_order=0):
+    """The constants WCSPH.__init__ derives (WCSPH.py:35-79, TaitEOS.py:33-44).
+    sum_order = 1 sums every particle's neighbours in reverse order: not a
+    reference setting, but a control run that differs from the reference only
+    by round-off, to size how round-off differences grow along a trajectory."""
     co = 10.0 * np.sqrt(2 * 9.81 * height)
     gamma = 7.0
     B = co * co * rho0 / gamma
     return WCSPHParams(gamma=gamma, B=B, rho0=rho0, Pb=Pb, co=co, alpha=alpha, beta=beta, epsilon=0.5,
                        r0=r0, D=5 * 9.81 * height, p1=4.0, p2=2.0, use_xsph=int(use_xsph),
-                       use_summation_density=int(use_summation_density), kernel=int(kernel))
+                       use_summation_density=int(use_summation_density), kernel=int(kernel),
+                       sum_order=int(sum_order))
 
 
 class Particles:
@@ -199,8 +206,12 @@ class NN:
                              _dp(hij), _dp(q), _dp(r), cap)
         return hij[:n], q[:n], r[:n], idx[:n]
 
-    def all(self, label=None, label_filter=-1):
-        """CSR neighbour lists near(i) for all i (label_filter -1) or one label."""
+    def all(self, label=None, label_filter=-1, nthreads=1, sorted_lists=False):
+        """CSR neighbour lists near(i) for all i (label_filter -1) or one label,
+        each in the reference's traversal order (ascending index order with
+        sorted_lists).  nthreads > 1 runs the queries on OpenMP threads."""
+        if nthreads > 1 or sorted_lists:
+            return self._all_mt(label, label_filter, nthreads, sorted_lists)
         n = len(self._x)
         lab = np.ascontiguousarray(label, dtype=np.int8) if label is not None else np.zeros(n, np.int8)
         off = np.zeros(n + 1, dtype=np.int64)
@@ -209,6 +220,18 @@ class NN:
         idx = np.zeros(max(int(off[-1]), 1), dtype=np.int64)
         lib().or_nn_all(self.h, n, _dp(self._x), _dp(self._y), _dp(self._hh), lab.ctypes.data,
                         label_filter, _i64p(off), idx.ctypes.data)
+        return off, idx[:int(off[-1])]
+
+    def _all_mt(self, label, label_filter, nthreads, sorted_lists):
+        n = len(self._x)
+        lab = np.ascontiguousarray(label, dtype=np.int8) if label is not None else np.zeros(n, np.int8)
+        off = np.zeros(n + 1, dtype=np.int64)
+        args = (self.h, n, _dp(self._x), _dp(self._y), _dp(self._hh), lab.ctypes.data, label_filter, _i64p(off))
+        if lib().or_nn_all_mt(*args, None, max(1, nthreads), int(sorted_lists)):
+            raise RuntimeError("oracle neighbour export failed")
+        idx = np.zeros(max(int(off[-1]), 1), dtype=np.int64)
+        if lib().or_nn_all_mt(*args, idx.ctypes.data, max(1, nthreads), int(sorted_lists)):
+            raise RuntimeError("oracle neighbour export failed")
         return off, idx[:int(off[-1])]
 
 
@@ -364,6 +387,14 @@ def probe_density(nn, P, x, y, h_search, h_kernel, kernel, rho0, B, gamma):
 def loop(params, nn, P, nthreads=1):
     s = P.cstruct()
     return lib().or_loop(C.byref(params), nn.h, C.byref(s), nthreads)
+
+
+def loop_range(params, nn, P, i0, i1):
+    """_loop's regular pass for the fluid particles in [i0, i1) on one thread
+    (after the EOS pass over all particles), on the table of the last
+    nn.update: a bounded sample of one evaluation, for timing."""
+    s = P.cstruct()
+    return lib().or_loop_range(C.byref(params), nn.h, C.byref(s), int(i0), int(i1))
 
 
 def compute(params, nn, P, h_fixed, nthreads=1):

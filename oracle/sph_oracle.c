@@ -450,15 +450,80 @@ int or_nn_all(void *p, int64_t n, const double *x, const double *y, const double
   return OR_OK;
 }
 
+static int cmp_i64(const void *a, const void *b) {
+  const int64_t x = *(const int64_t *)a, y = *(const int64_t *)b;
+  return x < y ? -1 : (x > y ? 1 : 0);
+}
+
+/* or_nn_all over nthreads OpenMP threads (the same lists; each particle's
+ * query is independent).  sorted != 0 writes every list in ascending index
+ * order instead of the reference's traversal order, which makes set
+ * comparisons of large cases a plain array comparison. */
+int or_nn_all_mt(void *p, int64_t n, const double *x, const double *y, const double *h, const int8_t *label,
+                 int label_filter, int64_t *offsets, int64_t *idx, int nthreads, int sorted) {
+  or_nn *nn = (or_nn *)p;
+  int err = 0;
+  if (nthreads < 1) nthreads = 1;
+  if (!idx) {
+#pragma omp parallel num_threads(nthreads) reduction(| : err)
+    {
+      nbuf b = {0};
+#pragma omp for schedule(dynamic, 256)
+      for (int64_t i = 0; i < n; i++) {
+        int64_t cnt = 0;
+        if (label_filter < 0 || label[i] == label_filter) {
+          if (near_pos(nn, x[i], y[i], h[i], x, y, h, &b)) err |= 1;
+          cnt = b.n;
+        }
+        offsets[i + 1] = cnt;
+      }
+      nbuf_free(&b);
+    }
+    offsets[0] = 0;
+    for (int64_t i = 0; i < n; i++) offsets[i + 1] += offsets[i];
+    return err ? OR_ERR_ALLOC : OR_OK;
+  }
+#pragma omp parallel num_threads(nthreads) reduction(| : err)
+  {
+    nbuf b = {0};
+#pragma omp for schedule(dynamic, 256)
+    for (int64_t i = 0; i < n; i++) {
+      if (!(label_filter < 0 || label[i] == label_filter)) continue;
+      if (near_pos(nn, x[i], y[i], h[i], x, y, h, &b)) { err |= 1; continue; }
+      int64_t *dst = idx + offsets[i];
+      const int64_t cnt = offsets[i + 1] - offsets[i];
+      if (b.n != cnt) { err |= 2; continue; }
+      for (int64_t k = 0; k < b.n; k++) dst[k] = b.idx[k];
+      if (sorted) qsort(dst, (size_t)cnt, sizeof(int64_t), cmp_i64);
+    }
+    nbuf_free(&b);
+  }
+  return err ? OR_ERR_ALLOC : OR_OK;
+}
+
 /* ------------------------------------------------------------------------ */
 /* The derivative loop (src/Tools/SolverTools.py:120-175)                    */
 /* ------------------------------------------------------------------------ */
 
-/* WCSPH constants and switches (src/Methods/WCSPH.py:35-79) */
+/* WCSPH constants and switches (src/Methods/WCSPH.py:35-79).  sum_order is
+ * not a reference setting: 0 sums each particle's neighbours in the
+ * reference's order; 1 sums them in reverse, a control run whose only
+ * difference is round-off, used to size how fast round-off differences grow
+ * along a trajectory. */
 typedef struct {
   double gamma, B, rho0, Pb, co, alpha, beta, epsilon, r0, D, p1, p2;
-  int32_t use_xsph, use_summation_density, kernel, pad;
+  int32_t use_xsph, use_summation_density, kernel, sum_order;
 } or_wcsph;
+
+/* reverse the order of a neighbour buffer (the sum_order = 1 control) */
+static void nbuf_reverse(nbuf *b) {
+  for (int64_t a = 0, z = b->n - 1; a < z; a++, z--) {
+    int64_t ti = b->idx[a]; b->idx[a] = b->idx[z]; b->idx[z] = ti;
+    double t = b->hij[a]; b->hij[a] = b->hij[z]; b->hij[z] = t;
+    t = b->q[a]; b->q[a] = b->q[z]; b->q[z] = t;
+    t = b->r[a]; b->r[a] = b->r[z]; b->r[z] = t;
+  }
+}
 
 /* SOA particle view; the arrays are the particle_dtype fields
  * (src/Common.py:26-57) of the active particles, in their order. */
@@ -474,6 +539,7 @@ typedef struct {
 static int loop_one(const or_wcsph *w, const or_nn *nn, or_particles *P, int64_t i, nbuf *b, or_comp **cbuf,
                     int64_t *ccap) {
   if (near_pos(nn, P->x[i], P->y[i], P->h[i], P->x, P->y, P->h, b)) return -1;
+  if (w->sum_order == 1) nbuf_reverse(b);
   int64_t J = b->n;
   if (J == 0) return 0; /* keep the previous values (SolverTools.py:150-153) */
   if (J > *ccap) {
@@ -545,6 +611,7 @@ int or_loop(const or_wcsph *w, void *nnp, or_particles *P, int nthreads) {
       for (int64_t i = 0; i < n; i++) {
         if (P->label[i] != LABEL_FLUID) continue;
         if (near_pos(nn, P->x[i], P->y[i], P->h[i], P->x, P->y, P->h, &b)) { err |= 1; continue; }
+        if (w->sum_order == 1) nbuf_reverse(&b);
         double rho = 0.0;
         for (int64_t k = 0; k < b.n; k++) {
           int64_t g = b.idx[k];
@@ -570,6 +637,31 @@ int or_loop(const or_wcsph *w, void *nnp, or_particles *P, int nthreads) {
     nbuf_free(&b);
     free(cbuf);
   }
+  return err ? OR_ERR_ALLOC : OR_OK;
+}
+
+/* The regular pass of _loop (SolverTools.py:143-173) for the fluid particles
+ * in [i0, i1) only, on one thread, after the EOS pass over all particles: a
+ * bounded sample of an evaluation, for timing the reference's loop at sizes
+ * where a whole single-threaded evaluation takes minutes. */
+int or_loop_range(const or_wcsph *w, void *nnp, or_particles *P, int64_t i0, int64_t i1) {
+  or_nn *nn = (or_nn *)nnp;
+  for (int64_t i = 0; i < P->n; i++) {
+    P->p[i] = tait(w->gamma, w->B, w->rho0, P->rho[i], P->label[i], w->Pb);
+    P->c[i] = w->co;
+  }
+  nbuf b = {0};
+  or_comp *cbuf = NULL;
+  int64_t ccap = 0;
+  int err = 0;
+  if (i0 < 0) i0 = 0;
+  if (i1 > P->n) i1 = P->n;
+  for (int64_t i = i0; i < i1 && !err; i++) {
+    if (P->label[i] != LABEL_FLUID) continue;
+    if (loop_one(w, nn, P, i, &b, &cbuf, &ccap)) err = 1;
+  }
+  nbuf_free(&b);
+  free(cbuf);
   return err ? OR_ERR_ALLOC : OR_OK;
 }
 

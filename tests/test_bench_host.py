@@ -1,5 +1,6 @@
 """bench.py's host-side logic on the CPU: the graph plan that covers exactly
-the requested steps, the workload recipes and their CPU samples."""
+the requested steps, the workload recipes, the configuration both arms
+report and the roofline annotations."""
 import numpy as np
 
 
@@ -20,13 +21,14 @@ def test_dam_break_recipe_sizes():
     # boundary convention of the examples: m = rho = h = 0
     b = pa["label"] != 0
     assert not np.any(pa["m"][b]) and not np.any(pa["h"][b])
-    small, height, what = bench.sample("dambreak1m", wl, 60)
-    assert int(np.sum(small["label"] == 0)) == 60 * 120
-    assert abs(height - 1.2) < 1e-12 and "60x120" in what
+    cfg = bench.arm_config("dambreak1m", wl)
+    assert cfg["n_fluid"] == 707 * 1414 and cfg["n_particles"] == 1027986
+    assert cfg["workload"].startswith("dambreak1m: ")
 
 
 def test_roofline_annotations_cover_both_forms():
     import bench
-    assert set(bench.LIMITER) == {"mixed", "fp64"}
-    assert bench.TRAFFIC_PER_PARTICLE[("dambreak1m", "mixed")] < bench.PAIR_BYTES
+    assert set(bench.LIMITER_FROM_PROFILE) == {"mixed", "fp64"}
+    per, when = bench.TRAFFIC_FROM_PROFILE[("dambreak1m", "mixed")]
+    assert 0 < per < 2 * bench.PAIR_BYTES and when
     assert bench.STEP_BYTES == 32 + 144 + 24 + 81 + 104
