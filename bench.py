@@ -343,6 +343,42 @@ def run_reference(args, wl_name):
     print(json.dumps(out))
 
 
+def solver_run_bench(wl, precision="mixed", lengths=(20, 120)):
+    """The drop-in Solver.run (the reference's driver loop: TimeStep with its
+    0.25 / 0.25 numbers, settling ended by customSettle at the first check,
+    no export properties, no incremental write-out) on the workload, timed
+    around run() with the host clock for two run lengths; the steady
+    throughput is the difference of fluid particle-steps over the difference
+    of times, so set-up, the two settling steps and the settling transfer
+    cancel."""
+    import torch
+    import sph
+    kernels = {0: sph.CubicSpline, 1: sph.Gaussian, 2: sph.Wendland}
+    pa = wl["pa"]
+    nf = int(np.sum(pa["label"] == 0))
+    co = 10.0 * np.sqrt(2 * 9.81 * wl["height"])
+    dt_c = 0.25 * wl["h"] / co
+    runs = []
+    for n in lengths:
+        s = sph.Solver(sph.WCSPH(wl["height"], wl["r0"], 1000.0, False, 0.0), sph.PEC(False, True),
+                       kernels[wl["kernel"]](), duration=n * dt_c, h=wl["h"], exportProperties=[],
+                       incrementalWriteout=False, customSettle=lambda pA, sv: True, precision=precision)
+        s.addParticles(pa.copy())
+        s.setup()
+        torch.cuda.synchronize()
+        t0 = time.perf_counter()
+        s.run()
+        el = time.perf_counter() - t0
+        runs.append((s.t_step, el))
+        del s
+        torch.cuda.empty_cache()
+    (k1, t1), (k2, t2) = runs
+    return {"value": nf * (k2 - k1) / (t2 - t1), "unit": UNIT, "precision": precision,
+            "steps": [k1, k2], "seconds": [t1, t2], "ms_per_step_steady": (t2 - t1) / (k2 - k1) * 1e3,
+            "how": "sph.Solver.run (settled steps in device chunks of 64 with one host synchronisation each), "
+                   "host clock around run(), steady rate from two run lengths"}
+
+
 def replica_value(el, nfluid, steps, world, device):
     """Whole-job throughput of N independent replicas: the slowest rank's
     elapsed time (max over ranks) and the fluid particle-steps of all ranks
@@ -356,7 +392,7 @@ def replica_value(el, nfluid, steps, world, device):
     return el, world * nfluid * steps / el
 
 
-def adjoint_case(nsteps=200):
+def adjoint_case(nsteps=200, adjoint_precision="fp64"):
     """The differentiation form's case: a 1.0 x 2.0 m column at dx = 0.01
     (20k fluid) against the right wall of the 4 x 3 m tank, 200 PEC steps,
     checkpoints every 20; loss = time integral of the load on the right wall.
@@ -367,29 +403,20 @@ def adjoint_case(nsteps=200):
     from sph import adjoint, scenarios
     pa = scenarios.cfg_adjoint()
     return adjoint.WallLoadCase(pa, height=2.0, r0=0.01, h=0.013, dt=5e-5, nsteps=nsteps, wall_x=4.0,
-                                checkpoint=20 if nsteps >= 100 else 10)
+                                checkpoint=20 if nsteps >= 100 else 10, adjoint_precision=adjoint_precision)
 
 
-def adjoint_cost(reps=3):
-    """Forward pass (loss only) and backward pass (replay + adjoint) of the
-    differentiation form, CUDA-event timed; gradient checks against central
-    differences (eps = 1e-6, FP64) along alpha and one random direction each
-    for the initial positions and velocities."""
+def _adjoint_timed(case, pos, vel, reps):
+    """Median forward (loss only), forward with checkpoints and backward
+    times (ms, CUDA events) and the last gradients."""
     import torch
     from sph import adjoint
-    case = adjoint_case()
-    # a small seeded initial velocity field, N(0, 0.01 m/s) per component:
-    # at rest every pair sits on the kink of the artificial-viscosity switch
-    # (v_ij . x_ij = 0), where the loss has only one-sided derivatives
-    torch.manual_seed(3)
-    pos = case.positions()
-    vel = case.velocities() + 0.01 * torch.randn_like(pos)
     a = torch.tensor(0.01, dtype=torch.float64, device="cuda", requires_grad=True)
     p = pos.clone().requires_grad_(True)
     v = vel.clone().requires_grad_(True)
     torch.autograd.grad(adjoint.WallLoadLoss.apply(a, p, v, case), (a, p, v))  # warm-up
     case.loss(0.01, pos, vel)
-    ev = [torch.cuda.Event(enable_timing=True) for _ in range(5)]
+    ev = [torch.cuda.Event(enable_timing=True) for _ in range(4)]
     fwd, fwd_ckpt, bwd = [], [], []
     for _ in range(reps):
         torch.cuda.synchronize()
@@ -404,32 +431,71 @@ def adjoint_cost(reps=3):
         fwd.append(ev[0].elapsed_time(ev[1]))
         fwd_ckpt.append(ev[1].elapsed_time(ev[2]))
         bwd.append(ev[2].elapsed_time(ev[3]))
-    f, fc, b = float(np.median(fwd)), float(np.median(fwd_ckpt)), float(np.median(bwd))
+    return (float(np.median(fwd)), float(np.median(fwd_ckpt)), float(np.median(bwd)), loss.item(), ga, gp, gv)
+
+
+def adjoint_cost(reps=3):
+    """The differentiation form, FP64 and mixed adjoint: forward pass (loss
+    only) and backward pass (replay + adjoint), CUDA-event timed; gradient
+    checks against central differences (eps = 1e-6, FP64 forward) along
+    alpha and one random direction each for the initial velocities (over the
+    configured 200 steps) and positions (over 50 steps: over 200 the loss is
+    kinked in the positions, where pairs cross the Lennard-Jones cutoff, and
+    the differences do not converge in eps); the mixed adjoint's gradients
+    against the FP64 adjoint's."""
+    import torch
+    from sph import adjoint
+    case = adjoint_case()
+    case_m = adjoint_case(adjoint_precision="mixed")
+    # a small seeded initial velocity field, N(0, 0.01 m/s) per component:
+    # at rest every pair sits on the kink of the artificial-viscosity switch
+    # (v_ij . x_ij = 0), where the loss has only one-sided derivatives
+    torch.manual_seed(3)
+    pos = case.positions()
+    vel = case.velocities() + 0.01 * torch.randn_like(pos)
+    f, fc, b, loss, ga, gp, gv = _adjoint_timed(case, pos, vel, reps)
+    fm, fcm, bm, loss_m, gam, gpm, gvm = _adjoint_timed(case_m, pos, vel, reps)
     torch.manual_seed(2)
     dpos = torch.randn_like(pos)
     dpos /= torch.linalg.norm(dpos)
     dvel = torch.randn_like(vel)
     dvel /= torch.linalg.norm(dvel)
-    checks = {"alpha": (ga.item(), adjoint.central_difference(case, 0.01, pos, vel, d_alpha=1.0)),
-              "v0_direction": ((gv * dvel).sum().item(),
-                               adjoint.central_difference(case, 0.01, pos, vel, d_vel=dvel)),
-              "x0_direction": ((gp * dpos).sum().item(),
-                               adjoint.central_difference(case, 0.01, pos, vel, d_pos=dpos))}
-    # over 200 steps the loss is kinked in x0 (pairs crossing the
-    # Lennard-Jones cutoff), so the x0 difference does not converge in eps;
-    # the same check over the first 50 steps does
+    fd = {"alpha": adjoint.central_difference(case, 0.01, pos, vel, d_alpha=1.0),
+          "v0_direction": adjoint.central_difference(case, 0.01, pos, vel, d_vel=dvel)}
+    grads = {"fp64": {"alpha": ga.item(), "v0_direction": (gv * dvel).sum().item()},
+             "mixed": {"alpha": gam.item(), "v0_direction": (gvm * dvel).sum().item()}}
     short = adjoint_case(nsteps=50)
-    _, ga50, gp50, gv50 = adjoint.gradients(short, 0.01, pos, vel)
-    checks["x0_direction_50_steps"] = ((gp50 * dpos).sum().item(),
-                                       adjoint.central_difference(short, 0.01, pos, vel, d_pos=dpos))
-    checks["v0_direction_50_steps"] = ((gv50 * dvel).sum().item(),
-                                       adjoint.central_difference(short, 0.01, pos, vel, eps=1e-5, d_vel=dvel))
+    short_m = adjoint_case(nsteps=50, adjoint_precision="mixed")
+    _, _, gp50, gv50 = adjoint.gradients(short, 0.01, pos, vel)
+    _, _, gp50m, gv50m = adjoint.gradients(short_m, 0.01, pos, vel)
+    fd["x0_direction_50_steps"] = adjoint.central_difference(short, 0.01, pos, vel, d_pos=dpos)
+    fd["v0_direction_50_steps"] = adjoint.central_difference(short, 0.01, pos, vel, eps=1e-5, d_vel=dvel)
+    grads["fp64"]["x0_direction_50_steps"] = (gp50 * dpos).sum().item()
+    grads["fp64"]["v0_direction_50_steps"] = (gv50 * dvel).sum().item()
+    grads["mixed"]["x0_direction_50_steps"] = (gp50m * dpos).sum().item()
+    grads["mixed"]["v0_direction_50_steps"] = (gv50m * dvel).sum().item()
+    # over 200 steps along positions, as a figure only (no convergence in eps)
+    x0_200 = {"adjoint": (gp * dpos).sum().item(),
+              "central_difference": adjoint.central_difference(case, 0.01, pos, vel, d_pos=dpos)}
+
+    def nrel(a, b):
+        return (torch.linalg.norm(a - b) / torch.linalg.norm(b)).item()
+
     return {"case": "20k-fluid dam break against the right wall, v0 ~ N(0, 0.01 m/s), 200 PEC steps, dt=5e-5, "
-                    "FP64, checkpoints every 20",
-            "n_fluid": case.nf, "loss": loss.item(), "forward_ms": f, "forward_with_checkpoints_ms": fc,
+                    "FP64 forward, checkpoints every 20",
+            "n_fluid": case.nf, "loss": loss, "forward_ms": f, "forward_with_checkpoints_ms": fc,
             "backward_ms": b, "backward_over_forward": b / f, "forward_plus_backward_over_forward": (fc + b) / f,
-            "fd_rel_err": {k: abs(g - d) / abs(d) for k, (g, d) in checks.items()},
-            "grad_vs_fd": {k: [g, d] for k, (g, d) in checks.items()}}
+            "fd_rel_err": {k: abs(grads["fp64"][k] - d) / abs(d) for k, d in fd.items()},
+            "grad_vs_fd": {k: [grads["fp64"][k], d] for k, d in fd.items()},
+            "x0_direction_200_steps": x0_200,
+            "mixed": {"what": "FP32 pair arithmetic in the adjoint pair product, FP64 forward and replay",
+                      "backward_ms": bm, "backward_over_forward": bm / f,
+                      "forward_plus_backward_over_forward": (fcm + bm) / f,
+                      "fd_rel_err": {k: abs(grads["mixed"][k] - d) / abs(d) for k, d in fd.items()},
+                      "vs_fp64_adjoint": {"alpha": abs(gam.item() - ga.item()) / abs(ga.item()),
+                                          "positions": nrel(gpm, gp), "velocities": nrel(gvm, gv),
+                                          "positions_50_steps": nrel(gp50m, gp50),
+                                          "velocities_50_steps": nrel(gv50m, gv50)}}}
 
 
 def batch_bench(count=256, steps=50, warmup=5):
@@ -654,8 +720,10 @@ def main():
                              "alternating device copies of the state",
                       "h2d_bytes_per_step": h2d,
                       "d2h_bytes_per_step": d2h, "steps": ke}
-        out["cpu_baseline"] = cpu_baseline(args.workload, wl)
         del dp, ws
+        torch.cuda.empty_cache()
+        out["solver_run"] = solver_run_bench(wl, args.precision)
+        out["cpu_baseline"] = cpu_baseline(args.workload, wl)
         torch.cuda.empty_cache()
         out["adjoint"] = adjoint_cost()
         torch.cuda.empty_cache()

@@ -143,7 +143,10 @@ typedef struct sph_workspace {
 int sph_abi_version(void);
 
 /* Bytes of device workspace for up to n particles and max_cells search cells
- * (max_cells <= 0 picks the default, sph_default_max_cells(n)). */
+ * (max_cells <= 0 picks the default, sph_default_max_cells(n)), including
+ * the sorted state copy that sph_run steps on (19 doubles, a label and an
+ * index per particle); a smaller workspace that holds everything else still
+ * works, sph_run then steps on the caller's arrays. */
 int sph_workspace_size(int64_t n, int64_t max_cells, size_t *bytes);
 int64_t sph_default_max_cells(int64_t n);
 
@@ -198,9 +201,11 @@ int sph_nn_update(const sph_particles_t *pa, const sph_config_t *cfg, const sph_
  * on the table of the last sph_nn_update: counts[i] = number of neighbours
  * (device int64[n]).  Then, with offsets = exclusive prefix sum of counts
  * (device int64[n+1]), sph_nn_export writes the neighbour indices of i into
- * idx[offsets[i] .. offsets[i+1]) in ascending index order.  The neighbour
- * SETS are those of the reference, bit for bit, including its truncated
- * 3x3-cell stencil and its aliasing of x-overflow cells. */
+ * idx[offsets[i] .. offsets[i+1]).  The lists are those of the reference,
+ * bit for bit and in its order: the 3x3 stencil cells with the x shift outer
+ * and the y shift inner, descending index inside a cell (the head-insert
+ * order of its linked lists, NNLinkedList.py:50-78, 129-141), including its
+ * truncated stencil and its aliasing of x-overflow cells. */
 int sph_nn_count(const sph_particles_t *pa, const sph_config_t *cfg, const sph_workspace_t *ws, int64_t *counts,
                  sph_stream_t stream);
 int sph_nn_export(const sph_particles_t *pa, const sph_config_t *cfg, const sph_workspace_t *ws, const int64_t *offsets,
@@ -210,7 +215,7 @@ int sph_nn_export(const sph_particles_t *pa, const sph_config_t *cfg, const sph_
  * (px, py, ph device arrays) on the table of the last build in ws (as the
  * reference, distances use pa's current positions): the same count /
  * offsets / export protocol as sph_nn_count / sph_nn_export, each list in
- * ascending index order with its h_ij, q and r (device arrays, offsets[np]
+ * the reference's order with its h_ij, q and r (device arrays, offsets[np]
  * entries). */
 int sph_nn_probe_count(const sph_particles_t *pa, const sph_workspace_t *ws, int64_t np, const double *px,
                        const double *py, const double *ph, int64_t *counts, sph_stream_t stream);
@@ -228,6 +233,32 @@ int sph_nn_probe_export(const sph_particles_t *pa, const sph_workspace_t *ws, in
 int sph_probe_density(const sph_particles_t *pa, const sph_wcsph_t *w, int kernel, const sph_workspace_t *ws,
                       int64_t np, const double *px, const double *py, const double *h_search, const double *h_kernel,
                       double *rho, double *p, sph_stream_t stream);
+
+/* One particle's block of neighbours in the reference's computed_dtype layout
+ * (src/Common.py:60-98) as device structure-of-arrays of n entries: label,
+ * m, p, rho, h (the pair's averaged h), c, r, the kernel value w and
+ * gradient dw_x, dw_y, and the differences x, y, vx, vy (particle minus
+ * neighbour), as _assignProps fills it (src/Tools/SolverTools.py:74-104). */
+typedef struct sph_block {
+  int64_t n;
+  const int8_t *label;
+  const double *m, *p, *rho, *h, *c, *r, *w, *dw_x, *dw_y, *x, *y, *vx, *vy;
+} sph_block_t;
+
+/* The per-neighbour-block equations of one particle, the work of the
+ * reference's plugin methods WCSPH.compute_density_change,
+ * compute_acceleration and compute_velocity (src/Methods/WCSPH.py:151-203)
+ * and of BoundaryForce (src/Equations/BoundaryForce.py:6-42), which _loop
+ * calls per particle (src/Tools/SolverTools.py:143-173).  self4 (host) =
+ * {p, rho, h, c} of the particle; out (device, 7 doubles) receives the sums
+ * {Continuity, Momentum x, Momentum y (no gravity), BoundaryForce x, y,
+ * XSPH x, y} (src/Equations/Continuity.py:4-16, Momentum.py:5-57,
+ * XSPH.py:5-31), each in the block's order as the reference sums them.  The
+ * methods' switches (summation density, XSPH, the -9.81 of gravity) are the
+ * caller's.  Not a hot path: the step runs these equations fused in its
+ * pair kernels. */
+int sph_block_equations(const sph_block_t *blk, const double *self4, const sph_wcsph_t *w, double *out,
+                        sph_stream_t stream);
 
 /* Solver._compute (src/Solver.py:232-256) = NNLinkedList.update, the h reset
  * (fixed or computeH, src/Tools/SolverTools.py:106-118) and the derivative
@@ -299,7 +330,13 @@ int sph_newmark_acceleration(int64_t n, int32_t kl, int32_t ku, const double *M,
 /* nsteps bare time steps of Solver.run's loop body (src/Solver.py:366-410)
  * with settling and storage left out: dt (TimeStep or cfg->dt_fixed) ->
  * predict -> _compute -> correct, all on the device.  dt_hist, if not NULL,
- * receives 3 doubles per step {dt, dt_courant, dt_force} (device memory). */
+ * receives 3 doubles per step {dt, dt_courant, dt_force} (device memory).
+ * A run of 4 or more steps, in a workspace sized by sph_workspace_size,
+ * steps on a copy of the state in the workspace, gathered once into the
+ * sorted order of a first neighbour build and scattered back at the end;
+ * the results are the same, bit for bit.  The workspace's neighbour table
+ * then refers to that copy: call sph_nn_update before sph_nn_count,
+ * sph_nn_export or the probes. */
 int sph_run(sph_particles_t *pa, const sph_wcsph_t *w, const sph_config_t *cfg, const sph_workspace_t *ws, int64_t nsteps,
             double *dt_hist, sph_stream_t stream);
 
@@ -337,7 +374,12 @@ int sph_run_profiled(sph_particles_t *pa, const sph_wcsph_t *w, const sph_config
 int sph_run_wall_load(sph_particles_t *pa, const sph_wcsph_t *w, const sph_config_t *cfg, const sph_workspace_t *ws,
                       int64_t nsteps, double wall_x, double *fr, double *load_hist, sph_stream_t stream);
 
-/* Adjoint of one step.  On entry xb .. drhob hold d loss / d S' for the
+/* Adjoint of one step (cfg->precision: SPH_PREC_FP64, the reference's
+ * arithmetic, or SPH_PREC_MIXED, the mixed form: the pair arithmetic of the
+ * vector-Jacobian product in FP32 over the FP64 records and adjoint vectors;
+ * the state update and the step-to-step accumulation stay FP64, and the
+ * forward and its replay are FP64 either way).  On entry xb .. drhob hold
+ * d loss / d S' for the
  * state after the step (fluid particles; caller order), on exit d loss / d S
  * for the state before it; S is pa's x, y, vx, vy, rho, ax, ay, drho (the
  * state before the step, as sph_run leaves it).  alphab[i] accumulates the
@@ -380,7 +422,7 @@ int sph_batch_workspace_size(int64_t n_total, int64_t n_inst, int64_t max_cells,
 /* Prepares ws (allocated with sph_batch_workspace_size and the same
  * max_cells) for the instances: offsets (host, n_inst + 1), w and h_fixed
  * (host, one per instance), cfg (shared settings).  tile_shift_max: the
- * largest tile shift of the own-grid cell numbering (0..3; -1: default).
+ * largest tile shift of the own-grid cell numbering (0..4; -1: default).
  * Synchronises. */
 int sph_batch_setup(const sph_workspace_t *ws, int64_t n_inst, const int64_t *offsets, const sph_wcsph_t *w,
                     const double *h_fixed, const sph_config_t *cfg, int32_t tile_shift_max, sph_stream_t stream);

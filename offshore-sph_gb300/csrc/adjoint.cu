@@ -1,4 +1,4 @@
-// adjoint.cu -- reverse mode of the WCSPH step (FP64 form).
+// adjoint.cu -- reverse mode of the WCSPH step (FP64 and mixed forms).
 //
 // The forward step with a fixed dt (src/Solver.py:370-372 timeStep path) and
 // the PEC integrator (src/Integrators/PEC.py:32-89, damping 0) maps the state
@@ -287,6 +287,182 @@ __global__ void __launch_bounds__(kAdjBlock, 12) k_pair_adjoint(AdjPtrs P, AdjPa
   }
 }
 
+// ---------------------------------------------------------------------------
+// Mixed form of the adjoint pair product: the same vector-Jacobian product as
+// adjoint_query with the pair arithmetic in FP32 (hardware reciprocals and
+// square roots) and the per-particle sums in FP32, over the FP64 records of
+// the forward evaluation and the FP64 adjoint vectors.  Differences of FP64
+// positions and velocities are formed in FP64 and then rounded, so large
+// coordinates lose no accuracy.  The forward's q <= 3 decision is redone
+// exactly where FP32 could decide it differently.
+// ---------------------------------------------------------------------------
+template <int KERNEL>
+__device__ __forceinline__ void grad_coef_f(float r, float q, float ih, float ir, float &coef, float &dcoef) {
+  coef = 0.f;
+  dcoef = 0.f;
+  const float ih2 = ih * ih;
+  if (KERNEL == SPH_KERNEL_CUBIC) {
+    if (q > 2.0f || r < 1e-10f) return;
+    const float al = (float)kCubicFac * ih2;
+    float g, gp;
+    if (q > 1.0f) {
+      const float t = 2.0f - q;
+      g = -0.75f * t * t;
+      gp = 1.5f * t;
+    } else {
+      g = -3.0f * q * (1.0f - 0.75f * q);
+      gp = -3.0f + 4.5f * q;
+    }
+    const float a = al * ih * ir;
+    coef = a * g;
+    dcoef = a * (gp * ih - g * ir);
+  } else if (KERNEL == SPH_KERNEL_WENDLAND) {
+    if (q >= 2.0f || r < 1e-10f) return;
+    const float al = (float)kWendFac * ih2;
+    const float in = 1.0f - 0.5f * q, in2 = in * in, in4 = in2 * in2;
+    const float g = in4 * in * (-14.0f / 3.0f) * q * (1.0f + 2.5f * q);
+    const float gp = (-14.0f / 3.0f) * (in4 * in * (1.0f + 5.0f * q) - 2.5f * in4 * q * (1.0f + 2.5f * q));
+    const float a = al * ih * ir;
+    coef = a * g;
+    dcoef = a * (gp * ih - g * ir);
+  } else {
+    if (!(q <= 3.0f) || !(r > 1e-12f * ih)) return;
+    coef = -2.0f * (float)kInvPi * ih2 * __expf(-q * q) * ih2;
+    dcoef = coef * (-2.0f * r * ih2);
+  }
+}
+
+template <int KERNEL>
+__device__ __forceinline__ void adjoint_query_mixed(const AdjPtrs &P, const AdjParams &ap, long long k, int i,
+                                                    float &gx, float &gy, float &gvx, float &gvy, float &grho,
+                                                    float &gal) {
+  const DevGrid &g = *P.grid;
+  const double4_32a Ak = P.r64a[k], Bk = P.r64b[k];
+  const double xk = Ak.x, yk = Ak.y, vxk = Ak.z, vyk = Ak.w;
+  const double hk = Bk.w;
+  const float mk = d2f_trunc(Bk.x), rhok = d2f_trunc(Bk.y), othrk = d2f_trunc(Bk.z), hkf = d2f_trunc(hk);
+  const float lAxk = d2f_trunc(P.lax[i]), lAyk = d2f_trunc(P.lay[i]), lDk = d2f_trunc(P.lad[i]);
+  const float dothk = d2f_trunc(dothr_drho(Bk.y, Bk.z, ap));
+  const float ihk = __fdividef(1.0f, hkf);
+  const float cbar = 0.5f * (float)ap.co, alpha = (float)ap.alpha, beta = (float)ap.beta;
+  const float r0 = (float)ap.r0, D = (float)ap.D, p1 = (float)ap.p1, p2 = (float)ap.p2;
+  const float omega_m = (float)ap.omega * mk;
+  const int2 qref = P.meta[k];
+  const int qkey = P.keys_sorted[k];
+  const bool slow = qref.x >= g.ncx || !(hk > 0.0);
+  const int W = g.mode == 0 ? 1 : (slow ? g.wide : g.wt);
+  const bool filter = g.mode == 1 && (g.need_filter || P.ctrl->alias_count > 0);
+  const float4 Qi = P.rec0[k];
+  const float hif = Qi.z, pad = g.pad_e;
+  const float SK = (float)Support<KERNEL>::q * 1.000002f;
+  const Stencil sten(g, qref, qkey, W);
+  for_stencil(sten, P.cstart, [&](unsigned int j) {
+    if (j == (unsigned int)k) return;
+    if (filter && !in_ref_stencil(P.meta, j, g, qref)) return;
+    {
+      const float4 qj = P.rec0[j];
+      const float fx = Qi.x - qj.x, fy = Qi.y - qj.y;
+      const float hijf = 0.5f * (hif + fabsf(qj.z));
+      float reach = SK * hijf;
+      if (signbit(qj.z)) reach = fmaxf(reach, fminf(r0, 3.0f * hijf) * 1.000002f);
+      const float rp = reach + pad;
+      if (fx * fx + fy * fy > rp * rp) return;
+    }
+    const double4_32a Aj = P.r64a[j], Bj = P.r64b[j];
+    const double dxd = xk - Aj.x, dyd = yk - Aj.y;
+    const float dx = d2f_trunc(dxd), dy = d2f_trunc(dyd);
+    const float d2 = dx * dx + dy * dy;
+    if (!(d2 > 1e-24f)) return;  // coincident: no kernel gradient, no boundary force
+    const float ir = rsqrtf(d2);
+    const float r = d2 * ir;
+    const double hj = fabs(Bj.w);
+    const float hjf = d2f_trunc(hj);
+    const float hij = 0.5f * (hkf + hjf);
+    const float ih = hj == hk ? ihk : (hj == 0.0 ? 2.0f * ihk : __fdividef(1.0f, hij));
+    const float q = r * ih;
+    bool in = q <= 3.0f;
+    if (fabsf(q - 3.0f) < 1e-4f) {  // the forward's neighbour test (NNLinkedList.py:74), exactly
+      const double rd = __dsqrt_rn(__dadd_rn(__dmul_rn(dxd, dxd), __dmul_rn(dyd, dyd)));
+      in = __ddiv_rn(rd, __dmul_rn(0.5, __dadd_rn(hk, hj))) <= 3.0;
+    }
+    if (!in) return;
+    if (!signbit(Bj.w)) {
+      // fluid pair: continuity + momentum with artificial viscosity
+      const float mj = d2f_trunc(Bj.x), rhoj = d2f_trunc(Bj.y), othrj = d2f_trunc(Bj.z);
+      const float vxij = d2f_trunc(vxk - Aj.z), vyij = d2f_trunc(vyk - Aj.w);
+      float coef, dcoef;
+      grad_coef_f<KERNEL>(r, q, ih, ir, coef, dcoef);
+      if (coef == 0.f && dcoef == 0.f) return;
+      const float dWx = coef * dx, dWy = coef * dy;
+      const float dot = vxij * dx + vyij * dy;
+      const float irbar = __fdividef(2.0f, rhok + rhoj);
+      float Pi = 0.f, dPi_dmu = 0.f, mu = 0.f, iden = 0.f, hb = 0.f;
+      if (dot < 0.f) {
+        hb = 0.5f * (hkf + hij);
+        iden = __fdividef(1.0f, d2 + 0.01f * hb * hb);
+        mu = hb * dot * iden;
+        Pi = mu * (beta * mu - alpha * cbar) * irbar;
+        dPi_dmu = (2.0f * beta * mu - alpha * cbar) * irbar;
+      }
+      const float S = othrk + othrj + Pi;
+      const int pj = P.perm[j];
+      const float lAxj = d2f_trunc(P.lax[pj]), lAyj = d2f_trunc(P.lay[pj]), lDj = d2f_trunc(P.lad[pj]);
+      const float lQx = -mj * lAxk + mk * lAxj, lQy = -mj * lAyk + mk * lAyj;
+      const float lC = mj * lDk + mk * lDj;
+      const float lQdW = lQx * dWx + lQy * dWy;
+      // (d dW / d u)^T z = coef z + dcoef (u . z) u / r
+      const float cq = S * dcoef * (dx * lQx + dy * lQy) * ir + lC * dcoef * dot * ir;
+      gx += S * coef * lQx + lC * coef * vxij + cq * dx;
+      gy += S * coef * lQy + lC * coef * vyij + cq * dy;
+      gvx += lC * dWx;
+      gvy += lC * dWy;
+      if (dot < 0.f) {
+        const float f = lQdW * dPi_dmu * hb * iden;
+        const float c2 = 2.0f * dot * iden;
+        gx += f * (vxij - c2 * dx);
+        gy += f * (vyij - c2 * dy);
+        gvx += f * dx;
+        gvy += f * dy;
+        gal += mj * (lAxk * dWx + lAyk * dWy) * (mu * cbar * irbar);
+      }
+      grho += lQdW * (dothk - 0.5f * Pi * irbar);
+    } else if (r <= r0 && r > 1e-12f) {
+      // boundary pair: Lennard-Jones force and the wall load
+      const float s = r0 * ir;
+      float sp1, sp2;
+      if (ap.lj_42) {
+        sp2 = s * s;
+        sp1 = sp2 * sp2;
+      } else {
+        sp1 = __powf(s, p1);
+        sp2 = __powf(s, p2);
+      }
+      const float ir2 = ir * ir;
+      const float phi = (sp1 - sp2) * ir2;
+      const float dphi = ((-p1 - 2.0f) * sp1 + (p2 + 2.0f) * sp2) * ir2 * ir;
+      const float zx = lAxk - ((ap.omega != 0.0 && Aj.x >= ap.wall_x) ? omega_m : 0.f), zy = lAyk;
+      const float c = dphi * (dx * zx + dy * zy) * ir;
+      gx += D * (phi * zx + c * dx);
+      gy += D * (phi * zy + c * dy);
+    }
+  });
+}
+
+template <int KERNEL>
+__global__ void __launch_bounds__(kBlock) k_pair_adjoint_mixed(AdjPtrs P, AdjParams ap) {
+  const long long k = (long long)blockIdx.x * blockDim.x + threadIdx.x;
+  if (k >= ap.n) return;
+  const int i = P.perm[k];
+  float gx = 0.f, gy = 0.f, gvx = 0.f, gvy = 0.f, grho = 0.f, gal = 0.f;
+  if (!signbit(P.r64b[k].w)) adjoint_query_mixed<KERNEL>(P, ap, k, i, gx, gy, gvx, gvy, grho, gal);
+  P.xhb[i] = f2d(gx);
+  P.yhb[i] = f2d(gy);
+  P.vxhb[i] = f2d(gvx);
+  P.vyhb[i] = f2d(gvy);
+  P.rhohb[i] = f2d(grho);
+  P.alb[i] = f2d(gal);
+}
+
 // lambda_A = dt vb' + ab', lambda_D = dt rhob' + drhob' (zero for non-fluid)
 __global__ void k_adj_pre(const int8_t *__restrict__ label, long long n, double dt, const double *vxb,
                           const double *vyb, const double *rhob, const double *axb, const double *ayb,
@@ -419,10 +595,17 @@ void launch_adjoint_step(const StepArgs &s, const StepArgs &h, const WsPtrs &w, 
   ap.wall_x = adj.wall_x;
   ap.dt = dt;
   ap.n = n;
-  const unsigned nbp = nblocks(n * kAdjSplit, kAdjBlock);
-  if (cfg.kernel == SPH_KERNEL_CUBIC) k_pair_adjoint<SPH_KERNEL_CUBIC><<<nbp, kAdjBlock, 0, st>>>(P, ap);
-  else if (cfg.kernel == SPH_KERNEL_WENDLAND) k_pair_adjoint<SPH_KERNEL_WENDLAND><<<nbp, kAdjBlock, 0, st>>>(P, ap);
-  else k_pair_adjoint<SPH_KERNEL_GAUSSIAN><<<nbp, kAdjBlock, 0, st>>>(P, ap);
+  if (cfg.precision == SPH_PREC_MIXED) {
+    const unsigned nbm = nblocks(n, kBlock);
+    if (cfg.kernel == SPH_KERNEL_CUBIC) k_pair_adjoint_mixed<SPH_KERNEL_CUBIC><<<nbm, kBlock, 0, st>>>(P, ap);
+    else if (cfg.kernel == SPH_KERNEL_WENDLAND) k_pair_adjoint_mixed<SPH_KERNEL_WENDLAND><<<nbm, kBlock, 0, st>>>(P, ap);
+    else k_pair_adjoint_mixed<SPH_KERNEL_GAUSSIAN><<<nbm, kBlock, 0, st>>>(P, ap);
+  } else {
+    const unsigned nbp = nblocks(n * kAdjSplit, kAdjBlock);
+    if (cfg.kernel == SPH_KERNEL_CUBIC) k_pair_adjoint<SPH_KERNEL_CUBIC><<<nbp, kAdjBlock, 0, st>>>(P, ap);
+    else if (cfg.kernel == SPH_KERNEL_WENDLAND) k_pair_adjoint<SPH_KERNEL_WENDLAND><<<nbp, kAdjBlock, 0, st>>>(P, ap);
+    else k_pair_adjoint<SPH_KERNEL_GAUSSIAN><<<nbp, kAdjBlock, 0, st>>>(P, ap);
+  }
   k_adj_post<<<nb, kBlock, 0, st>>>(s.label, n, dt, adj.xb, adj.yb, adj.vxb, adj.vyb, adj.rhob, adj.axb, adj.ayb,
                                     adj.drhob, adj.xhb, adj.yhb, adj.vxhb, adj.vyhb, adj.rhohb, adj.alb, adj.alphab);
 }

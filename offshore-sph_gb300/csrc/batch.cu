@@ -119,7 +119,7 @@ int sph_batch_setup(const sph_workspace_t *ws, int64_t n_inst, const int64_t *of
     if (offsets[b + 1] <= offsets[b] || !(h_fixed[b] > 0.0)) return SPH_ERR_INVALID_ARGUMENT;
     if (w[b].use_xsph || w[b].use_summation_density) return SPH_ERR_INVALID_ARGUMENT;
   }
-  const int ts_own = tile_shift_max >= 0 && tile_shift_max <= 3 ? tile_shift_max : SPH_TILE_SHIFT_OWN;
+  const int ts_own = tile_shift_max >= 0 && tile_shift_max <= 4 ? tile_shift_max : SPH_TILE_SHIFT_OWN;
   std::vector<InstParams> ip((size_t)n_inst);
   for (int64_t b = 0; b < n_inst; b++) {
     InstParams &p = ip[(size_t)b];

@@ -43,6 +43,10 @@ WsLayout make_layout(long long n_cap, long long max_cells) {
   L.fb = take((size_t)L.fb_cap * 8);
   L.tiles = take((mc + 1) * 4);
   L.total = off;
+  L.shadow = take(n * 8 * kStateFields);
+  L.shadow_label = take(n);
+  L.shadow_orig = take(n * 4);
+  L.total_shadow = off;
   return L;
 }
 
@@ -73,6 +77,11 @@ WsPtrs ws_ptrs(const sph_workspace_t *ws) {
   p.n_cap = L.n_cap;
   p.max_cells = L.max_cells;
   p.n_parts = L.n_parts;
+  const bool room = ws->bytes >= L.total_shadow;
+  p.shadow = room ? (double *)(b + L.shadow) : nullptr;
+  p.shadow_label = room ? (int8_t *)(b + L.shadow_label) : nullptr;
+  p.shadow_orig = room ? (int *)(b + L.shadow_orig) : nullptr;
+  p.orig = nullptr;
   return p;
 }
 
@@ -124,6 +133,61 @@ __global__ void k_selftest_staging(const float4 *src, unsigned int *result) {
     result[0] = same ? 1u : 0u;
     result[1] = ok1 ? 1u : 2u;
   }
+}
+
+// ---------------------------------------------------------------------------
+// The sorted copy of the state.  A run of several steps gathers the caller's
+// arrays once into the sorted order of a first neighbour build and steps on
+// that copy: particles that are neighbours in space are then neighbours in
+// memory, so each step's keys, scatter, records and derivative writes touch
+// nearly consecutive addresses instead of gathering through the caller's
+// order.  The in-cell order still ranks by the caller's index (WsPtrs::orig),
+// so the results are those of stepping on the caller's arrays, bit for bit.
+// At the end the copy is scattered back.
+// ---------------------------------------------------------------------------
+StepArgs shadow_args(const WsPtrs &w, long long n) {
+  StepArgs b;
+  b.n = n;
+  b.label = w.shadow_label;
+  double *f = w.shadow;
+  const long long st = w.n_cap > 0 ? w.n_cap : 1;
+  double **dst[kStateFields] = {&b.m, &b.rho, &b.p, &b.c, &b.drho, &b.h, &b.x, &b.y, &b.vx, &b.vy,
+                                &b.ax, &b.ay, &b.xsphx, &b.xsphy, &b.x0, &b.y0, &b.vx0, &b.vy0, &b.rho0};
+  for (int q = 0; q < kStateFields; q++) *dst[q] = f + q * st;
+  return b;
+}
+
+__device__ __forceinline__ double *const *state_fields(const StepArgs &a, double *(&f)[kStateFields]) {
+  f[0] = a.m; f[1] = a.rho; f[2] = a.p; f[3] = a.c; f[4] = a.drho; f[5] = a.h; f[6] = a.x; f[7] = a.y;
+  f[8] = a.vx; f[9] = a.vy; f[10] = a.ax; f[11] = a.ay; f[12] = a.xsphx; f[13] = a.xsphy; f[14] = a.x0;
+  f[15] = a.y0; f[16] = a.vx0; f[17] = a.vy0; f[18] = a.rho0;
+  return f;
+}
+
+// copy slot s = caller particle perm[s]; orig[s] remembers it
+__global__ void k_shadow_gather(StepArgs src, StepArgs dst, const int *__restrict__ perm, int *__restrict__ orig) {
+  const long long s = (long long)blockIdx.x * blockDim.x + threadIdx.x;
+  if (s >= src.n) return;
+  const int i = perm[s];
+  orig[s] = i;
+  double *fs[kStateFields], *fd[kStateFields];
+  state_fields(src, fs);
+  state_fields(dst, fd);
+#pragma unroll
+  for (int q = 0; q < kStateFields; q++) fd[q][s] = fs[q][i];
+  const_cast<int8_t *>(dst.label)[s] = src.label[i];
+}
+
+// the copy back to the caller's order (labels do not change)
+__global__ void k_shadow_scatter(StepArgs src, StepArgs dst, const int *__restrict__ orig) {
+  const long long s = (long long)blockIdx.x * blockDim.x + threadIdx.x;
+  if (s >= src.n) return;
+  const int i = orig[s];
+  double *fs[kStateFields], *fd[kStateFields];
+  state_fields(src, fs);
+  state_fields(dst, fd);
+#pragma unroll
+  for (int q = 0; q < kStateFields; q++) fd[q][i] = fs[q][s];
 }
 
 __global__ void k_fill_dt(double *dt_hist, long long nsteps, double dt) {
@@ -180,7 +244,7 @@ int sph_workspace_size(int64_t n, int64_t max_cells, size_t *bytes) {
   if (!bytes || n < 0) return SPH_ERR_INVALID_ARGUMENT;
   if (max_cells <= 0) max_cells = sph_default_max_cells(n);
   if (max_cells > 0x3fffffffll) return SPH_ERR_INVALID_ARGUMENT;
-  *bytes = make_layout(n, max_cells).total;
+  *bytes = make_layout(n, max_cells).total_shadow;
   return SPH_OK;
 }
 
@@ -402,6 +466,30 @@ int sph_correct(sph_particles_t *pa, const sph_config_t *cfg, const double *dt, 
   return check_launch();
 }
 
+// Runs of at least this many steps step on the sorted copy of the state
+// (when the workspace has room for it): the gather and scatter cost about a
+// step's worth of memory traffic.
+constexpr int64_t kShadowMinSteps = 4;
+
+// Start of a run on the sorted copy: a neighbour build of the caller's state
+// (its order only), then the gather; returns the copy's StepArgs and sets
+// wp.orig.  Without room or for short runs, the caller's own arrays.
+static StepArgs run_state(const StepArgs &a, WsPtrs &wp, const sph_config_t &cfg, const sph_wcsph_t &wc,
+                          int64_t nsteps, cudaStream_t st) {
+  if (nsteps < kShadowMinSteps || !wp.shadow) return a;
+  launch_bounds(a, wp, cfg, wc, kStageNone, false, nullptr, nullptr, st);
+  launch_build(a, wp, cfg, wc, st);
+  const StepArgs b = shadow_args(wp, a.n);
+  k_shadow_gather<<<nblocks(a.n), kBlock, 0, st>>>(a, b, wp.perm, wp.shadow_orig);
+  wp.orig = wp.shadow_orig;
+  return b;
+}
+
+static void run_finish(const StepArgs &a, const StepArgs &b, const WsPtrs &wp, cudaStream_t st) {
+  if (!wp.orig) return;
+  k_shadow_scatter<<<nblocks(a.n), kBlock, 0, st>>>(b, a, wp.orig);
+}
+
 int sph_run(sph_particles_t *pa, const sph_wcsph_t *w, const sph_config_t *cfg, const sph_workspace_t *ws,
             int64_t nsteps, double *dt_hist, sph_stream_t stream) {
   if (!particles_ok(pa) || !w || !config_ok(cfg) || nsteps < 0) return SPH_ERR_INVALID_ARGUMENT;
@@ -409,8 +497,9 @@ int sph_run(sph_particles_t *pa, const sph_wcsph_t *w, const sph_config_t *cfg, 
   if (e) return e;
   if (pa->n == 0 || nsteps == 0) return SPH_OK;
   cudaStream_t st = (cudaStream_t)stream;
-  StepArgs a = step_args(pa);
+  const StepArgs caller = step_args(pa);
   WsPtrs wp = ws_ptrs(ws);
+  const StepArgs a = run_state(caller, wp, *cfg, *w, nsteps, st);
   const bool fixed = cfg->dt_fixed > 0.0;
   double *ring = &wp.ctrl->dt_ring[0][0];
   if (fixed) {
@@ -429,21 +518,22 @@ int sph_run(sph_particles_t *pa, const sph_wcsph_t *w, const sph_config_t *cfg, 
     compute_body(a, wp, *w, *cfg, fixed ? nullptr : nxt, hist_next, st);
   }
   launch_correct(a, *cfg, ring + 3 * ((nsteps - 1) & 1), cfg->dt_fixed, st);
+  run_finish(caller, a, wp, st);
   return check_launch();
 }
 
-// the differentiation form's constraints: fixed dt and h, PEC, FP64, no XSPH
-// or summation density
-static bool adjoint_config_ok(const sph_wcsph_t *w, const sph_config_t *cfg) {
+// the differentiation form's constraints: fixed dt and h, PEC, no XSPH or
+// summation density; the forward is FP64, the adjoint step FP64 or mixed
+static bool adjoint_config_ok(const sph_wcsph_t *w, const sph_config_t *cfg, bool mixed_ok) {
   return cfg->dt_fixed > 0.0 && cfg->h_fixed > 0.0 && cfg->integrator == SPH_INTEGRATOR_PEC &&
-         cfg->precision == SPH_PREC_FP64 && !w->use_xsph && !w->use_summation_density && !cfg->pec_use_xsph &&
-         cfg->damping == 0.0;
+         (cfg->precision == SPH_PREC_FP64 || (mixed_ok && cfg->precision == SPH_PREC_MIXED)) && !w->use_xsph &&
+         !w->use_summation_density && !cfg->pec_use_xsph && cfg->damping == 0.0;
 }
 
 int sph_run_wall_load(sph_particles_t *pa, const sph_wcsph_t *w, const sph_config_t *cfg, const sph_workspace_t *ws,
                       int64_t nsteps, double wall_x, double *fr, double *load_hist, sph_stream_t stream) {
   if (!particles_ok(pa) || !w || !config_ok(cfg) || nsteps < 0 || !fr || !load_hist) return SPH_ERR_INVALID_ARGUMENT;
-  if (!adjoint_config_ok(w, cfg)) return SPH_ERR_INVALID_ARGUMENT;
+  if (!adjoint_config_ok(w, cfg, false)) return SPH_ERR_INVALID_ARGUMENT;
   int e = ws_ok(ws, pa->n);
   if (e) return e;
   if (pa->n == 0 || nsteps == 0) return SPH_OK;
@@ -470,7 +560,7 @@ int sph_adjoint_step(const sph_particles_t *pa, sph_particles_t *half, const sph
                      const sph_workspace_t *ws, const sph_adjoint_t *adj, sph_stream_t stream) {
   if (!particles_ok(pa) || !particles_ok(half) || half->n != pa->n || !w || !config_ok(cfg) || !adj)
     return SPH_ERR_INVALID_ARGUMENT;
-  if (!adjoint_config_ok(w, cfg)) return SPH_ERR_INVALID_ARGUMENT;
+  if (!adjoint_config_ok(w, cfg, true)) return SPH_ERR_INVALID_ARGUMENT;
   const double *need[] = {adj->xb, adj->yb, adj->vxb, adj->vyb, adj->rhob, adj->axb, adj->ayb, adj->drhob,
                           adj->alphab, adj->lax, adj->lay, adj->lad, adj->xhb, adj->yhb, adj->vxhb, adj->vyhb,
                           adj->rhohb, adj->alb};
@@ -492,8 +582,9 @@ int sph_run_profiled(sph_particles_t *pa, const sph_wcsph_t *w, const sph_config
   for (int k = 0; k < SPH_NSTAGES; k++) stage_ms[k] = 0.0;
   if (pa->n == 0 || nsteps == 0) return SPH_OK;
   cudaStream_t st = (cudaStream_t)stream;
-  StepArgs a = step_args(pa);
+  const StepArgs caller = step_args(pa);
   WsPtrs wp = ws_ptrs(ws);
+  const StepArgs a = run_state(caller, wp, *cfg, *w, nsteps, st);
   const bool fixed = cfg->dt_fixed > 0.0;
   double *ring = &wp.ctrl->dt_ring[0][0];
   cudaEvent_t ev[SPH_NSTAGES + 1];
@@ -530,6 +621,7 @@ int sph_run_profiled(sph_particles_t *pa, const sph_wcsph_t *w, const sph_config
   }
   cudaEventRecord(ev[SPH_STAGE_PAIR + 1], st);
   launch_correct(a, *cfg, ring + 3 * ((nsteps - 1) & 1), cfg->dt_fixed, st);
+  run_finish(caller, a, wp, st);  // the copy back counts with the last corrector
   lap(SPH_STAGE_CORRECT, SPH_STAGE_PAIR + 1);
   if (check_launch()) rc = SPH_ERR_CUDA;
   for (int k = 0; k <= SPH_NSTAGES; k++) cudaEventDestroy(ev[k]);

@@ -536,6 +536,7 @@ __global__ void __launch_bounds__(kBlock) k_keys(const double *__restrict__ x, c
 // ---------------------------------------------------------------------------
 constexpr int kScanThreads = 1024;
 constexpr int kScanPer = kScanTile / kScanThreads;
+static_assert(kScanPer == 4, "one uint4 of counts per thread");
 
 // The single-scene scan: scan tile b's offset is the sum of the totals of
 // tiles 0 .. b-1 (counted by k_keys), so one pass writes cstart.
@@ -549,10 +550,13 @@ __global__ void __launch_bounds__(kScanThreads) k_scan_cells(const unsigned int 
   const long long m = (long long)g->ncells + 1;
   const long long base = (long long)blockIdx.x * kScanTile;
   if (base >= m) return;
-  // the tile's counts and the earlier tiles' totals load together
+  // the tile's counts and the earlier tiles' totals load together; a tile
+  // that holds no particle (k_keys counted its total) skips its counts
   const long long c0 = base + (long long)threadIdx.x * kScanPer;
-  unsigned int v[kScanPer];
-  if (c0 + 3 < m) {
+  const bool empty = part[blockIdx.x] == 0u;
+  unsigned int v[kScanPer] = {0u, 0u, 0u, 0u};
+  if (empty) {
+  } else if (c0 + 3 < m) {
     const uint4 q = *(const uint4 *)(counts + c0);
     v[0] = q.x; v[1] = q.y; v[2] = q.z; v[3] = q.w;
   } else {
@@ -779,7 +783,7 @@ __global__ void __launch_bounds__(kBlock) k_cellsort(const int *__restrict__ per
                                                      int *__restrict__ tiles, StepArgs a, RecParams rp,
                                                      float4 *__restrict__ rec0, float4 *__restrict__ rec1,
                                                      float4 *__restrict__ rec2, double4_32a *__restrict__ r64a,
-                                                     double4_32a *__restrict__ r64b) {
+                                                     double4_32a *__restrict__ r64b, const int *__restrict__ orig) {
   __shared__ unsigned long long red[kBlock / 32];
   __shared__ unsigned int redn[kBlock / 32];
   const long long k = (long long)blockIdx.x * blockDim.x + threadIdx.x;
@@ -792,8 +796,16 @@ __global__ void __launch_bounds__(kBlock) k_cellsort(const int *__restrict__ per
     if (key < gp->ncells && (unsigned)k == __ldg(&cstart[(key >> ts2) << ts2]))
       tiles[atomicAdd(&ctrl->tl_count, 1u)] = key >> ts2;
     const int v = perm_tmp[k];
+    // rank inside the cell by particle index: the caller's index when the
+    // run steps on the sorted copy of the state (orig), so that the order,
+    // and with it every sum, is the same as on the caller's arrays
     unsigned int rank = 0;
-    for (unsigned int t = s; t < e; t++) rank += (unsigned)(perm_tmp[t] < v);
+    if (orig) {
+      const int ov = orig[v];
+      for (unsigned int t = s; t < e; t++) rank += (unsigned)(orig[perm_tmp[t]] < ov);
+    } else {
+      for (unsigned int t = s; t < e; t++) rank += (unsigned)(perm_tmp[t] < v);
+    }
     const unsigned int slot = s + rank;
     perm[slot] = v;
     meta[slot] = refcell[v];
@@ -839,7 +851,7 @@ void launch_build(const StepArgs &a, const WsPtrs &w, const sph_config_t &cfg, c
 #define SPH_CELLSORT(P, ...)                                                                                   \
   k_cellsort<__VA_ARGS__><<<nb, kBlock, 0, st>>>(w.perm_tmp, w.keys_sorted, w.cstart, w.refcell, a.n, w.grid,   \
                                                  w.ctrl, w.perm, w.meta, w.tiles, a, P, w.rec0, w.rec1, w.rec2, \
-                                                 w.rec64a, w.rec64b)
+                                                 w.rec64a, w.rec64b, w.orig)
   if (!rp) {
     SPH_CELLSORT(none, kRecNone);
   } else if (cfg.precision == SPH_PREC_MIXED) {

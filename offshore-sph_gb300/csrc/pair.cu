@@ -127,6 +127,7 @@ struct MixedAcc {
 
 struct MixedConsts {
   float KC, r02f, co, alpha, beta, eps, D;
+  float avc;  // alpha c_ij with c_ij = co / 2 (Momentum.py's averaged c, the neighbour's c being 0)
 };
 
 template <int KERNEL>
@@ -140,7 +141,84 @@ __device__ __forceinline__ MixedConsts mixed_consts(const PairParams &pp) {
   c.beta = (float)pp.beta;
   c.eps = (float)pp.eps;
   c.D = (float)pp.D;
+  c.avc = c.alpha * 0.5f * c.co;
   return c;
+}
+
+// Uniform fluid h (the run has a fixed h, Solver(h=...)): every fluid record
+// carries the same FP32 h, so for a fluid query i and a fluid neighbour j,
+// h_ij = 0.5 (h_i + h_j) = h_i exactly, and the averaged h of the viscosity
+// term is h_i as well.  The kernel and viscosity constants are then per
+// query, computed once.
+struct UniformQ {
+  float lim;    // (support h)^2
+  float inv_h;  // 1 / h
+  float al;     // the kernel's normalisation at h
+  float hb2;    // 0.01 h^2 (viscosity denominator)
+};
+
+template <int KERNEL>
+__device__ __forceinline__ UniformQ uniform_q(const MixedConsts &c, float h) {
+  UniformQ u;
+  u.lim = c.KC * (h * h);
+  u.inv_h = __fdividef(1.0f, h);
+  const float fac = KERNEL == SPH_KERNEL_CUBIC ? (float)kCubicFac
+                                               : (KERNEL == SPH_KERNEL_WENDLAND ? (float)kWendFac : (float)kInvPi);
+  u.al = fac * u.inv_h * u.inv_h;
+  u.hb2 = 0.01f * (h * h);
+  return u;
+}
+
+// One FLUID neighbour j of fluid query i under a uniform fluid h (see
+// UniformQ): the same equations as mixed_pair's fluid branch with the
+// per-pair h arithmetic taken out.
+template <int KERNEL, bool XSPH, bool SUMDENS>
+__device__ __forceinline__ void mixed_fluid_uh(MixedAcc &acc, const MixedConsts &c, const UniformQ &u, float hq,
+                                               float4 Qi, float4 Ri, float4 Vi, float4 qj, float4 rj,
+                                               const float4 *vjp) {
+  const float dx = (Qi.x - qj.x) + (Ri.x - rj.x);
+  const float dy = (Qi.y - qj.y) + (Ri.y - rj.y);
+  const float d2 = dx * dx + dy * dy;
+  if (d2 > u.lim) return;
+  const float4 vj = *vjp;
+  const float inv_r = d2 > 0.f ? rsqrtf(d2) : 0.f;
+  const float r = d2 * inv_r;
+  const float q = r * u.inv_h;
+  const float vxij = (Vi.x - vj.x) + (Vi.z - vj.z);
+  const float vyij = (Vi.y - vj.y) + (Vi.w - vj.w);
+  float w, coef;
+  if (KERNEL == SPH_KERNEL_CUBIC) {
+    const float t2 = fmaxf(2.0f - q, 0.f);
+    const bool outer = q > 1.0f;
+    w = XSPH ? (outer ? u.al * 0.25f * (t2 * t2 * t2) : u.al * (1.0f - 1.5f * (q * q) * (1.0f - 0.5f * q))) : 0.f;
+    const float gq = outer ? -0.75f * (t2 * t2) : -3.0f * q * (1.0f - 0.75f * q);
+    coef = r >= 1e-10f ? u.al * gq * u.inv_h * inv_r : 0.f;
+  } else if (KERNEL == SPH_KERNEL_WENDLAND) {
+    const float inner = fmaxf(1.0f - 0.5f * q, 0.f);
+    const float i2 = inner * inner, i5 = i2 * i2 * inner;
+    w = XSPH ? u.al * (i5 * inner) * ((35.0f / 12.0f) * q * q + 3.0f * q + 1.0f) : 0.f;
+    const float gq = i5 * (-14.0f / 3.0f) * q * (1.0f + 2.5f * q);
+    coef = r >= 1e-10f ? u.al * gq * u.inv_h * inv_r : 0.f;
+  } else {
+    const float e = __expf(-q * q);
+    w = u.al * e;
+    coef = r * hq > 1e-12f ? -2.0f * u.al * e * u.inv_h * u.inv_h : 0.f;
+  }
+  const float dwx = coef * dx, dwy = coef * dy;
+  const float mj = qj.w;
+  if (!SUMDENS) acc.fd = fmaf(mj, vxij * dwx + vyij * dwy, acc.fd);
+  const float dot = vxij * dx + vyij * dy;
+  const float ir = __fdividef(2.0f, Ri.z + rj.z);  // 1 / rho_ij
+  const float mu = hq * dot * __fdividef(1.0f, d2 + u.hb2);
+  const float PI = dot < 0.f ? mu * (c.beta * mu - c.avc) * ir : 0.f;
+  const float fac = mj * (Ri.w + rj.w + PI);
+  acc.fax = fmaf(-fac, dwx, acc.fax);
+  acc.fay = fmaf(-fac, dwy, acc.fay);
+  if (XSPH) {
+    const float fx = -c.eps * mj * w * ir;
+    acc.fsx = fmaf(fx, vxij, acc.fsx);
+    acc.fsy = fmaf(fx, vyij, acc.fsy);
+  }
 }
 
 // One candidate j of query i: the exact support test, then continuity,
@@ -214,6 +292,17 @@ __device__ __forceinline__ void mixed_pair(MixedAcc &acc, const MixedConsts &c, 
   }
 }
 
+// One list entry j of query i: with a uniform fluid h (UH), fluid neighbours
+// take the fast path and the rest (boundary particles) the general one.
+template <int KERNEL, bool XSPH, bool SUMDENS, bool UH>
+__device__ __forceinline__ void mixed_entry(MixedAcc &acc, const MixedConsts &c, const UniformQ &u, float4 Qi,
+                                            float4 Ri, float4 Vi, float4 qj, float4 rj, const float4 *vjp) {
+  if (UH && !signbit(qj.z))
+    mixed_fluid_uh<KERNEL, XSPH, SUMDENS>(acc, c, u, Qi.z, Qi, Ri, Vi, qj, rj, vjp);
+  else
+    mixed_pair<KERNEL, XSPH, SUMDENS>(acc, c, Qi, Ri, Vi, qj, rj, vjp);
+}
+
 // Writes the derivatives of particle i (gravity on y) and returns its encoded
 // a^2 for the TimeStep reduction.
 template <bool XSPH, bool SUMDENS>
@@ -253,7 +342,7 @@ struct PairOcc {
 // Global-path evaluation of query slot k (all candidate records read from
 // global memory); returns the encoded a^2 of a fluid query, else the max
 // identity.  lists: the block's per-thread candidate lists.
-template <int KERNEL, bool XSPH, bool SUMDENS, bool MIXED>
+template <int KERNEL, bool XSPH, bool SUMDENS, bool MIXED, bool UH = false>
 __device__ __forceinline__ unsigned long long pair_query(const StepArgs &a, const PairPtrs &P, const PairParams &pp,
                                                          const DevGrid &g, bool filter, long long k,
                                                          unsigned int (*lists)[kPairBlock], int cell0 = 0) {
@@ -288,6 +377,7 @@ __device__ __forceinline__ unsigned long long pair_query(const StepArgs &a, cons
       // accumulators: FP32 (mixed) or FP64
       MixedAcc acc;
       const MixedConsts mc = mixed_consts<KERNEL>(pp);
+      const UniformQ uq = uniform_q<KERNEL>(mc, hif);
       double dd = 0.0, dax = 0.0, day = 0.0, dbx = 0.0, dby = 0.0, dsx = 0.0, dsy = 0.0, dfr = 0.0;
 
       // ---- phase 2: pair physics over the list
@@ -295,7 +385,7 @@ __device__ __forceinline__ unsigned long long pair_query(const StepArgs &a, cons
         for (int t = 0; t < cnt; t++) {
           const unsigned int j = lists[t][tid];
           if (MIXED) {
-            mixed_pair<KERNEL, XSPH, SUMDENS>(acc, mc, Qi, Ri, Vi, P.rec0[j], P.rec1[j], P.rec2 + j);
+            mixed_entry<KERNEL, XSPH, SUMDENS, UH>(acc, mc, uq, Qi, Ri, Vi, P.rec0[j], P.rec1[j], P.rec2 + j);
           } else {
             const double4_32a A = P.r64a[j], B = P.r64b[j];
             const double dx = xi - A.x, dy = yi - A.y;
@@ -440,7 +530,7 @@ __global__ void __launch_bounds__(kPairBlock, PairOcc<MIXED>::blocks)
 // slots), on the global path; the last block resets the list and, when asked,
 // finishes the TimeStep reduction.
 constexpr int kListBlocks = 6;
-template <int KERNEL, bool XSPH, bool SUMDENS>
+template <int KERNEL, bool XSPH, bool SUMDENS, bool UH>
 __global__ void __launch_bounds__(kPairBlock, kListBlocks)
     k_pair_list(StepArgs a, PairPtrs P, PairParams pp, const int2 *__restrict__ fb, double *dt_out,
                 double *dt_hist) {
@@ -454,7 +544,7 @@ __global__ void __launch_bounds__(kPairBlock, kListBlocks)
       const int2 r = fb[e];
       if ((int)threadIdx.x < r.y) {
         const unsigned long long q =
-            pair_query<KERNEL, XSPH, SUMDENS, true>(a, P, pp, g, filter, r.x + threadIdx.x, lists);
+            pair_query<KERNEL, XSPH, SUMDENS, true, UH>(a, P, pp, g, filter, r.x + threadIdx.x, lists);
         ea = q > ea ? q : ea;
       }
     }
@@ -546,12 +636,60 @@ __global__ void __launch_bounds__(kPairBlock) k_sumdens(StepArgs a, PairPtrs P, 
 // ---------------------------------------------------------------------------
 // Neighbour-set export (NNLinkedList.near for every particle, FP64 exact):
 // count pass (idx == nullptr) or fill pass.  Reads the caller's arrays.
+// Each list comes out in the reference's order (NNLinkedList.py:50-78): the
+// 3x3 stencil cells with the x shift outer and the y shift inner, and inside
+// a cell its linked list, head-insert order, i.e. descending index.
 // ---------------------------------------------------------------------------
+// Sort key of member j in the list of a query whose raw reference cell is
+// qref: the stencil position of j's storage cell (an x-overflow particle is
+// stored in the aliased cell), then descending index.  Smaller comes first.
+__device__ __forceinline__ unsigned long long ref_order_key(const int2 *__restrict__ refcell, long long ncx,
+                                                            int2 qref, long long j) {
+  const int2 rc = refcell[j];
+  int sx, sy;
+  storage_cell(rc.x, rc.y, ncx, sx, sy);
+  const unsigned p = (unsigned)((sx - qref.x + 1) * 3 + (sy - qref.y + 1));  // 0..8 for members
+  return ((unsigned long long)p << 32) | (unsigned long long)(0xffffffffu - (unsigned)j);
+}
+
+// insertion sort of idx[0..cnt) (and the parallel arrays, when given) into
+// the reference's order
+__device__ void sort_ref_order(int64_t *idx, double *a0, double *a1, double *a2, long long cnt,
+                               const int2 *__restrict__ refcell, long long ncx, int2 qref) {
+  for (long long s = 1; s < cnt; s++) {
+    const int64_t v = idx[s];
+    const unsigned long long kv = ref_order_key(refcell, ncx, qref, v);
+    double b0 = 0, b1 = 0, b2 = 0;
+    if (a0) {
+      b0 = a0[s];
+      b1 = a1[s];
+      b2 = a2[s];
+    }
+    long long t = s - 1;
+    while (t >= 0 && ref_order_key(refcell, ncx, qref, idx[t]) > kv) {
+      idx[t + 1] = idx[t];
+      if (a0) {
+        a0[t + 1] = a0[t];
+        a1[t + 1] = a1[t];
+        a2[t + 1] = a2[t];
+      }
+      t--;
+    }
+    idx[t + 1] = v;
+    if (a0) {
+      a0[t + 1] = b0;
+      a1[t + 1] = b1;
+      a2[t + 1] = b2;
+    }
+  }
+}
+
 __global__ void __launch_bounds__(kPairBlock)
     k_nn_export(const double *__restrict__ x, const double *__restrict__ y, const double *__restrict__ h,
                 long long n, const int *__restrict__ perm, const int *__restrict__ keys_sorted,
-                const int2 *__restrict__ meta, const unsigned int *__restrict__ cstart,
-                const DevGrid *__restrict__ gp, int64_t *counts, const int64_t *offsets, int64_t *idx) {
+                const int2 *__restrict__ meta, const int2 *__restrict__ refcell,
+                const unsigned int *__restrict__ cstart, const DevGrid *__restrict__ gp, int64_t *counts,
+                const int64_t *offsets, int64_t *idx) {
   const DevGrid g = *gp;
   long long k = (long long)blockIdx.x * blockDim.x + threadIdx.x;
   if (k >= n) return;
@@ -581,16 +719,7 @@ __global__ void __launch_bounds__(kPairBlock)
     counts[i] = cnt;
     return;
   }
-  // ascending order within the list
-  for (long long s = 1; s < cnt; s++) {
-    int64_t v = idx[base + s];
-    long long t = s - 1;
-    while (t >= 0 && idx[base + t] > v) {
-      idx[base + t + 1] = idx[base + t];
-      t--;
-    }
-    idx[base + t + 1] = v;
-  }
+  sort_ref_order(idx + base, nullptr, nullptr, nullptr, cnt, refcell, g.ncx, qref);
 }
 
 // ---------------------------------------------------------------------------
@@ -610,13 +739,11 @@ __global__ void __launch_bounds__(kPairBlock)
 // non-empty tiles the neighbour build writes, the next claim overlapping the
 // current tile.
 // ---------------------------------------------------------------------------
-constexpr int kHaloCellsMax = 144;  // (8 + 2 * 2)^2: 8x8 tiles with a 5x5 stencil
+constexpr int kTileThreads = 256;   // threads of a tile block (8 warps)
+constexpr int kHaloCellsMax = 400;  // (16 + 2 * 2)^2: 16x16 tiles with a 5x5 stencil
 constexpr int kHaloScanPer = (kHaloCellsMax + 31) / 32;
-#ifndef SPH_TILE_BLOCKS
-#define SPH_TILE_BLOCKS 7
-#endif
 #ifndef SPH_HALO_CAP
-#define SPH_HALO_CAP 384
+#define SPH_HALO_CAP 1024
 #endif
 #ifndef SPH_TILE_UNROLL_PAIRS
 #define SPH_TILE_UNROLL_PAIRS 1
@@ -624,12 +751,17 @@ constexpr int kHaloScanPer = (kHaloCellsMax + 31) / 32;
 #ifndef SPH_TILE_UNROLL_CANDS
 #define SPH_TILE_UNROLL_CANDS 2
 #endif
-constexpr int kTileBlocks = SPH_TILE_BLOCKS;
+// resident tile blocks per SM (registers and shared memory allow three for
+// the 32-entry lists of the 2h kernels, two for the Gaussian's 64)
+template <int KERNEL>
+struct TileBlocks {
+  static constexpr int value = ListCap<KERNEL>::value == 32 ? 3 : 2;
+};
 constexpr int kTileUnrollPairs = SPH_TILE_UNROLL_PAIRS;  // ILP over list entries
 constexpr int kTileUnrollCands = SPH_TILE_UNROLL_CANDS;  // ILP over stencil candidates
 constexpr int kHaloCap = SPH_HALO_CAP;  // particles of one halo in shared memory
 static_assert(kHaloCap <= 65535, "list entries are 16-bit");
-static_assert(kHaloCellsMax < 256, "query map entries are 8-bit halo cells");
+static_assert(kHaloCellsMax <= 65535, "query map entries are 16-bit halo cells");
 static_assert(kHaloCap * 48 < (1 << 20), "an mbarrier phase counts fewer than 2^20 bytes");
 
 __device__ __forceinline__ void fb_push(DevCtrl *ctrl, int2 *fb, unsigned int fb_cap, unsigned int s,
@@ -672,9 +804,22 @@ struct TileSync {
   bool abort;  // a staging wait ran out: the block stops
 };
 
-// One tile (see above): stage its halo, run its queries.  Returns this
-// thread's largest encoded a^2 over its queries.  All threads of the block
-// call it together.
+// shared memory of the tile kernels (dynamic: above the 48 KB static limit)
+template <int KERNEL>
+struct TileShared {
+  float4 h0[kHaloCap], h1[kHaloCap], h2[kHaloCap];  // rec0, rec1, rec2 of the halo
+  unsigned short lists[ListCap<KERNEL>::value][kTileThreads];
+  unsigned int hoff[kHaloCellsMax + 1];  // shared-memory offset of each halo cell, then the total
+  unsigned int hgs[kHaloCellsMax];       // its first sorted slot
+  unsigned short qmap[kHaloCap];         // halo cell of each query of the tile
+  unsigned long long bar;                // completion of the staging copies
+  int s_tile[2];                         // this and the next claimed tile (-1: none left)
+  int s_inst[2];                         // their instances (batched form)
+  unsigned long long red[kTileThreads / 32];
+};
+
+// One tile: stage its halo, run its queries.  Returns this thread's largest
+// encoded a^2 over its queries.  All threads of the block call it together.
 //   1. halo table: every halo cell's first sorted slot and count;
 //   2. warp 0: exclusive scan of the counts (shared-memory offsets), then the
 //      halo's records as bulk asynchronous copies, one per contiguous run of
@@ -683,22 +828,29 @@ struct TileSync {
 //      on the block's mbarrier; meanwhile the other threads map each query of
 //      the tile to its halo cell;
 //   3. after the (bounded) wait, each query walks its stencil rows.
-template <int KERNEL, bool XSPH, bool SUMDENS>
+// TSC / WC: the tile shift and stencil half-width as compile-time constants
+// (the own grid's 16x16 tiles with a 5x5 stencil), so that the halo
+// coordinate arithmetic has no integer division; 0 takes them from tg.
+// UH: every fluid particle has the same h (UniformQ).
+template <int KERNEL, bool XSPH, bool SUMDENS, bool UH, int TSC, int WC>
 __device__ __forceinline__ unsigned long long tile_process(const StepArgs &a, const PairPtrs &P, const TileGeom &tg,
-                                                           const MixedConsts &mc, int t, float4 *h0, float4 *h1,
-                                                           float4 *h2, unsigned short (*lists)[kPairBlock],
-                                                           unsigned int *hoff, unsigned int *hgs,
-                                                           unsigned char *qmap, TileSync &sync, DevCtrl *ctrl,
-                                                           int2 *fb, unsigned int fb_cap) {
+                                                           const MixedConsts &mc, int t, TileShared<KERNEL> &sm,
+                                                           TileSync &sync, DevCtrl *ctrl, int2 *fb,
+                                                           unsigned int fb_cap) {
   constexpr int kListCap = ListCap<KERNEL>::value;
   const int tid = threadIdx.x;
-  const int ts = tg.ts, ntlx = tg.ntlx, W = tg.W, T = tg.T, HW = tg.HW, HC = tg.HC;
+  const int ts = TSC ? TSC : tg.ts;
+  const int W = TSC ? WC : tg.W;
+  const int T = 1 << ts, HW = T + 2 * W, HC = HW * HW;
+  const int ntlx = tg.ntlx;
+  float4 *h0 = sm.h0, *h1 = sm.h1, *h2 = sm.h2;
+  unsigned int *hoff = sm.hoff, *hgs = sm.hgs;
   const unsigned int *cst = P.cstart + tg.cell0;  // this grid's cells
   unsigned long long ea = kEncMaxId;
   const unsigned int qs = __ldg(&cst[t << (2 * ts)]), qe = __ldg(&cst[(t + 1) << (2 * ts)]);
   const int ox = (t % ntlx) * T - W, oy = (t / ntlx) * T - W;
   // 1. halo table: counts and first slots
-  for (int c = tid; c < HC; c += kPairBlock) {
+  for (int c = tid; c < HC; c += kTileThreads) {
     const int x = ox + c % HW, y = oy + c / HW;
     unsigned int gs = 0, cnt = 0;
     if (x >= 0 && x < tg.ntx && y >= 0 && y < tg.nty) {
@@ -774,10 +926,10 @@ __device__ __forceinline__ unsigned long long tile_process(const StepArgs &a, co
   }
   // query -> halo cell, for the tile's own cells (their sorted slots are the
   // tile's query range, in cell order)
-  for (int c = tid; c < T * T; c += kPairBlock) {
-    const int hc = (W + c / T) * HW + W + c % T;
+  for (int c = tid; c < T * T; c += kTileThreads) {
+    const int hc = (W + (c >> ts)) * HW + W + (c & (T - 1));
     const unsigned int cnt = hoff[hc + 1] - hoff[hc], base = hgs[hc] - qs;
-    for (unsigned int u = 0; u < cnt; u++) qmap[base + u] = (unsigned char)hc;
+    for (unsigned int u = 0; u < cnt; u++) sm.qmap[base + u] = (unsigned short)hc;
   }
   const uint32_t parity = sync.phase & 1u;
   sync.phase++;
@@ -793,8 +945,8 @@ __device__ __forceinline__ unsigned long long tile_process(const StepArgs &a, co
   // (every |h| <= hmaxf), so that one compare per candidate suffices
   const float SK = (float)Support<KERNEL>::q * 1.000002f;  // support / h, padded
   const unsigned int nq = qe - qs;
-  for (unsigned int q = tid; q < nq; q += kPairBlock) {
-    const int hc = qmap[q];
+  for (unsigned int q = tid; q < nq; q += kTileThreads) {
+    const int hc = sm.qmap[q];
     const int hx = hc % HW, hy = hc / HW;
     const unsigned int k = qs + q;
     const unsigned int sq = hoff[hc] + (k - hgs[hc]);  // the query's own shared-memory slot
@@ -802,18 +954,19 @@ __device__ __forceinline__ unsigned long long tile_process(const StepArgs &a, co
     const float hif = Qi.z;
     if (signbit(hif)) continue;  // queries are fluid
     // an x-overflow alias (reference cells only) or h <= 0: global path
-    if ((tg.W == 1 && P.meta[k].x >= tg.ncx) || !(hif > 0.f)) {
+    if ((W == 1 && P.meta[k].x >= tg.ncx) || !(hif > 0.f)) {
       fb_push(ctrl, fb, fb_cap, k, 1u);
       continue;
     }
     const float4 Ri = h1[sq], Vi = h2[sq];
     const int i = P.perm[k];
+    const UniformQ uq = uniform_q<KERNEL>(mc, hif);
     MixedAcc acc;
     auto physics = [&](int cnt) {
 #pragma unroll kTileUnrollPairs
       for (int u = 0; u < cnt; u++) {
-        const unsigned int j = lists[u][tid];
-        mixed_pair<KERNEL, XSPH, SUMDENS>(acc, mc, Qi, Ri, Vi, h0[j], h1[j], h2 + j);
+        const unsigned int j = sm.lists[u][tid];
+        mixed_entry<KERNEL, XSPH, SUMDENS, UH>(acc, mc, uq, Qi, Ri, Vi, h0[j], h1[j], h2 + j);
       }
     };
     const float hq = 0.5f * (hif + tg.hmaxf);
@@ -837,7 +990,7 @@ __device__ __forceinline__ unsigned long long tile_process(const StepArgs &a, co
         for (; j < ce; j++) {
           const float2 p = *reinterpret_cast<const float2 *>(h0 + j);
           const float dx = Qi.x - p.x, dy = Qi.y - p.y;
-          lists[nl][tid] = (unsigned short)j;
+          sm.lists[nl][tid] = (unsigned short)j;
           nl += (fmaf(dx, dx, dy * dy) <= rq2 && j != sq) ? 1 : 0;
         }
       }
@@ -851,36 +1004,34 @@ __device__ __forceinline__ unsigned long long tile_process(const StepArgs &a, co
 }
 
 // block-wide max of v in thread 0 (all threads call it)
+template <int NT>
 __device__ __forceinline__ unsigned long long block_max_u64(unsigned long long v, unsigned long long *red) {
   const unsigned long long wm = warp_max_u64(v);
   if ((threadIdx.x & 31) == 0) red[threadIdx.x >> 5] = wm;
   __syncthreads();
   unsigned long long b = kEncMaxId;
   if (threadIdx.x == 0)
-    for (int w = 0; w < kPairBlock / 32; w++) b = red[w] > b ? red[w] : b;
+    for (int w = 0; w < NT / 32; w++) b = red[w] > b ? red[w] : b;
   __syncthreads();
   return b;
 }
 
-// shared memory of the tile kernels
-template <int KERNEL>
-struct TileShared {
-  float4 h0[kHaloCap], h1[kHaloCap], h2[kHaloCap];  // rec0, rec1, rec2 of the halo
-  unsigned short lists[ListCap<KERNEL>::value][kPairBlock];
-  unsigned int hoff[kHaloCellsMax + 1];  // shared-memory offset of each halo cell, then the total
-  unsigned int hgs[kHaloCellsMax];       // its first sorted slot
-  unsigned char qmap[kHaloCap];          // halo cell of each query of the tile
-  unsigned long long bar;                // completion of the staging copies
-  int s_tile[2];                         // this and the next claimed tile (-1: none left)
-  int s_inst[2];                         // their instances (batched form)
-  unsigned long long red[kPairBlock / 32];
-};
+// the tile of a single-scene grid with the shape the grid has
+template <int KERNEL, bool XSPH, bool SUMDENS, bool UH>
+__device__ __forceinline__ unsigned long long tile_any(const StepArgs &a, const PairPtrs &P, const TileGeom &tg,
+                                                       const MixedConsts &mc, int t, TileShared<KERNEL> &sm,
+                                                       TileSync &sync, DevCtrl *ctrl, int2 *fb, unsigned int fb_cap) {
+  if (tg.ts == 4 && tg.W == 2)
+    return tile_process<KERNEL, XSPH, SUMDENS, UH, 4, 2>(a, P, tg, mc, t, sm, sync, ctrl, fb, fb_cap);
+  return tile_process<KERNEL, XSPH, SUMDENS, UH, 0, 0>(a, P, tg, mc, t, sm, sync, ctrl, fb, fb_cap);
+}
 
-template <int KERNEL, bool XSPH, bool SUMDENS>
-__global__ void __launch_bounds__(kPairBlock, kTileBlocks)
+template <int KERNEL, bool XSPH, bool SUMDENS, bool UH>
+__global__ void __launch_bounds__(kTileThreads, TileBlocks<KERNEL>::value)
     k_pair_tiles(StepArgs a, PairPtrs P, PairParams pp, const int *__restrict__ tiles, int2 *__restrict__ fb,
                  unsigned int fb_cap) {
-  __shared__ TileShared<KERNEL> sm;
+  extern __shared__ __align__(128) unsigned char smem_raw[];
+  TileShared<KERNEL> &sm = *reinterpret_cast<TileShared<KERNEL> *>(smem_raw);
   const int tid = threadIdx.x;
   DevCtrl *ctrl = P.ctrl;
   const DevGrid *gp = P.grid;
@@ -917,9 +1068,7 @@ __global__ void __launch_bounds__(kPairBlock, kTileBlocks)
         const unsigned int c = atomicAdd(&ctrl->tile_next, 1u);
         sm.s_tile[(it + 1) & 1] = c < ntl ? tiles[c] : -1;
       }
-      const unsigned long long q = tile_process<KERNEL, XSPH, SUMDENS>(a, P, tg, mc, t, sm.h0, sm.h1, sm.h2, sm.lists,
-                                                                        sm.hoff, sm.hgs, sm.qmap, sync, ctrl, fb,
-                                                                        fb_cap);
+      const unsigned long long q = tile_any<KERNEL, XSPH, SUMDENS, UH>(a, P, tg, mc, t, sm, sync, ctrl, fb, fb_cap);
       ea = q > ea ? q : ea;
       if (sync.abort) break;
     }
@@ -927,7 +1076,7 @@ __global__ void __launch_bounds__(kPairBlock, kTileBlocks)
   // this block's max a^2 (the list kernel finishes the TimeStep reduction);
   // the last block resets the tile counter
   if (pp.do_dt) {
-    const unsigned long long ba = block_max_u64(ea, sm.red);
+    const unsigned long long ba = block_max_u64<kTileThreads>(ea, sm.red);
     if (tid == 0 && ba != kEncMaxId) atomicMax(&ctrl->pd_a2max, ba);
   }
   if (tid == 0) {
@@ -942,12 +1091,14 @@ __global__ void __launch_bounds__(kPairBlock, kTileBlocks)
 // ---------------------------------------------------------------------------
 // Batched form: the tile kernel over the (instance, tile) list of all
 // instances, each tile with its instance's grid and constants, and the
-// fallback list with each entry's instance (see nn_build.cu).
+// fallback list with each entry's instance (see nn_build.cu).  Every instance
+// has a fixed h, so the uniform-h form applies.
 // ---------------------------------------------------------------------------
 template <int KERNEL, bool XSPH, bool SUMDENS>
-__global__ void __launch_bounds__(kPairBlock, kTileBlocks)
+__global__ void __launch_bounds__(kTileThreads, TileBlocks<KERNEL>::value)
     k_bt_pair_tiles(StepArgs a, PairPtrs P, BatchPtrs B, int2 *__restrict__ fb, unsigned int fb_cap) {
-  __shared__ TileShared<KERNEL> sm;
+  extern __shared__ __align__(128) unsigned char smem_raw[];
+  TileShared<KERNEL> &sm = *reinterpret_cast<TileShared<KERNEL> *>(smem_raw);
   const int tid = threadIdx.x;
   DevCtrl *ctrl = P.ctrl;
   const unsigned int ntl = ctrl->tl_count;
@@ -989,10 +1140,9 @@ __global__ void __launch_bounds__(kPairBlock, kTileBlocks)
       continue;
     }
     const MixedConsts mc = mixed_consts<KERNEL>(pp);
-    const unsigned long long ea = tile_process<KERNEL, XSPH, SUMDENS>(a, P, tg, mc, t, sm.h0, sm.h1, sm.h2, sm.lists,
-                                                                       sm.hoff, sm.hgs, sm.qmap, sync, ctrl, fb,
-                                                                       fb_cap);
-    const unsigned long long ba = block_max_u64(ea, sm.red);
+    const unsigned long long ea =
+        tile_any<KERNEL, XSPH, SUMDENS, true>(a, P, tg, mc, t, sm, sync, ctrl, fb, fb_cap);
+    const unsigned long long ba = block_max_u64<kTileThreads>(ea, sm.red);
     if (tid == 0 && ba != kEncMaxId) atomicMax(&B.sl[b].pd_a2max, ba);
     if (sync.abort) break;
   }
@@ -1019,8 +1169,8 @@ __global__ void __launch_bounds__(kPairBlock, kListBlocks)
     const bool filter = g.mode == 1 && (g.need_filter || B.sl[b].alias_count > 0);
     unsigned long long ea = kEncMaxId;
     if ((int)threadIdx.x < r.y)
-      ea = pair_query<KERNEL, XSPH, SUMDENS, true>(a, P, pp, g, filter, r.x + threadIdx.x, lists, B.coff[b]);
-    const unsigned long long ba = block_max_u64(ea, red);
+      ea = pair_query<KERNEL, XSPH, SUMDENS, true, true>(a, P, pp, g, filter, r.x + threadIdx.x, lists, B.coff[b]);
+    const unsigned long long ba = block_max_u64<kPairBlock>(ea, red);
     if (threadIdx.x == 0 && ba != kEncMaxId) atomicMax(&B.sl[b].pd_a2max, ba);
   }
   if (threadIdx.x == 0) {
@@ -1063,8 +1213,9 @@ __global__ void __launch_bounds__(kPairBlock)
     k_nn_probe(const double *__restrict__ px, const double *__restrict__ py, const double *__restrict__ ph,
                long long np, const double *__restrict__ x, const double *__restrict__ y,
                const double *__restrict__ h, const int *__restrict__ perm, const int2 *__restrict__ meta,
-               const unsigned int *__restrict__ cstart, const DevGrid *__restrict__ gp, int64_t *counts,
-               const int64_t *offsets, int64_t *idx, double *hij_out, double *q_out, double *r_out) {
+               const int2 *__restrict__ refcell, const unsigned int *__restrict__ cstart,
+               const DevGrid *__restrict__ gp, int64_t *counts, const int64_t *offsets, int64_t *idx,
+               double *hij_out, double *q_out, double *r_out) {
   const DevGrid g = *gp;
   const long long k = (long long)blockIdx.x * blockDim.x + threadIdx.x;
   if (k >= np) return;
@@ -1097,22 +1248,7 @@ __global__ void __launch_bounds__(kPairBlock)
     counts[k] = cnt;
     return;
   }
-  for (long long s = 1; s < cnt; s++) {  // ascending particle index
-    const int64_t v = idx[base + s];
-    const double a0 = hij_out[base + s], a1 = q_out[base + s], a2 = r_out[base + s];
-    long long t = s - 1;
-    while (t >= 0 && idx[base + t] > v) {
-      idx[base + t + 1] = idx[base + t];
-      hij_out[base + t + 1] = hij_out[base + t];
-      q_out[base + t + 1] = q_out[base + t];
-      r_out[base + t + 1] = r_out[base + t];
-      t--;
-    }
-    idx[base + t + 1] = v;
-    hij_out[base + t + 1] = a0;
-    q_out[base + t + 1] = a1;
-    r_out[base + t + 1] = a2;
-  }
+  sort_ref_order(idx + base, hij_out + base, q_out + base, r_out + base, cnt, refcell, g.ncx, qref);
 }
 
 // rho = sum_fluid m_j W(r_j, hk) / sum_{fluid, rho_j >= 1e-3} W(r_j, hk) m_j / rho_j over
@@ -1158,8 +1294,9 @@ __global__ void __launch_bounds__(kPairBlock)
 void launch_nn_probe(const StepArgs &a, const WsPtrs &w, long long np, const double *px, const double *py,
                      const double *ph, int64_t *counts, const int64_t *offsets, int64_t *idx, double *hij, double *q,
                      double *r, cudaStream_t st) {
-  k_nn_probe<<<nblocks(np, kPairBlock), kPairBlock, 0, st>>>(px, py, ph, np, a.x, a.y, a.h, w.perm, w.meta, w.cstart,
-                                                              w.grid, counts, offsets, idx, hij, q, r);
+  k_nn_probe<<<nblocks(np, kPairBlock), kPairBlock, 0, st>>>(px, py, ph, np, a.x, a.y, a.h, w.perm, w.meta,
+                                                              w.refcell, w.cstart, w.grid, counts, offsets, idx,
+                                                              hij, q, r);
 }
 
 void launch_probe_density(const StepArgs &a, const WsPtrs &w, int kernel, long long np, const double *px,
@@ -1214,16 +1351,40 @@ int sm_count() {
   return cache[dev];
 }
 
+// Dynamic shared memory of a tile kernel instantiation: allowed above 48 KB
+// once per device (the attribute is per kernel and device).
+template <typename K>
+static size_t tile_smem(K kern, size_t bytes) {
+  static bool done[64] = {false};
+  int dev = 0;
+  cudaGetDevice(&dev);
+  if (dev >= 0 && dev < 64 && !done[dev]) {
+    cudaFuncSetAttribute(kern, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)bytes);
+    done[dev] = true;
+  }
+  return bytes;
+}
+
+template <int KERNEL, bool XSPH, bool SUMDENS, bool UH>
+static void mixed_pair_launch(const StepArgs &a, const WsPtrs &w, const PairParams &pp, double *dt_out,
+                              double *dt_hist, cudaStream_t st) {
+  // persistent tile kernel, then the global path over what it left
+  const int sms = sm_count();
+  auto tk = k_pair_tiles<KERNEL, XSPH, SUMDENS, UH>;
+  const size_t smem = tile_smem(tk, sizeof(TileShared<KERNEL>));
+  tk<<<sms * TileBlocks<KERNEL>::value, kTileThreads, smem, st>>>(a, pair_ptrs(w), pp, w.tiles, w.fb,
+                                                                   (unsigned)w.fb_cap);
+  k_pair_list<KERNEL, XSPH, SUMDENS, UH><<<sms * kListBlocks, kPairBlock, 0, st>>>(a, pair_ptrs(w), pp, w.fb,
+                                                                                    dt_out, dt_hist);
+}
+
 template <int KERNEL, bool XSPH, bool SUMDENS>
 static void pair_dispatch(const StepArgs &a, const WsPtrs &w, const sph_config_t &cfg, const PairParams &pp,
                           double *dt_out, double *dt_hist, cudaStream_t st) {
   if (cfg.precision == SPH_PREC_MIXED) {
-    // persistent tile kernel, then the global path over what it left
-    const int sms = sm_count();
-    k_pair_tiles<KERNEL, XSPH, SUMDENS><<<sms * kTileBlocks, kPairBlock, 0, st>>>(a, pair_ptrs(w), pp, w.tiles,
-                                                                                   w.fb, (unsigned)w.fb_cap);
-    k_pair_list<KERNEL, XSPH, SUMDENS><<<sms * kListBlocks, kPairBlock, 0, st>>>(a, pair_ptrs(w), pp, w.fb,
-                                                                                          dt_out, dt_hist);
+    // a fixed h makes every fluid record's h the same (the uniform-h form)
+    if (cfg.h_fixed > 0.0) mixed_pair_launch<KERNEL, XSPH, SUMDENS, true>(a, w, pp, dt_out, dt_hist, st);
+    else mixed_pair_launch<KERNEL, XSPH, SUMDENS, false>(a, w, pp, dt_out, dt_hist, st);
   } else {
     // one query per thread; below a few blocks per SM, one-warp blocks so
     // that the FP64-bound work spreads evenly over the SMs
@@ -1271,21 +1432,22 @@ void launch_sumdens(const StepArgs &a, const WsPtrs &w, const sph_config_t &cfg,
 void launch_nn_count(const StepArgs &a, const WsPtrs &w, int64_t *counts, const int64_t *offsets, int64_t *idx,
                      cudaStream_t st) {
   k_nn_export<<<nblocks(a.n, kPairBlock), kPairBlock, 0, st>>>(a.x, a.y, a.h, a.n, w.perm, w.keys_sorted, w.meta,
-                                                               w.cstart, w.grid, counts, offsets, idx);
+                                                               w.refcell, w.cstart, w.grid, counts, offsets, idx);
 }
 
 template <int KERNEL, bool XSPH, bool SUMDENS>
 static void bt_pair_dispatch(const StepArgs &a, const WsPtrs &w, const BatchPtrs &B, int tile_blocks,
                              cudaStream_t st) {
   const int sms = sm_count();
-  k_bt_pair_tiles<KERNEL, XSPH, SUMDENS><<<sms * tile_blocks, kPairBlock, 0, st>>>(a, pair_ptrs(w), B, w.fb,
-                                                                                   (unsigned)w.fb_cap);
+  if (tile_blocks < 1 || tile_blocks > TileBlocks<KERNEL>::value) tile_blocks = TileBlocks<KERNEL>::value;
+  auto tk = k_bt_pair_tiles<KERNEL, XSPH, SUMDENS>;
+  const size_t smem = tile_smem(tk, sizeof(TileShared<KERNEL>));
+  tk<<<sms * tile_blocks, kTileThreads, smem, st>>>(a, pair_ptrs(w), B, w.fb, (unsigned)w.fb_cap);
   k_bt_pair_list<KERNEL, XSPH, SUMDENS><<<sms * kListBlocks, kPairBlock, 0, st>>>(a, pair_ptrs(w), B, w.fb);
 }
 
 void launch_bt_pair(const StepArgs &a, const WsPtrs &w, const BatchPtrs &B, int kernel, bool xsph, int tile_blocks,
                     cudaStream_t st) {
-  if (tile_blocks < 1 || tile_blocks > kTileBlocks) tile_blocks = kTileBlocks;
   (void)xsph;  // the batched form has no XSPH
   if (kernel == SPH_KERNEL_CUBIC) bt_pair_dispatch<SPH_KERNEL_CUBIC, false, false>(a, w, B, tile_blocks, st);
   else if (kernel == SPH_KERNEL_WENDLAND) bt_pair_dispatch<SPH_KERNEL_WENDLAND, false, false>(a, w, B, tile_blocks, st);

@@ -25,7 +25,7 @@ constexpr int kScanTile = 4096;  // cells per scan tile (1024 threads x 4, one u
 #define SPH_TILE_SHIFT_REF 2
 #endif
 #ifndef SPH_TILE_SHIFT_OWN
-#define SPH_TILE_SHIFT_OWN 3
+#define SPH_TILE_SHIFT_OWN 4
 #endif
 
 // ---------------------------------------------------------------------------
@@ -192,11 +192,15 @@ struct DevGrid {
 };
 
 // Byte offsets of the workspace regions (computed on the host).
+// total: what every entry point needs; total_shadow adds the sorted copy of
+// the state that sph_run steps on when the workspace has room for it.
 struct WsLayout {
   size_t ctrl, grid, keys, refcell, crank, perm_tmp, keys_sorted, perm, meta, counts, cstart, scan_part, rec0,
       rec1, rec2, rec64a, rec64b, fb, tiles, total;
+  size_t shadow, shadow_label, shadow_orig, total_shadow;
   long long n_cap, max_cells, n_parts, fb_cap;
 };
+constexpr int kStateFields = 19;  // the FP64 fields of particle_dtype
 
 WsLayout make_layout(long long n_cap, long long max_cells);
 
@@ -315,6 +319,14 @@ struct WsPtrs {
   int2 *fb;  // fallback list of the tile pair kernel: (first slot, count <= 128)
   int *tiles;  // non-empty tiles of the current build, in no particular order
   long long n_cap, max_cells, n_parts, fb_cap;
+  // The sorted copy of the state (when the workspace has room): kStateFields
+  // arrays of n_cap doubles, the labels, and each copy index's caller index.
+  double *shadow;
+  int8_t *shadow_label;
+  int *shadow_orig;
+  // set while a run steps on the copy: the in-cell order ranks particles by
+  // their caller index orig[i] instead of their index i (null: by i)
+  const int *orig;
 };
 
 WsPtrs ws_ptrs(const sph_workspace_t *ws);

@@ -4,7 +4,9 @@
 (``src/Common.py:26-57``): the same names, order and types (154 bytes, packed),
 so that arrays built for the reference load here unchanged and results can be
 handed back in the reference's format.  ``ParticleType`` mirrors
-``src/Common.py:8-12``.
+``src/Common.py:8-12``; ``computed_dtype`` is the reference's per-neighbour
+block record (``src/Common.py:60-98``) that the per-block plugin methods of a
+Method take.
 """
 import enum
 
@@ -36,3 +38,10 @@ particle_dtype = np.dtype({
 })
 
 assert particle_dtype.itemsize == 154
+
+#: one neighbour of a particle as _assignProps fills it
+#: (src/Tools/SolverTools.py:74-104): the argument of Method.compute_* per block
+computed_dtype = np.dtype({
+    "names": ["label", "m", "p", "rho", "h", "q", "c", "r", "w", "dw_x", "dw_y", "x", "y", "vx", "vy"],
+    "formats": [np.int8] + [np.float64] * 14,
+})

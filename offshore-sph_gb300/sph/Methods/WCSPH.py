@@ -3,10 +3,12 @@
 Same constructor and attributes as the reference (height, rho0, useXSPH,
 useSummationDensity, epsilon, gamma, co, B, Pb, alpha, beta, r0, D, p1, p2);
 the attributes stay assignable, as on the reference's jitclass, and are read
-at every device call.  The per-particle methods run on the device; the
+at every device call.  The per-particle methods run on the device.  The
 per-neighbour-block methods (compute_density_change, compute_acceleration,
-compute_velocity) are fused into the device pair kernel and are not offered
-as separate host calls.
+compute_velocity) take the reference's arguments -- one particle and its
+neighbours as a computed_dtype block -- and evaluate the block on the device
+(sph_block_equations); the step itself runs the same equations fused in its
+pair kernels.
 """
 import math
 
@@ -70,14 +72,26 @@ class WCSPH(Method):
         """co for every particle (WCSPH.py:110-129)."""
         return np.full(len(pA), self.co, dtype=np.float64)
 
-    def compute_density_change(self, p, comp):
-        raise NotImplementedError("continuity is evaluated inside the fused device pair kernel; "
-                                  "use Solver._compute or sph.core.compute")
+    def _block(self, p, comp):
+        return core.block_equations(comp, p, self.wcsph_struct())
 
     def compute_acceleration(self, p, comp):
-        raise NotImplementedError("momentum is evaluated inside the fused device pair kernel; "
-                                  "use Solver._compute or sph.core.compute")
+        """Momentum with artificial viscosity, then gravity (WCSPH.py:151-169,
+        src/Equations/Momentum.py:5-57): [a_x, a_y - 9.81]."""
+        out = self._block(p, comp)
+        return [float(out[1]), float(out[2]) - 9.81]
 
     def compute_velocity(self, p, comp):
-        raise NotImplementedError("XSPH is evaluated inside the fused device pair kernel; "
-                                  "use Solver._compute or sph.core.compute")
+        """XSPH (WCSPH.py:171-189, src/Equations/XSPH.py:5-31):
+        [vx, vy, vx + xsph_x, vy + xsph_y] with XSPH, else [vx, vy, 0, 0]."""
+        if self.useXSPH:
+            out = self._block(p, comp)
+            return [float(p["vx"]), float(p["vy"]), float(p["vx"]) + float(out[5]), float(p["vy"]) + float(out[6])]
+        return [float(p["vx"]), float(p["vy"]), 0.0, 0.0]
+
+    def compute_density_change(self, p, comp):
+        """Continuity (WCSPH.py:191-203, src/Equations/Continuity.py:4-16), or
+        0 with summation density."""
+        if self.useSummationDensity:
+            return 0.0
+        return float(self._block(p, comp)[0])

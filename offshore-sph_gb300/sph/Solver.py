@@ -10,9 +10,15 @@ arithmetic over FP64 state) and ``device``.
 run() follows the reference's loop (Solver.py:346-475): a settling phase with
 damping until the kinetic energy drops below kE times its initial value (or
 maxSettle steps, or customSettle), then the temporary boundary is removed,
-damping switches off and time advances.  step(n) runs n bare steps (dt ->
-predict -> _compute -> correct) without settling or storage, all on the
-device.
+damping switches off and time advances.  Without a coupling function every
+step is one device call of the step body (dt -> predict -> _compute ->
+correct, sph_run).  Once settled, steps run in chunks with one host
+synchronisation per chunk: the dt history and the export properties of every
+step stay on the device until the chunk ends and come down together.  A
+chunk that would pass the end of the run is rolled back to a device snapshot
+and re-run to the exact step, so the steps taken are the reference's.  With
+a coupling function (user Python on the host array) every step synchronises.
+step(n) runs n bare steps without settling or storage.
 """
 import math
 import sys
@@ -64,6 +70,7 @@ class Solver:
                                              "compute", "time_step", "neighbour_hood", "coupling")}
         self._dp = None
         self._ws = None
+        self._chunk_max = 64  # settled steps per host synchronisation
 
     # ------------------------------------------------------------------ state
     def addParticles(self, particles):
@@ -172,6 +179,9 @@ class Solver:
         self.settled = False
         dt_dev = torch.zeros(1, dtype=torch.float64, device=self.device)
         while self.t < self.duration:
+            if self.coupling is None:
+                t_step = self._device_steps(t_step)
+                continue
             if self.timeStep is None:
                 self.dt = self._minTimeStep()
             else:
@@ -219,6 +229,92 @@ class Solver:
         self._download()
         self.timing_data["total"] = perf_counter() - start_all
         self.t_step = t_step
+
+    # ------------------------------------------------------ device-side loop
+    def _chunk_steps(self, t_step):
+        """Steps of the next settled chunk: up to _chunk_max, ending at the
+        next incremental write-out, and no more than the remaining time
+        allows at the last dt (a chunk that still overshoots is rolled
+        back)."""
+        k = self._chunk_max
+        if self.incrementalWriteout:
+            k = min(k, self.incrementalFreq - t_step % self.incrementalFreq)
+        if self.dt_a and self.dt_a[-1] > 0:
+            k = min(k, max(1, int(0.9 * (self.duration - self.t) / self.dt_a[-1])))
+        return max(1, k)
+
+    def _device_steps(self, t_step):
+        """One settling step, or one chunk of settled steps, of run()'s loop
+        body on the device (no coupling function).  Returns the new t_step."""
+        wc = self.method.wcsph_struct()
+        cfg = self._cfg()
+        need = [k for k in self.exportProperties if k in FLOAT_FIELDS]
+        k = self._chunk_steps(t_step) if self.settled else 1
+        snap = self._dp._buf.clone() if (self.settled and k > 1) else None
+        taken = k
+        for attempt in range(2):
+            hist = torch.zeros((taken, 3), dtype=torch.float64, device=self.device)
+            exp = torch.empty((taken, len(need), self._dp.n), dtype=torch.float64, device=self.device) \
+                if need else None
+            start = perf_counter()
+            for s in range(taken):
+                core.run(self._dp, wc, cfg, self._ws, 1, hist[s])
+                if exp is not None:
+                    for j, key in enumerate(need):
+                        exp[s, j].copy_(self._dp.fields[key])
+            h = hist.cpu().numpy()  # the chunk's one synchronisation
+            self.timing_data["compute"] += perf_counter() - start
+            self._ws.check()
+            if not self.settled:
+                break
+            # the reference's loop takes step s only while t < duration
+            t, run_steps = self.t, taken
+            for s in range(taken):
+                if t >= self.duration:
+                    run_steps = s
+                    break
+                t += float(h[s, 0])
+            if run_steps == taken:
+                break
+            self._dp._buf.copy_(snap)  # roll back, then take exactly the steps the reference takes
+            taken = run_steps
+        start = perf_counter()
+        ex = exp.cpu().numpy() if exp is not None else None
+        idx = np.nonzero(self.indexes)[0]
+        for s in range(taken):
+            self.dt_a.append(float(h[s, 0]))
+            self.dt = float(h[s, 0])
+            if self.timeStep is None:
+                self.dt_c.append(float(h[s, 1]))
+                self.dt_f.append(float(h[s, 2]))
+                if h[s, 0] < 1e-6:
+                    self.ts_error = len(self.dt_a) - 1
+            for key in self.exportProperties:
+                full = np.array(self.particleArray[key], copy=True)
+                if key in need:
+                    full[idx] = ex[s, need.index(key)]
+                self.export[key].append(full)
+            if self.settled:
+                self.t += self.dt
+            if self.incrementalWriteout and (t_step + s) % self.incrementalFreq == 0:
+                self._download()
+                self.data = [self.particleArray.copy()]
+                self.save("{0}-{1}.hdf5".format(self.incrementalFile, t_step + s), printLocation=False)
+        self.timing_data["storage"] += perf_counter() - start
+        t_step += taken
+        if not self.settled and t_step > 1:
+            ke, cs = 1e12, False
+            if self.customSettle is None:
+                ke = self._kinetic_energy()
+            else:
+                self._download()
+                cs = self.customSettle(self.particleArray, self)
+            if (ke < self.kE) or (t_step > self.maxSettle) or cs:
+                if t_step > self.maxSettle:
+                    print("\nWARNING! Maximum settle steps reached, check configuration, maybe increase "
+                          "spacing between wall and particles.")
+                self._settle()
+        return t_step
 
     def _coupled_update(self, dt_dev, predict):
         """couplingIntegrator.predict / correct of the Coupled particles

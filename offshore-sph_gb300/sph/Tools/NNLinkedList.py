@@ -3,10 +3,11 @@
 update(pA) builds the device cell table (a counting sort over cell ids
 instead of linked lists); near(i, pA) and nearPos(x, y, h, pA) return the
 reference's (h_ij, q, r, nbrs) for one point; neighbour_sets() returns every
-particle's list at once (CSR).  The sets equal the reference's bit for bit,
-including its 3x3-cell stencil truncation and its x-overflow cell aliasing;
-the order inside a list is ascending index (the reference returns
-head-insert order)."""
+particle's list at once (CSR).  The lists equal the reference's bit for bit
+and in its order (stencil cells with the x shift outer and the y shift
+inner, descending index inside a cell: the head-insert order of its linked
+lists), including its 3x3-cell stencil truncation and its x-overflow cell
+aliasing."""
 import numpy as np
 import torch
 

@@ -10,7 +10,7 @@ Drop-in classes with the reference's names and constructors:
 Every stage of the step runs in libsph_gb300.so (CUDA, sm_103a) through its C
 ABI (include/sph_gb300.h); there is no CPU fallback.
 """
-from .Common import ParticleType, particle_dtype, get_label_code
+from .Common import ParticleType, computed_dtype, particle_dtype, get_label_code
 from .Methods.WCSPH import WCSPH
 from .Kernels.CubicSpline import CubicSpline
 from .Kernels.Gaussian import Gaussian
@@ -23,5 +23,5 @@ from .Tools.NNLinkedList import NNLinkedList
 from .Equations.TimeStep import TimeStep
 from .Solver import Solver
 
-__all__ = ["ParticleType", "particle_dtype", "get_label_code", "WCSPH", "CubicSpline", "Gaussian", "Wendland", "PEC",
+__all__ = ["ParticleType", "computed_dtype", "particle_dtype", "get_label_code", "WCSPH", "CubicSpline", "Gaussian", "Wendland", "PEC",
            "Euler", "Verlet", "NewmarkBeta", "NNLinkedList", "TimeStep", "Solver"]

@@ -47,6 +47,14 @@ class Particles(C.Structure):
     _fields_ = [("n", C.c_int64), ("label", C.c_void_p)] + [(k, C.c_void_p) for k in FIELDS]
 
 
+BLOCK_ARRAYS = ("m", "p", "rho", "h", "c", "r", "w", "dw_x", "dw_y", "x", "y", "vx", "vy")
+
+
+class Block(C.Structure):
+    """sph_block_t: one neighbour block in computed_dtype layout (device)."""
+    _fields_ = [("n", C.c_int64), ("label", C.c_void_p)] + [(k, C.c_void_p) for k in BLOCK_ARRAYS]
+
+
 class Workspace(C.Structure):
     _fields_ = [("ptr", C.c_void_p), ("bytes", C.c_size_t), ("n_cap", C.c_int64), ("max_cells", C.c_int64)]
 
@@ -68,7 +76,8 @@ EXPORTS = ("sph_abi_version", "sph_workspace_size", "sph_default_max_cells", "sp
            "sph_compute_static", "sph_run_wall_load", "sph_adjoint_step", "sph_batch_workspace_size",
            "sph_batch_setup", "sph_batch_instance_cells", "sph_batch_run", "sph_nn_probe_count",
            "sph_nn_probe_export", "sph_probe_density", "sph_newmark_predict", "sph_newmark_correct",
-           "sph_newmark_work_size", "sph_newmark_acceleration", "sph_selftest_staging")
+           "sph_newmark_work_size", "sph_newmark_acceleration", "sph_selftest_staging",
+           "sph_block_equations")
 SPH_ERR_STATIC_LIMIT = 5
 STATIC_MAX_PARTICLES = 32768
 STATIC_MAX_CELLS = 131072
@@ -126,6 +135,7 @@ def load():
         "sph_nn_probe_export": (C.c_int, [PP, WS, C.c_int64, vp, vp, vp, vp, vp, vp, vp, vp, vp]),
         "sph_probe_density": (C.c_int, [PP, WP, C.c_int, WS, C.c_int64, vp, vp, vp, vp, vp, vp, vp]),
         "sph_selftest_staging": (C.c_int, [vp, vp, vp]),
+        "sph_block_equations": (C.c_int, [C.POINTER(Block), C.POINTER(C.c_double), WP, vp, vp]),
         "sph_newmark_predict": (C.c_int, [PP, C.c_double, C.c_double, vp, vp]),
         "sph_newmark_correct": (C.c_int, [PP, C.c_double, C.c_double, vp, vp]),
         "sph_newmark_work_size": (C.c_int, [C.c_int64, C.c_int32, C.c_int32, C.POINTER(C.c_size_t)]),

@@ -18,7 +18,10 @@ replays each segment from its checkpoint, keeping a copy of the workspace
 after every replayed step (its neighbour build and FP64 records), and walks
 the segment in reverse with the hand-written adjoint step
 (``sph_adjoint_step``: the vector-Jacobian product of the fused pair
-evaluation and of PEC), which reuses those builds.
+evaluation and of PEC), which reuses those builds.  ``adjoint_precision``
+"mixed" runs that product's pair arithmetic in FP32 (the mixed form); the
+forward, the checkpoints and the replay stay FP64, so the loss and its
+finite differences are the FP64 ones.
 The initial density is an input held fixed (it is not recomputed from
 perturbed positions), as are h and the boundary particles.
 """
@@ -46,7 +49,7 @@ class WallLoadCase:
     """
 
     def __init__(self, pa, height, r0, h, dt, nsteps, wall_x, checkpoint=20, kernel=L.KERNEL_CUBIC,
-                 rho0=1000.0, device="cuda"):
+                 rho0=1000.0, device="cuda", adjoint_precision="fp64"):
         self.n = len(pa)
         self.nsteps = int(nsteps)
         self.checkpoint = int(checkpoint)
@@ -54,6 +57,10 @@ class WallLoadCase:
         self.wall_x = float(wall_x)
         self.height, self.r0, self.rho0 = float(height), float(r0), float(rho0)
         self.cfg = core.config_struct(kernel=kernel, precision="fp64", h_fixed=h, dt_fixed=dt, cfl_c=0.3)
+        # the adjoint step's own form: "fp64", or "mixed" (FP32 pair arithmetic
+        # in the vector-Jacobian product; the forward stays FP64)
+        self.cfg_adj = core.config_struct(kernel=kernel, precision=adjoint_precision, h_fixed=h, dt_fixed=dt,
+                                          cfl_c=0.3)
         self.fluid = torch.from_numpy(pa["label"] == 0).to(device)
         self.nf = int(self.fluid.sum().item())
         # base state: hydrostatic density and pressure (WCSPH.initialize), fixed h
@@ -162,7 +169,7 @@ class WallLoadLoss(torch.autograd.Function):
             case.ws.check()
             for s in reversed(range(m)):
                 ws_s = L.Workspace(ptr=builds[s].data_ptr(), bytes=w0.bytes, n_cap=w0.n_cap, max_cells=w0.max_cells)
-                L.check(lib.sph_adjoint_step(core._P(case.base), core._P(half), C.byref(wc), C.byref(case.cfg),
+                L.check(lib.sph_adjoint_step(core._P(case.base), core._P(half), C.byref(wc), C.byref(case.cfg_adj),
                                              C.byref(ws_s), C.byref(cs), current_stream()), "sph_adjoint_step")
             del builds
         f = case.fluid

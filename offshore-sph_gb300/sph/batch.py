@@ -127,7 +127,7 @@ class Ensemble:
         return int(self.fluid.sum().item())
 
     # -- autotuning --------------------------------------------------------
-    def autotune(self, shifts=(2, 3), blocks=(5, 6, 7), steps=5, warmup=2):
+    def autotune(self, shifts=(3, 4), blocks=(2, 3), steps=5, warmup=2):
         """Times every (tile shift, resident tile-kernel blocks per SM) pair
         on this ensemble from the current state (restored afterwards) and
         keeps the fastest.  Returns {(shift, blocks): ms per step}."""

@@ -18,14 +18,17 @@ LIBDIR = os.path.join(PKG, "_lib")
 OBJDIR = os.path.join(ROOT, "_build")
 LIB = os.path.join(LIBDIR, "libsph_gb300.so")
 
-SOURCES = ["nn_build.cu", "pair.cu", "integrate.cu", "capi.cu", "static_ws.cu", "adjoint.cu", "batch.cu", "newmark.cu"]
+SOURCES = ["nn_build.cu", "pair.cu", "integrate.cu", "capi.cu", "static_ws.cu", "adjoint.cu", "batch.cu", "newmark.cu",
+           "block.cu"]
 ARCH = ["-gencode", "arch=compute_103a,code=sm_103a"]
 FLAGS = ["-O3", "-std=c++20", "-lineinfo", "-Xcompiler", "-fPIC", "--expt-relaxed-constexpr",
          "-I", INCLUDE, "-I", CSRC]
 # the mixed-form pair arithmetic flushes FP32 denormals: its reciprocals and
 # square roots then take the plain hardware approximations (the FP64 form is
 # unaffected; every FP32 pair operand of a real scene is far from 1e-38)
-SOURCE_FLAGS = {"pair.cu": ["-ftz=true"]}
+# the per-block plugin equations sum without contraction, as the reference's
+# loops do
+SOURCE_FLAGS = {"pair.cu": ["-ftz=true"], "block.cu": ["-fmad=false"]}
 
 
 def nvcc():

@@ -117,7 +117,8 @@ def nn_update(dp, cfg, ws):
 
 def nn_export(dp, cfg, ws):
     """Neighbour lists of the last nn_update: (offsets[n+1], idx) as numpy
-    int64, each list ascending."""
+    int64, each list in the reference's order (stencil cells x shift outer,
+    y shift inner; descending index inside a cell)."""
     lib = L.load()
     counts = torch.zeros(dp.n, dtype=torch.int64, device=dp.device)
     L.check(lib.sph_nn_count(_P(dp), C.byref(cfg), C.byref(ws.ws), counts.data_ptr(), current_stream()),
@@ -140,7 +141,8 @@ def _dev(v, n=None):
 
 def nn_probe(dp, ws, px, py, ph):
     """NNLinkedList.nearPos for many points on the table of the last build:
-    (offsets[np+1], idx, h_ij, q, r) as numpy, each list ascending."""
+    (offsets[np+1], idx, h_ij, q, r) as numpy, each list in the reference's
+    order."""
     lib = L.load()
     px = _dev(px)
     n = px.numel()
@@ -172,6 +174,24 @@ def probe_density(dp, wc, kernel, ws, px, py, h_search, h_kernel):
                                        py.data_ptr(), hs.data_ptr(), hk.data_ptr(), rho.data_ptr(), p.data_ptr(),
                                        current_stream()), "sph_probe_density")
     return rho, p
+
+
+def block_equations(comp, p, wc):
+    """The per-block equations of one particle on the device
+    (sph_block_equations): comp is a computed_dtype array (host), p the
+    particle (a particle_dtype record or a mapping with p, rho, h, c).
+    Returns the 7 sums (continuity, momentum x, y without gravity, boundary
+    force x, y, XSPH x, y) as a numpy array."""
+    n = len(comp)
+    arrs = {k: torch.as_tensor(np.ascontiguousarray(comp[k], dtype=np.float64), device="cuda")
+            for k in L.BLOCK_ARRAYS}
+    lab = torch.as_tensor(np.ascontiguousarray(comp["label"], dtype=np.int8), device="cuda")
+    blk = L.Block(n=n, label=lab.data_ptr(), **{k: v.data_ptr() for k, v in arrs.items()})
+    self4 = (C.c_double * 4)(float(p["p"]), float(p["rho"]), float(p["h"]), float(p["c"]))
+    out = torch.zeros(7, dtype=torch.float64, device="cuda")
+    L.check(L.load().sph_block_equations(C.byref(blk), self4, C.byref(wc), out.data_ptr(), current_stream()),
+            "sph_block_equations")
+    return out.cpu().numpy()
 
 
 def kernel_eval(kernel, r, h):

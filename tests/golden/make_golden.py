@@ -291,11 +291,11 @@ def gen_probes(ref):
     offs, idx, hijs, qs, rs, rhos, ps = [0], [], [], [], [], [], []
     for x, y in zip(px, py):
         hij, q, r, nb = nn.nearPos(float(x), float(y), h, pA)
-        order = np.argsort(nb)
-        idx.extend(nb[order].tolist())
-        hijs.extend(np.asarray(hij)[order].tolist())
-        qs.extend(np.asarray(q)[order].tolist())
-        rs.extend(np.asarray(r)[order].tolist())
+        # the reference's own order (stencil cells, head-insert order inside)
+        idx.extend(np.asarray(nb).tolist())
+        hijs.extend(np.asarray(hij).tolist())
+        qs.extend(np.asarray(q).tolist())
+        rs.extend(np.asarray(r).tolist())
         offs.append(len(idx))
         w = CubicSpline.evaluate(np.asarray(r, dtype=np.float64), np.ones(len(nb)) * h)
         wt = Shepard(w, pA[nb]["label"], pA[nb]["m"], pA[nb]["rho"])
@@ -384,6 +384,38 @@ def gen_coupled_run(ref):
           **{"final_" + k: np.array(fin[k]) for k in fin.dtype.names},
           export_y=np.array(solver.export["y"]))
     print("  solver_coupled: %.1f s, %d steps" % (time.time() - t0, len(solver.dt_a)))
+
+
+def gen_plain_run(ref):
+    """Solver.run of the small tank with a temporary gate, no coupling:
+    settling (damping 0.05) ended by customSettle after three steps, the
+    gate deleted, then Courant/force dt steps to the duration."""
+    from src.Solver import Solver
+    from src.Methods.WCSPH import WCSPH
+    from src.Kernels.CubicSpline import CubicSpline
+    from src.Integrators.PEC import PEC
+    from sph import scenarios as S
+    sys.path.insert(0, os.path.dirname(HERE))
+    import sphcases as SC
+    pa, dx = SC.plain_run_case(S)
+    method = WCSPH(height=0.4, r0=dx, rho0=1000.0, useXSPH=False, Pb=0.0, useSummationDensity=False)
+    solver = Solver(method, PEC(False, True), CubicSpline(), SC.PLAIN_RUN["duration"], incrementalWriteout=False,
+                    h=1.3 * dx, customSettle=SC.settle_after_three, exportProperties=["x", "y", "p"])
+    Solver.particleArray = None
+    solver.particleArray = None
+    solver.addParticles(pa.copy())
+    t0 = time.time()
+    solver.setup()
+    init = solver.particleArray.copy()
+    solver.run()
+    fin = solver.particleArray
+    _save("solver_plain.npz", dt_a=np.array(solver.dt_a), dt_c=np.array(solver.dt_c), dt_f=np.array(solver.dt_f),
+          t=solver.t, settleTime=solver.settleTime, t_step=solver.t_step,
+          **{"init_" + k: np.array(init[k]) for k in init.dtype.names},
+          **{"final_" + k: np.array(fin[k]) for k in fin.dtype.names},
+          export_x=np.array(solver.export["x"])[::SC.PLAIN_RUN["export_every"]],
+          export_p=np.array(solver.export["p"])[::SC.PLAIN_RUN["export_every"]])
+    print("  solver_plain: %.1f s, %d steps" % (time.time() - t0, len(solver.dt_a)))
 
 
 def _nn_case(name, pa, scale=2.0):
@@ -579,7 +611,7 @@ def main():
     _install_shims()
     sys.path.insert(0, a.ref)
     gens = dict(kernels=gen_kernels, equations=gen_equations, eos=gen_eos_integrators, nn=gen_nn, extra=gen_extra, probes=gen_probes,
-                newmark=gen_newmark)
+                newmark=gen_newmark, plain_run=gen_plain_run)
     for k, g in gens.items():
         if a.only and k not in a.only.split(","):
             continue

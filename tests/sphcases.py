@@ -128,3 +128,28 @@ def settle_now(pA, solver):
     as the loop length over the fluid-only array, which plain Python rejects
     when boundaries exist)."""
     return True
+
+
+# ---------------------------------------------------------------------------
+# Plain Solver.run case: the small tank with a temporary wall that the end of
+# settling removes (the dam-break example's gate, examples/DamBreak.py:31)
+# ---------------------------------------------------------------------------
+PLAIN_RUN = dict(dx=0.025, duration=0.02, settle_steps=3, export_every=50)  # exports kept: every 50th step
+
+
+def plain_run_case(S):
+    """(particles, dx) of the plain run: the small tank plus 12 TempBoundary
+    particles just right of the column."""
+    dx = PLAIN_RUN["dx"]
+    tank = S.dam_break(width=0.2, height=0.4, dx=dx, tank_width=0.8, tank_height=0.6)
+    gate = np.zeros(12, dtype=tank.dtype)
+    gate["label"] = 2
+    gate["x"] = 0.21 + 0.0125
+    gate["y"] = (np.arange(12) + 0.5) * 0.0125 * 2
+    return np.concatenate((tank, gate)), dx
+
+
+def settle_after_three(pA, solver):
+    """customSettle: end the settling once three steps have run."""
+    return len(solver.dt_a) >= PLAIN_RUN["settle_steps"]
+

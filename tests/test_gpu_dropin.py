@@ -160,8 +160,6 @@ def test_wcsph_pressure_and_initialize(sph):
     assert SC.rel_err(m2.compute_pressure(pa), z["p_pb"]) <= 1e-13
     out = m.initialize(pa.copy())
     assert SC.rel_err(out["rho"], z["rho_height"]) <= 1e-13
-    with pytest.raises(NotImplementedError):
-        m.compute_acceleration(pa[0], None)
 
 
 def test_linked_list_matches_brute_force(sph):
@@ -179,8 +177,28 @@ def test_linked_list_matches_brute_force(sph):
     assert np.all(q <= 3.0)
     z = SC.load("nn_grid26")
     off, idx = nn.neighbour_sets()
-    for i in range(len(pa)):
-        assert set(idx[off[i]:off[i + 1]].tolist()) == set(z["idx"][z["offsets"][i]:z["offsets"][i + 1]].tolist())
+    assert np.array_equal(off, z["offsets"]) and np.array_equal(idx, z["idx"])  # the reference's order too
+
+
+def test_near_returns_the_reference_lists_in_order(sph):
+    """NNLinkedList.near(i) (src/Tools/NNLinkedList.py:41-84) on the tank:
+    nbrs in the reference's order (stencil cells with the x shift outer,
+    descending index inside a cell) and the same h_ij, q, r, against the
+    oracle's restatement of the reference."""
+    import oracle
+    from sph import scenarios as S
+    pa = S.dam_break(width=0.2, height=0.4, dx=0.025, tank_width=0.8, tank_height=0.6)
+    pa["h"][pa["label"] == 0] = 1.3 * 0.025
+    nn = sph.NNLinkedList(2.0)
+    nn.update(pa)
+    ref = oracle.NN(2.0)
+    ref.update(pa["x"], pa["y"], pa["h"])
+    for i in (0, 1, 17, 40, len(pa) // 2, len(pa) - 1):
+        hij, q, r, nb = nn.near(i, pa)
+        rh, rq, rr, rn = ref.near(float(pa["x"][i]), float(pa["y"][i]), float(pa["h"][i]))
+        assert nb.dtype == np.uint64
+        assert np.array_equal(nb.astype(np.int64), rn), i
+        assert np.array_equal(hij, rh) and np.array_equal(r, rr) and np.array_equal(q, rq), i
 
 
 def _tank(sph, dx=0.025):
@@ -321,3 +339,85 @@ def test_solver_coupled_run_matches_reference(sph):
     for k in ("x", "y", "vx", "vy", "ay"):
         assert SC.rel_err(fin[k][c], z["final_" + k][c]) <= 1e-8, k
     assert SC.rel_err(np.array(solver.export["y"]), z["export_y"]) <= 1e-8
+
+
+def test_per_block_method_calls_match_reference(sph):
+    """WCSPH.compute_density_change / compute_acceleration / compute_velocity
+    on one particle and a computed_dtype block (src/Methods/WCSPH.py:151-203),
+    and the boundary force of the same block, against the reference's
+    equation functions on the golden blocks (src/Equations/Continuity.py,
+    Momentum.py, BoundaryForce.py, XSPH.py)."""
+    from sph import core
+    z = SC.load("equations")
+    for b in range(int(z["nblocks"])):
+        J = len(z["b%d_r" % b])
+        comp = np.zeros(J, dtype=sph.computed_dtype)
+        for k in comp.dtype.names:
+            if "b%d_%s" % (b, k) in z.files:
+                comp[k] = z["b%d_%s" % (b, k)]
+        p5, par6 = z["self5"][b], z["par6"][b]
+        p = np.zeros(1, dtype=sph.particle_dtype)[0]
+        p["p"], p["rho"], p["h"], p["c"], p["m"] = p5
+        p["vx"], p["vy"] = 0.3, -0.2
+        want = z["out"][b]
+        for xsph in (False, True):
+            m = sph.WCSPH(2.0, par6[2], 1000.0, xsph, 0.0)
+            m.alpha, m.beta, m.D, m.p1, m.p2 = par6[0], par6[1], par6[3], par6[4], par6[5]
+
+            def close(a, w):
+                return abs(a - w) <= 1e-12 * max(1.0, abs(w))
+            assert close(m.compute_density_change(p, comp), want[0]), b
+            ax, ay = m.compute_acceleration(p, comp)
+            assert close(ax, want[1]) and close(ay, want[2] - 9.81), b
+            v = m.compute_velocity(p, comp)
+            if xsph:
+                assert v[:2] == [0.3, -0.2] and close(v[2], 0.3 + want[5]) and close(v[3], -0.2 + want[6]), b
+            else:
+                assert v == [0.3, -0.2, 0.0, 0.0]
+            out = core.block_equations(comp, p, m.wcsph_struct())
+            assert close(out[3], want[3]) and close(out[4], want[4]), b
+        msd = sph.WCSPH(2.0, par6[2], 1000.0, False, 0.0, useSummationDensity=True)
+        assert msd.compute_density_change(p, comp) == 0.0
+
+
+
+def _plain_run(sph, chunk):
+    from sph import scenarios as S
+    pa, dx = SC.plain_run_case(S)
+    solver = sph.Solver(sph.WCSPH(0.4, dx, 1000.0, False, 0.0), sph.PEC(False, True), sph.CubicSpline(),
+                        SC.PLAIN_RUN["duration"], incrementalWriteout=False, h=1.3 * dx,
+                        customSettle=SC.settle_after_three, exportProperties=["x", "y", "p"])
+    solver._chunk_max = chunk
+    solver.addParticles(pa.copy())
+    solver.setup()
+    solver.run()
+    return solver
+
+
+def test_solver_plain_run_matches_reference(sph):
+    """Solver.run without a coupling function (src/Solver.py:346-475): the
+    settling steps one at a time, then chunks of steps with one host
+    synchronisation each (rolled back and re-run when a chunk would pass the
+    duration), against the reference's own run of the same case: the same
+    number of steps, dt history, settling time, final state and per-step
+    exports.  The same run with one step per chunk gives identical results."""
+    z = SC.load("solver_plain")
+    solver = _plain_run(sph, 64)
+    assert solver.t_step == int(z["t_step"]) == len(solver.dt_a)
+    np.testing.assert_allclose(solver.dt_a, z["dt_a"], rtol=1e-9)
+    np.testing.assert_allclose(solver.dt_c, z["dt_c"], rtol=1e-9)
+    np.testing.assert_allclose(solver.dt_f, z["dt_f"], rtol=1e-9)
+    assert solver.settleTime == pytest.approx(float(z["settleTime"]), rel=1e-9)
+    assert solver.t == pytest.approx(float(z["t"]), rel=1e-9)
+    fin = solver.particleArray
+    for k in ("x", "y", "vx", "vy", "rho", "p", "ax", "ay", "drho"):
+        assert SC.rel_err(fin[k], z["final_" + k]) <= 1e-8, k
+    assert np.array_equal(fin["deleted"], z["final_deleted"])
+    every = SC.PLAIN_RUN["export_every"]
+    assert len(solver.export["x"]) == solver.t_step
+    assert SC.rel_err(np.array(solver.export["x"])[::every], z["export_x"]) <= 1e-8
+    assert SC.rel_err(np.array(solver.export["p"])[::every], z["export_p"]) <= 1e-8
+    one = _plain_run(sph, 1)
+    assert one.dt_a == solver.dt_a and one.t_step == solver.t_step
+    for k in ("x", "y", "vx", "vy", "rho", "p"):
+        assert np.array_equal(one.particleArray[k], fin[k]), k

@@ -4,8 +4,9 @@ benchmark configurations.
 - The 1000 x 1000 jittered lattice (cubic spline, and the Gaussian cut at
   q <= 3 on the reference's truncated 3 x 3 stencil of 2h cells) and the
   1M-fluid dam break (walls with h = 0, so the reference's cells are 1 m
-  wide): neighbour sets bit-exact for every particle (NNLinkedList.near,
-  src/Tools/NNLinkedList.py:41-141), and one derivative evaluation
+  wide): every particle's neighbour list bit-exact and in the reference's
+  order (NNLinkedList.near, src/Tools/NNLinkedList.py:41-141), and one
+  derivative evaluation
   (Solver._compute = nn.update + h + _loop, src/Solver.py:232-256,
   src/Tools/SolverTools.py:120-175) within 1e-10, norm-wise relative per
   field over the fluid, from the identical state.
@@ -55,7 +56,7 @@ def _prepared(name):
 
 
 @pytest.mark.parametrize("name", ["lattice1m", "lattice1m_gauss", "dambreak1m"])
-def test_fullsize_neighbour_sets_bit_exact(lib, name):
+def test_fullsize_neighbour_lists_bit_exact(lib, name):
     import oracle
     import torch
     from sph import _lib, core
@@ -68,12 +69,12 @@ def test_fullsize_neighbour_sets_bit_exact(lib, name):
     torch.cuda.empty_cache()
     nn = oracle.NN(2.0)
     assert nn.update(st["x"], st["y"], st["h"]) == 0
-    off_r, idx_r = nn.all(nthreads=_threads(), sorted_lists=True)
+    off_r, idx_r = nn.all(nthreads=_threads())  # the reference's traversal order
     assert np.array_equal(np.asarray(off), off_r), "neighbour counts differ"
     same = np.asarray(idx) == idx_r
     if not same.all():
         first = int(np.searchsorted(off_r, np.argmin(same), side="right") - 1)
-        pytest.fail("neighbour lists differ, first at particle %d" % first)
+        pytest.fail("neighbour lists differ (members or order), first at particle %d" % first)
 
 
 @pytest.mark.parametrize("name", ["lattice1m", "lattice1m_gauss", "dambreak1m"])

@@ -76,12 +76,22 @@ def _assert_same_sets(off_a, idx_a, off_b, idx_b):
     assert not bad, "neighbour sets differ for %d particles, first %s" % (len(bad), bad[:5])
 
 
+def _assert_same_lists(off_a, idx_a, off_b, idx_b):
+    """The same lists in the same order (the reference's traversal order)."""
+    _assert_same_sets(off_a, idx_a, off_b, idx_b)
+    assert np.array_equal(np.asarray(off_a), np.asarray(off_b))
+    same = np.asarray(idx_a) == np.asarray(idx_b)
+    if not same.all():
+        first = int(np.searchsorted(np.asarray(off_b), np.argmin(same), side="right") - 1)
+        raise AssertionError("neighbour lists in a different order, first at particle %d" % first)
+
+
 @pytest.mark.parametrize("name", ["nn_lattice", "nn_tank", "nn_alias", "nn_alias_boundary", "nn_grid26"])
 @pytest.mark.parametrize("max_cells", [0, 64])
 def test_nn_sets_bit_exact(sph, name, max_cells):
-    """NNLinkedList.near for every particle equals the reference's lists as
-    sets; max_cells = 64 forces the coarsened own-grid search with the
-    reference-stencil filter."""
+    """NNLinkedList.near for every particle equals the reference's lists, in
+    the reference's order; max_cells = 64 forces the coarsened own-grid
+    search with the reference-stencil filter."""
     core, state = sph
     from sph import _lib
     z = SC.load(name)
@@ -92,7 +102,7 @@ def test_nn_sets_bit_exact(sph, name, max_cells):
     core.nn_update(dp, cfg, ws)
     off, idx = core.nn_export(dp, cfg, ws)
     st = ws.check(allow=_lib.STATUS_INFO)
-    _assert_same_sets(off, idx, z["offsets"], z["idx"])
+    _assert_same_lists(off, idx, z["offsets"], z["idx"])
 
 
 @pytest.mark.parametrize("name", SC.SOLVER_CASES)
@@ -261,4 +271,4 @@ def test_nn_sets_dam_break_vs_oracle(sph):
     core.nn_update(dp, cfg, ws)
     off, idx = core.nn_export(dp, cfg, ws)
     ws.check()
-    _assert_same_sets(off, idx, off_r, idx_r)
+    _assert_same_lists(off, idx, off_r, idx_r)

@@ -82,10 +82,10 @@ def test_probes(oracle_lib):
     off = z["offsets"]
     for k, (x, y) in enumerate(zip(z["px"], z["py"])):
         hij, q, r, idx = nn.near(float(x), float(y), h)
-        o = np.argsort(idx)
-        want = z["idx"][off[k]:off[k + 1]]
-        assert np.array_equal(idx[o], want), k
-        assert np.array_equal(r[o], z["r"][off[k]:off[k + 1]]) and np.array_equal(q[o], z["q"][off[k]:off[k + 1]])
+        want = z["idx"][off[k]:off[k + 1]]  # the reference's own order
+        assert np.array_equal(idx, want), k
+        assert np.array_equal(r, z["r"][off[k]:off[k + 1]]) and np.array_equal(q, z["q"][off[k]:off[k + 1]])
+        assert np.array_equal(hij, z["hij"][off[k]:off[k + 1]])
     par = oracle.wcsph_params(0.4, 0.025, 1000.0)
     rho, p = oracle.probe_density(nn, P, z["px"], z["py"], np.full(len(z["px"]), h), np.full(len(z["px"]), h), 0,
                                   1000.0, par.B, 7.0)
