@@ -538,69 +538,90 @@ constexpr int kScanThreads = 1024;
 constexpr int kScanPer = kScanTile / kScanThreads;
 static_assert(kScanPer == 4, "one uint4 of counts per thread");
 
-// The single-scene scan: scan tile b's offset is the sum of the totals of
-// tiles 0 .. b-1 (counted by k_keys), so one pass writes cstart.
+// The single-scene scan.  Scan tile t's offset is the sum of the totals of
+// tiles 0 .. t-1 (counted by k_keys), so one pass writes cstart.  A block
+// takes a contiguous range of tiles and carries the running offset; a tile
+// that holds no particle is a plain fill of its offset (no counts read, no
+// barrier), which is most of the traversal grid of a tank that the fluid
+// fills only in part.
 __global__ void __launch_bounds__(kScanThreads) k_scan_cells(const unsigned int *__restrict__ counts,
                                                              const DevGrid *__restrict__ g,
                                                              const unsigned int *__restrict__ part,
-                                                             unsigned int *__restrict__ cstart) {
+                                                             unsigned int *__restrict__ cstart, int per_block) {
   __shared__ unsigned int warp_tot[32];
   __shared__ unsigned int red[32];
-  __shared__ unsigned int s_pre;
   const long long m = (long long)g->ncells + 1;
-  const long long base = (long long)blockIdx.x * kScanTile;
-  if (base >= m) return;
-  // the tile's counts and the earlier tiles' totals load together; a tile
-  // that holds no particle (k_keys counted its total) skips its counts
-  const long long c0 = base + (long long)threadIdx.x * kScanPer;
-  const bool empty = part[blockIdx.x] == 0u;
-  unsigned int v[kScanPer] = {0u, 0u, 0u, 0u};
-  if (empty) {
-  } else if (c0 + 3 < m) {
-    const uint4 q = *(const uint4 *)(counts + c0);
-    v[0] = q.x; v[1] = q.y; v[2] = q.z; v[3] = q.w;
-  } else {
-#pragma unroll
-    for (int t = 0; t < kScanPer; t++) v[t] = (c0 + t < m) ? counts[c0 + t] : 0u;
-  }
+  const long long ntiles = (m + kScanTile - 1) / kScanTile;
+  const long long t0 = (long long)blockIdx.x * per_block;
+  if (t0 >= ntiles) return;
+  const long long t1 = t0 + per_block < ntiles ? t0 + per_block : ntiles;
   unsigned int pre = 0;
-  for (int t = threadIdx.x; t < (int)blockIdx.x; t += kScanThreads) pre += part[t];
+  for (long long t = threadIdx.x; t < t0; t += kScanThreads) pre += part[t];
   pre = block_reduce(pre, AddU32(), 0u, red);
-  if (threadIdx.x == 0) s_pre = pre;
-  const unsigned int loc = v[0] + v[1] + v[2] + v[3];
+  __syncthreads();
+  if (threadIdx.x == 0) red[0] = pre;
+  __syncthreads();
+  pre = red[0];
   const int lane = threadIdx.x & 31, wid = threadIdx.x >> 5;
-  unsigned int inc = loc;
+  for (long long t = t0; t < t1; t++) {
+    const long long c0 = t * kScanTile + (long long)threadIdx.x * kScanPer;
+    const unsigned int tot = part[t];  // the same for every thread
+    unsigned int v[kScanPer] = {0u, 0u, 0u, 0u};
+    unsigned int run = pre;
+    if (tot != 0u) {
+      if (c0 + 3 < m) {
+        const uint4 q = *(const uint4 *)(counts + c0);
+        v[0] = q.x; v[1] = q.y; v[2] = q.z; v[3] = q.w;
+      } else {
 #pragma unroll
-  for (int o = 1; o < 32; o <<= 1) {
-    unsigned int u = __shfl_up_sync(0xffffffffu, inc, o);
-    if (lane >= o) inc += u;
-  }
-  if (lane == 31) warp_tot[wid] = inc;
-  __syncthreads();
-  if (wid == 0) {
-    unsigned int t = warp_tot[lane];
+        for (int u = 0; u < kScanPer; u++) v[u] = (c0 + u < m) ? counts[c0 + u] : 0u;
+      }
+      const unsigned int loc = v[0] + v[1] + v[2] + v[3];
+      unsigned int inc = loc;
 #pragma unroll
-    for (int o = 1; o < 32; o <<= 1) {
-      unsigned int u = __shfl_up_sync(0xffffffffu, t, o);
-      if (lane >= o) t += u;
+      for (int o = 1; o < 32; o <<= 1) {
+        const unsigned int u = __shfl_up_sync(0xffffffffu, inc, o);
+        if (lane >= o) inc += u;
+      }
+      if (lane == 31) warp_tot[wid] = inc;
+      __syncthreads();
+      if (wid == 0) {
+        unsigned int w = warp_tot[lane];
+#pragma unroll
+        for (int o = 1; o < 32; o <<= 1) {
+          const unsigned int u = __shfl_up_sync(0xffffffffu, w, o);
+          if (lane >= o) w += u;
+        }
+        warp_tot[lane] = w;  // inclusive over warps
+      }
+      __syncthreads();
+      run = pre + (wid ? warp_tot[wid - 1] : 0u) + inc - loc;
+      __syncthreads();  // warp_tot is read before the next tile writes it
     }
-    warp_tot[lane] = t;  // inclusive over warps
-  }
-  __syncthreads();
-  const unsigned int run = s_pre + (wid ? warp_tot[wid - 1] : 0u) + inc - loc;
-  const unsigned int r0 = run, r1 = r0 + v[0], r2 = r1 + v[1], r3 = r2 + v[2], r4 = r3 + v[3];
-  if (c0 + 3 < m) {
-    *(uint4 *)(cstart + c0) = make_uint4(r0, r1, r2, r3);
-  } else {
-    const unsigned int rr[4] = {r0, r1, r2, r3};
+    const unsigned int r0 = run, r1 = r0 + v[0], r2 = r1 + v[1], r3 = r2 + v[2], r4 = r3 + v[3];
+    if (c0 + 3 < m) {
+      *(uint4 *)(cstart + c0) = make_uint4(r0, r1, r2, r3);
+    } else {
+      const unsigned int rr[4] = {r0, r1, r2, r3};
 #pragma unroll
-    for (int t = 0; t < kScanPer; t++)
-      if (c0 + t < m) cstart[c0 + t] = rr[t];
+      for (int u = 0; u < kScanPer; u++)
+        if (c0 + u < m) cstart[c0 + u] = rr[u];
+    }
+    if (c0 <= m - 1 && m - 1 <= c0 + 3) {
+      const unsigned int rr[5] = {r0, r1, r2, r3, r4};
+      cstart[m] = rr[m - c0];  // total
+    }
+    pre += tot;
   }
-  if (c0 <= m - 1 && m - 1 <= c0 + 3) {
-    const unsigned int rr[5] = {r0, r1, r2, r3, r4};
-    cstart[m] = rr[m - c0];  // total
-  }
+}
+
+// blocks of the scan (a function of the capacity only, so that a captured
+// step replays with any grid) and the tiles each takes
+static void scan_launch(long long n_parts, int &blocks, int &per_block) {
+  const long long cap = (long long)sm_count() * 2;
+  const long long b = n_parts < cap ? n_parts : cap;
+  blocks = (int)(b < 1 ? 1 : b);
+  per_block = (int)((n_parts + blocks - 1) / blocks);
 }
 
 // Single-scene scatter: each particle to its cell's range at its arrival
@@ -843,7 +864,9 @@ void launch_build(const StepArgs &a, const WsPtrs &w, const sph_config_t &cfg, c
   (void)wc;
   const unsigned nb = nblocks(a.n);
   k_keys<<<nb, kBlock, 0, st>>>(a.x, a.y, a.n, w.grid, w.ctrl, w.keys, w.refcell, w.crank, w.counts, w.scan_part);
-  k_scan_cells<<<(unsigned)w.n_parts, kScanThreads, 0, st>>>(w.counts, w.grid, w.scan_part, w.cstart);
+  int sb, sper;
+  scan_launch(w.n_parts, sb, sper);
+  k_scan_cells<<<sb, kScanThreads, 0, st>>>(w.counts, w.grid, w.scan_part, w.cstart, sper);
   k_scatter_rank<<<nb, kBlock, 0, st>>>(w.keys, w.crank, a.n, w.counts, w.cstart, w.perm_tmp, w.keys_sorted,
                                         w.scan_part, w.n_parts);
   RecParams none;
@@ -1073,7 +1096,9 @@ void launch_bt_build(const StepArgs &a, const WsPtrs &w, const BatchPtrs &B, cud
   const unsigned nb = nblocks(a.n);
   k_bt_grid<<<1, 256, 0, st>>>(B, w.ctrl);
   k_bt_keys<<<nb, kBlock, 0, st>>>(a.x, a.y, a.n, B, w.ctrl, w.keys, w.refcell, w.crank, w.counts, w.scan_part);
-  k_scan_cells<<<(unsigned)w.n_parts, kScanThreads, 0, st>>>(w.counts, B.scan, w.scan_part, w.cstart);
+  int sb, sper;
+  scan_launch(w.n_parts, sb, sper);
+  k_scan_cells<<<sb, kScanThreads, 0, st>>>(w.counts, B.scan, w.scan_part, w.cstart, sper);
   k_scatter_rank<<<nb, kBlock, 0, st>>>(w.keys, w.crank, a.n, w.counts, w.cstart, w.perm_tmp, w.keys_sorted,
                                         w.scan_part, w.n_parts);
   k_bt_cellsort<<<nb, kBlock, 0, st>>>(w.perm_tmp, w.keys_sorted, w.cstart, w.refcell, a.n, B, w.ctrl, w.perm, w.meta,

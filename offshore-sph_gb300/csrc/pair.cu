@@ -1351,16 +1351,17 @@ int sm_count() {
   return cache[dev];
 }
 
-// Dynamic shared memory of a tile kernel instantiation: allowed above 48 KB
-// once per device (the attribute is per kernel and device).
+// Dynamic shared memory of a tile kernel: allowed above 48 KB once per device
+// and kernel (the attribute belongs to the kernel function on a device).
+// `done` is the calling launcher's own flag array: every tile kernel
+// instantiation has the same function type, so the flag cannot live here.
 template <typename K>
-static size_t tile_smem(K kern, size_t bytes) {
-  static bool done[64] = {false};
+static size_t tile_smem(K kern, size_t bytes, bool (&done)[64]) {
   int dev = 0;
   cudaGetDevice(&dev);
-  if (dev >= 0 && dev < 64 && !done[dev]) {
+  if (dev < 0 || dev >= 64 || !done[dev]) {
     cudaFuncSetAttribute(kern, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)bytes);
-    done[dev] = true;
+    if (dev >= 0 && dev < 64) done[dev] = true;
   }
   return bytes;
 }
@@ -1371,7 +1372,8 @@ static void mixed_pair_launch(const StepArgs &a, const WsPtrs &w, const PairPara
   // persistent tile kernel, then the global path over what it left
   const int sms = sm_count();
   auto tk = k_pair_tiles<KERNEL, XSPH, SUMDENS, UH>;
-  const size_t smem = tile_smem(tk, sizeof(TileShared<KERNEL>));
+  static bool done[64] = {false};  // this instantiation's attribute, per device
+  const size_t smem = tile_smem(tk, sizeof(TileShared<KERNEL>), done);
   tk<<<sms * TileBlocks<KERNEL>::value, kTileThreads, smem, st>>>(a, pair_ptrs(w), pp, w.tiles, w.fb,
                                                                    (unsigned)w.fb_cap);
   k_pair_list<KERNEL, XSPH, SUMDENS, UH><<<sms * kListBlocks, kPairBlock, 0, st>>>(a, pair_ptrs(w), pp, w.fb,
@@ -1441,7 +1443,8 @@ static void bt_pair_dispatch(const StepArgs &a, const WsPtrs &w, const BatchPtrs
   const int sms = sm_count();
   if (tile_blocks < 1 || tile_blocks > TileBlocks<KERNEL>::value) tile_blocks = TileBlocks<KERNEL>::value;
   auto tk = k_bt_pair_tiles<KERNEL, XSPH, SUMDENS>;
-  const size_t smem = tile_smem(tk, sizeof(TileShared<KERNEL>));
+  static bool done[64] = {false};  // this instantiation's attribute, per device
+  const size_t smem = tile_smem(tk, sizeof(TileShared<KERNEL>), done);
   tk<<<sms * tile_blocks, kTileThreads, smem, st>>>(a, pair_ptrs(w), B, w.fb, (unsigned)w.fb_cap);
   k_bt_pair_list<KERNEL, XSPH, SUMDENS><<<sms * kListBlocks, kPairBlock, 0, st>>>(a, pair_ptrs(w), B, w.fb);
 }
