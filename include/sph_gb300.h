@@ -84,8 +84,9 @@ enum {
   SPH_STATUS_NO_FLUID = 1u << 4,
   /* TimeStep's dt fell below 1e-6 (the reference records it, src/Solver.py:219-224) */
   SPH_STATUS_SMALL_DT = 1u << 5,
-  /* a block of the pair tile kernel gave up waiting for its shared-memory
-   * staging copies (a bounded wait ran out); that evaluation is incomplete */
+  /* a bounded wait on asynchronous shared-memory copies ran out (the pair
+   * kernels stage with plain loads and stores and do not set it; the bit is
+   * kept so that the values of the others stay fixed) */
   SPH_STATUS_STAGING_TIMEOUT = 1u << 6
 };
 

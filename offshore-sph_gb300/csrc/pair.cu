@@ -727,10 +727,10 @@ __global__ void __launch_bounds__(kPairBlock)
 // time and stages the records of the tile and its W-cell halo in shared
 // memory: a table of the (2^ts + 2W)^2 halo cells (counts -> exclusive scan ->
 // shared-memory offsets, cells row-major, so each stencil row of a query is
-// one contiguous shared-memory range), then one copy per cell.  Its queries
-// walk their stencils in shared memory, with 16-bit list entries.  The
-// candidate order (rows, then cells by x, then slot) is the global path's, so
-// both give bit-identical sums.
+// one contiguous shared-memory range), then the records row by row.  Its
+// queries walk their stencils in shared memory, with 16-bit list entries.
+// The candidate order (rows, then cells by x, then slot) is the global
+// path's, so both give the same sums.
 // Left to the global path, through the fallback list: tiles whose halo does
 // not fit, queries whose own cell is not in their stencil or whose h is not
 // positive, and every query when candidates need the reference-stencil filter
@@ -762,7 +762,6 @@ constexpr int kTileUnrollCands = SPH_TILE_UNROLL_CANDS;  // ILP over stencil can
 constexpr int kHaloCap = SPH_HALO_CAP;  // particles of one halo in shared memory
 static_assert(kHaloCap <= 65535, "list entries are 16-bit");
 static_assert(kHaloCellsMax <= 65535, "query map entries are 16-bit halo cells");
-static_assert(kHaloCap * 48 < (1 << 20), "an mbarrier phase counts fewer than 2^20 bytes");
 
 __device__ __forceinline__ void fb_push(DevCtrl *ctrl, int2 *fb, unsigned int fb_cap, unsigned int s,
                                         unsigned int len) {
@@ -796,14 +795,6 @@ __device__ __forceinline__ TileGeom tile_geom(const DevGrid &g, double r0, int c
   return tg;
 }
 
-// Per-block state of the tile kernels' staging: the mbarrier the bulk copies
-// complete on and the phase of the next tile.
-struct TileSync {
-  unsigned long long *bar;
-  uint32_t phase;
-  bool abort;  // a staging wait ran out: the block stops
-};
-
 // shared memory of the tile kernels (dynamic: above the 48 KB static limit)
 template <int KERNEL>
 struct TileShared {
@@ -812,7 +803,6 @@ struct TileShared {
   unsigned int hoff[kHaloCellsMax + 1];  // shared-memory offset of each halo cell, then the total
   unsigned int hgs[kHaloCellsMax];       // its first sorted slot
   unsigned short qmap[kHaloCap];         // halo cell of each query of the tile
-  unsigned long long bar;                // completion of the staging copies
   int s_tile[2];                         // this and the next claimed tile (-1: none left)
   int s_inst[2];                         // their instances (batched form)
   unsigned long long red[kTileThreads / 32];
@@ -821,13 +811,11 @@ struct TileShared {
 // One tile: stage its halo, run its queries.  Returns this thread's largest
 // encoded a^2 over its queries.  All threads of the block call it together.
 //   1. halo table: every halo cell's first sorted slot and count;
-//   2. warp 0: exclusive scan of the counts (shared-memory offsets), then the
-//      halo's records as bulk asynchronous copies, one per contiguous run of
-//      cells (the cells of one halo row inside one tile are consecutive ids,
-//      so their records are one global range) and record array, completing
-//      on the block's mbarrier; meanwhile the other threads map each query of
-//      the tile to its halo cell;
-//   3. after the (bounded) wait, each query walks its stencil rows.
+//   2. warp 0: exclusive scan of the counts (shared-memory offsets); then
+//      every warp copies halo rows into shared memory (a row is at most three
+//      runs of consecutive slots) and the threads map each query of the tile
+//      to its halo cell;
+//   3. each query walks its stencil rows.
 // TSC / WC: the tile shift and stencil half-width as compile-time constants
 // (the own grid's 16x16 tiles with a 5x5 stencil), so that the halo
 // coordinate arithmetic has no integer division; 0 takes them from tg.
@@ -835,8 +823,7 @@ struct TileShared {
 template <int KERNEL, bool XSPH, bool SUMDENS, bool UH, int TSC, int WC>
 __device__ __forceinline__ unsigned long long tile_process(const StepArgs &a, const PairPtrs &P, const TileGeom &tg,
                                                            const MixedConsts &mc, int t, TileShared<KERNEL> &sm,
-                                                           TileSync &sync, DevCtrl *ctrl, int2 *fb,
-                                                           unsigned int fb_cap) {
+                                                           DevCtrl *ctrl, int2 *fb, unsigned int fb_cap) {
   constexpr int kListCap = ListCap<KERNEL>::value;
   const int tid = threadIdx.x;
   const int ts = TSC ? TSC : tg.ts;
@@ -883,38 +870,10 @@ __device__ __forceinline__ unsigned long long tile_process(const StepArgs &a, co
       run += v[u];
     }
     if (tid == 31) hoff[HC] = inc;
-    const unsigned int tot = __shfl_sync(0xffffffffu, inc, 31);
-    __syncwarp();
-    if (tot > 0 && tot <= (unsigned)kHaloCap) {
-      // the previous tile's shared-memory reads (generic proxy) come before
-      // these copies (async proxy)
-      fence_proxy_async_smem();
-      if (tid == 0) mbar_arrive_expect_tx(sync.bar, tot * 48u);
-      __syncwarp();
-      for (int y = tid; y < HW; y += 32) {  // halo row y: runs of cells inside one tile
-        const int gy = oy + y;
-        if (gy < 0 || gy >= tg.nty) continue;
-        int x = ox > 0 ? ox : 0;
-        const int xe = ox + HW < tg.ntx ? ox + HW : tg.ntx;
-        while (x < xe) {
-          const int tile_end = ((x >> ts) + 1) << ts;
-          const int re = tile_end < xe ? tile_end : xe;
-          const int ca = y * HW + (x - ox), cb = y * HW + (re - ox);
-          const unsigned int s0 = hoff[ca], n = hoff[cb] - s0;
-          if (n) {
-            const unsigned int g0 = hgs[ca];
-            bulk_copy_g2s(h0 + s0, P.rec0 + g0, n * 16u, sync.bar);
-            bulk_copy_g2s(h1 + s0, P.rec1 + g0, n * 16u, sync.bar);
-            bulk_copy_g2s(h2 + s0, P.rec2 + g0, n * 16u, sync.bar);
-          }
-          x = re;
-        }
-      }
-    }
   }
   __syncthreads();
   const unsigned int total = hoff[HC];
-  if (total == 0) {  // nothing staged (a listed tile holds particles)
+  if (total == 0) {  // nothing to stage (a listed tile holds particles)
     __syncthreads();
     return ea;
   }
@@ -924,6 +883,47 @@ __device__ __forceinline__ unsigned long long tile_process(const StepArgs &a, co
     __syncthreads();
     return ea;
   }
+  // 2b. the halo's records, row by row: warp w copies halo rows w, w + 8,
+  // ...; a row's cells are one shared-memory range, and in global memory at
+  // most three runs (the cells of one row inside one tile are consecutive
+  // ids).  Each lane copies particles of the row with 16-byte loads and
+  // stores.  (One bulk copy per run and record array would be ~180 small
+  // asynchronous copies per tile, whose per-copy cost dominates.)
+  {
+    const int warp = tid >> 5, lane = tid & 31;
+    const int xa = ox > 0 ? ox : 0;
+    const int xe = ox + HW < tg.ntx ? ox + HW : tg.ntx;
+    for (int y = warp; y < HW; y += kTileThreads / 32) {
+      const int gy = oy + y;
+      if (gy < 0 || gy >= tg.nty || xa >= xe) continue;
+      const int cb = y * HW - ox;  // halo cell of grid column x: cb + x
+      if (T >= W) {
+        // runs [xa, x1), [x1, x2), [x2, xe) (empty when their bounds meet)
+        const int x1 = min(((xa >> ts) + 1) << ts, xe);
+        const int x2 = min(((x1 >> ts) + 1) << ts, xe);
+        const unsigned int sA = hoff[cb + xa], sB = hoff[cb + x1], sC = hoff[cb + x2], sE = hoff[cb + xe];
+        const unsigned int gA = hgs[cb + xa], gB = x1 < xe ? hgs[cb + x1] : 0u, gC = x2 < xe ? hgs[cb + x2] : 0u;
+        for (unsigned int k = sA + lane; k < sE; k += 32) {
+          const unsigned int src = k < sB ? gA + (k - sA) : (k < sC ? gB + (k - sB) : gC + (k - sC));
+          h0[k] = __ldg(P.rec0 + src);
+          h1[k] = __ldg(P.rec1 + src);
+          h2[k] = __ldg(P.rec2 + src);
+        }
+      } else {
+        // tiles narrower than the stencil: the row's runs one by one
+        for (int x = xa; x < xe;) {
+          const int re = min(((x >> ts) + 1) << ts, xe);
+          const unsigned int s0 = hoff[cb + x], e0 = hoff[cb + re], g0 = hgs[cb + x];
+          for (unsigned int k = s0 + lane; k < e0; k += 32) {
+            h0[k] = __ldg(P.rec0 + g0 + (k - s0));
+            h1[k] = __ldg(P.rec1 + g0 + (k - s0));
+            h2[k] = __ldg(P.rec2 + g0 + (k - s0));
+          }
+          x = re;
+        }
+      }
+    }
+  }
   // query -> halo cell, for the tile's own cells (their sorted slots are the
   // tile's query range, in cell order)
   for (int c = tid; c < T * T; c += kTileThreads) {
@@ -931,16 +931,7 @@ __device__ __forceinline__ unsigned long long tile_process(const StepArgs &a, co
     const unsigned int cnt = hoff[hc + 1] - hoff[hc], base = hgs[hc] - qs;
     for (unsigned int u = 0; u < cnt; u++) sm.qmap[base + u] = (unsigned short)hc;
   }
-  const uint32_t parity = sync.phase & 1u;
-  sync.phase++;
-  const bool ok = mbar_wait_bounded(sync.bar, parity);
-  if (__syncthreads_or(!ok)) {  // the copies did not land: flag, drain, stop this block
-    if (tid == 0) atomicOr(&ctrl->status, (unsigned)SPH_STATUS_STAGING_TIMEOUT);
-    mbar_wait_bounded(sync.bar, parity, kMbarDrainLimit);
-    sync.abort = true;
-    __syncthreads();
-    return ea;
-  }
+  __syncthreads();
   // 3. queries.  Candidate radius: the padded reach of the largest pair h
   // (every |h| <= hmaxf), so that one compare per candidate suffices
   const float SK = (float)Support<KERNEL>::q * 1.000002f;  // support / h, padded
@@ -1020,10 +1011,12 @@ __device__ __forceinline__ unsigned long long block_max_u64(unsigned long long v
 template <int KERNEL, bool XSPH, bool SUMDENS, bool UH>
 __device__ __forceinline__ unsigned long long tile_any(const StepArgs &a, const PairPtrs &P, const TileGeom &tg,
                                                        const MixedConsts &mc, int t, TileShared<KERNEL> &sm,
-                                                       TileSync &sync, DevCtrl *ctrl, int2 *fb, unsigned int fb_cap) {
+                                                       DevCtrl *ctrl, int2 *fb, unsigned int fb_cap) {
   if (tg.ts == 4 && tg.W == 2)
-    return tile_process<KERNEL, XSPH, SUMDENS, UH, 4, 2>(a, P, tg, mc, t, sm, sync, ctrl, fb, fb_cap);
-  return tile_process<KERNEL, XSPH, SUMDENS, UH, 0, 0>(a, P, tg, mc, t, sm, sync, ctrl, fb, fb_cap);
+    return tile_process<KERNEL, XSPH, SUMDENS, UH, 4, 2>(a, P, tg, mc, t, sm, ctrl, fb, fb_cap);
+  if (tg.ts == 3 && tg.W == 2)
+    return tile_process<KERNEL, XSPH, SUMDENS, UH, 3, 2>(a, P, tg, mc, t, sm, ctrl, fb, fb_cap);
+  return tile_process<KERNEL, XSPH, SUMDENS, UH, 0, 0>(a, P, tg, mc, t, sm, ctrl, fb, fb_cap);
 }
 
 template <int KERNEL, bool XSPH, bool SUMDENS, bool UH>
@@ -1039,9 +1032,6 @@ __global__ void __launch_bounds__(kTileThreads, TileBlocks<KERNEL>::value)
   const bool filter = gp->mode == 1 && (gp->need_filter || ctrl->alias_count > 0);
   const MixedConsts mc = mixed_consts<KERNEL>(pp);
   unsigned long long ea = kEncMaxId;
-  if (tid == 0) mbar_init(&sm.bar, 1);
-  __syncthreads();
-  TileSync sync{&sm.bar, 0u, false};
 
   if (filter || tg.HC > kHaloCellsMax) {
     // everything on the global path, in 128-slot chunks
@@ -1068,9 +1058,8 @@ __global__ void __launch_bounds__(kTileThreads, TileBlocks<KERNEL>::value)
         const unsigned int c = atomicAdd(&ctrl->tile_next, 1u);
         sm.s_tile[(it + 1) & 1] = c < ntl ? tiles[c] : -1;
       }
-      const unsigned long long q = tile_any<KERNEL, XSPH, SUMDENS, UH>(a, P, tg, mc, t, sm, sync, ctrl, fb, fb_cap);
+      const unsigned long long q = tile_any<KERNEL, XSPH, SUMDENS, UH>(a, P, tg, mc, t, sm, ctrl, fb, fb_cap);
       ea = q > ea ? q : ea;
-      if (sync.abort) break;
     }
   }
   // this block's max a^2 (the list kernel finishes the TimeStep reduction);
@@ -1102,8 +1091,6 @@ __global__ void __launch_bounds__(kTileThreads, TileBlocks<KERNEL>::value)
   const int tid = threadIdx.x;
   DevCtrl *ctrl = P.ctrl;
   const unsigned int ntl = ctrl->tl_count;
-  if (tid == 0) mbar_init(&sm.bar, 1);
-  TileSync sync{&sm.bar, 0u, false};
   if (tid == 0) {
     if (blockIdx.x == 0)  // every instance's dump cell (reference-OOB particles) is in no tile
       for (int b = 0; b < B.n_inst; b++) {
@@ -1140,11 +1127,9 @@ __global__ void __launch_bounds__(kTileThreads, TileBlocks<KERNEL>::value)
       continue;
     }
     const MixedConsts mc = mixed_consts<KERNEL>(pp);
-    const unsigned long long ea =
-        tile_any<KERNEL, XSPH, SUMDENS, true>(a, P, tg, mc, t, sm, sync, ctrl, fb, fb_cap);
+    const unsigned long long ea = tile_any<KERNEL, XSPH, SUMDENS, true>(a, P, tg, mc, t, sm, ctrl, fb, fb_cap);
     const unsigned long long ba = block_max_u64<kTileThreads>(ea, sm.red);
     if (tid == 0 && ba != kEncMaxId) atomicMax(&B.sl[b].pd_a2max, ba);
-    if (sync.abort) break;
   }
   if (tid == 0) {
     __threadfence();
