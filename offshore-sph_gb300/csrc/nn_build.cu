@@ -451,6 +451,7 @@ __device__ void grid_from_bounds(DevCtrl *ctrl, DevGrid *g, const GridParams &gp
   ctrl->hmin_all = kEncMinId; ctrl->hmax_new = kEncMaxId;
   ctrl->alias_count = 0;
   ctrl->tl_count = 0;
+  ctrl->tl_back = 0;
   const unsigned status = grid_setup(xmin, xmax, ymin, ymax, hmin, hmax, gp, g);
   if (status) atomicOr(&ctrl->status, status);
 }
@@ -534,94 +535,84 @@ __global__ void __launch_bounds__(kBlock) k_keys(const double *__restrict__ x, c
 // dump cell) into cstart[0 .. ncells + 1], in one pass over tiles of
 // kScanTile cells; launch sizes depend only on the capacity.
 // ---------------------------------------------------------------------------
-constexpr int kScanThreads = 1024;
-constexpr int kScanPer = kScanTile / kScanThreads;
-static_assert(kScanPer == 4, "one uint4 of counts per thread");
+constexpr int kScanThreads = 256;
+constexpr int kScanPer = kScanTile / kScanThreads;  // 16 cells (four uint4) per thread
+static_assert(kScanPer == 16, "four uint4 of counts per thread");
 
-// The single-scene scan.  Scan tile t's offset is the sum of the totals of
-// tiles 0 .. t-1 (counted by k_keys), so one pass writes cstart.  A block
-// takes a contiguous range of tiles and carries the running offset; a tile
-// that holds no particle is a plain fill of its offset (no counts read, no
-// barrier), which is most of the traversal grid of a tank that the fluid
-// fills only in part.
+// The single-scene scan: one block per scan tile, whose offset is the sum of
+// the totals of tiles 0 .. t-1 (counted by k_keys), so one pass writes
+// cstart.  Small blocks (all of them resident at once on the GPU) with two
+// barriers each; a tile that holds no particle skips its counts and writes
+// its offset.
 __global__ void __launch_bounds__(kScanThreads) k_scan_cells(const unsigned int *__restrict__ counts,
                                                              const DevGrid *__restrict__ g,
                                                              const unsigned int *__restrict__ part,
-                                                             unsigned int *__restrict__ cstart, int per_block) {
-  __shared__ unsigned int warp_tot[32];
-  __shared__ unsigned int red[32];
+                                                             unsigned int *__restrict__ cstart) {
+  __shared__ unsigned int warp_tot[kScanThreads / 32];
+  __shared__ unsigned int warp_pre[kScanThreads / 32];
   const long long m = (long long)g->ncells + 1;
-  const long long ntiles = (m + kScanTile - 1) / kScanTile;
-  const long long t0 = (long long)blockIdx.x * per_block;
-  if (t0 >= ntiles) return;
-  const long long t1 = t0 + per_block < ntiles ? t0 + per_block : ntiles;
-  unsigned int pre = 0;
-  for (long long t = threadIdx.x; t < t0; t += kScanThreads) pre += part[t];
-  pre = block_reduce(pre, AddU32(), 0u, red);
-  __syncthreads();
-  if (threadIdx.x == 0) red[0] = pre;
-  __syncthreads();
-  pre = red[0];
+  const long long t = blockIdx.x;
+  if (t * kScanTile >= m) return;
   const int lane = threadIdx.x & 31, wid = threadIdx.x >> 5;
-  for (long long t = t0; t < t1; t++) {
-    const long long c0 = t * kScanTile + (long long)threadIdx.x * kScanPer;
-    const unsigned int tot = part[t];  // the same for every thread
-    unsigned int v[kScanPer] = {0u, 0u, 0u, 0u};
-    unsigned int run = pre;
-    if (tot != 0u) {
-      if (c0 + 3 < m) {
-        const uint4 q = *(const uint4 *)(counts + c0);
-        v[0] = q.x; v[1] = q.y; v[2] = q.z; v[3] = q.w;
-      } else {
+  const long long c0 = t * kScanTile + (long long)threadIdx.x * kScanPer;
+  const bool empty = part[t] == 0u;
+  unsigned int v[kScanPer];
 #pragma unroll
-        for (int u = 0; u < kScanPer; u++) v[u] = (c0 + u < m) ? counts[c0 + u] : 0u;
-      }
-      const unsigned int loc = v[0] + v[1] + v[2] + v[3];
-      unsigned int inc = loc;
+  for (int u = 0; u < kScanPer; u++) v[u] = 0u;
+  if (!empty) {
+    if (c0 + kScanPer <= m) {
 #pragma unroll
-      for (int o = 1; o < 32; o <<= 1) {
-        const unsigned int u = __shfl_up_sync(0xffffffffu, inc, o);
-        if (lane >= o) inc += u;
+      for (int q = 0; q < kScanPer / 4; q++) {
+        const uint4 w = *(const uint4 *)(counts + c0 + 4 * q);
+        v[4 * q] = w.x; v[4 * q + 1] = w.y; v[4 * q + 2] = w.z; v[4 * q + 3] = w.w;
       }
-      if (lane == 31) warp_tot[wid] = inc;
-      __syncthreads();
-      if (wid == 0) {
-        unsigned int w = warp_tot[lane];
-#pragma unroll
-        for (int o = 1; o < 32; o <<= 1) {
-          const unsigned int u = __shfl_up_sync(0xffffffffu, w, o);
-          if (lane >= o) w += u;
-        }
-        warp_tot[lane] = w;  // inclusive over warps
-      }
-      __syncthreads();
-      run = pre + (wid ? warp_tot[wid - 1] : 0u) + inc - loc;
-      __syncthreads();  // warp_tot is read before the next tile writes it
-    }
-    const unsigned int r0 = run, r1 = r0 + v[0], r2 = r1 + v[1], r3 = r2 + v[2], r4 = r3 + v[3];
-    if (c0 + 3 < m) {
-      *(uint4 *)(cstart + c0) = make_uint4(r0, r1, r2, r3);
     } else {
-      const unsigned int rr[4] = {r0, r1, r2, r3};
 #pragma unroll
-      for (int u = 0; u < kScanPer; u++)
-        if (c0 + u < m) cstart[c0 + u] = rr[u];
+      for (int u = 0; u < kScanPer; u++) v[u] = (c0 + u < m) ? counts[c0 + u] : 0u;
     }
-    if (c0 <= m - 1 && m - 1 <= c0 + 3) {
-      const unsigned int rr[5] = {r0, r1, r2, r3, r4};
-      cstart[m] = rr[m - c0];  // total
-    }
-    pre += tot;
   }
-}
-
-// blocks of the scan (a function of the capacity only, so that a captured
-// step replays with any grid) and the tiles each takes
-static void scan_launch(long long n_parts, int &blocks, int &per_block) {
-  const long long cap = (long long)sm_count() * 2;
-  const long long b = n_parts < cap ? n_parts : cap;
-  blocks = (int)(b < 1 ? 1 : b);
-  per_block = (int)((n_parts + blocks - 1) / blocks);
+  // the totals of the earlier tiles
+  unsigned int pre = 0;
+  for (long long q = threadIdx.x; q < t; q += kScanThreads) pre += part[q];
+  pre = __reduce_add_sync(0xffffffffu, pre);
+  unsigned int loc = 0;
+#pragma unroll
+  for (int u = 0; u < kScanPer; u++) loc += v[u];
+  unsigned int inc = loc;
+#pragma unroll
+  for (int o = 1; o < 32; o <<= 1) {
+    const unsigned int x = __shfl_up_sync(0xffffffffu, inc, o);
+    if (lane >= o) inc += x;
+  }
+  if (lane == 31) {
+    warp_tot[wid] = inc;
+    warp_pre[wid] = pre;
+  }
+  __syncthreads();
+  unsigned int run = inc - loc;
+#pragma unroll
+  for (int w = 0; w < kScanThreads / 32; w++) {
+    if (w < wid) run += warp_tot[w];
+    run += warp_pre[w];
+  }
+  unsigned int r[kScanPer + 1];
+  r[0] = run;
+#pragma unroll
+  for (int u = 0; u < kScanPer; u++) r[u + 1] = r[u] + v[u];
+  if (c0 + kScanPer <= m) {
+#pragma unroll
+    for (int q = 0; q < kScanPer / 4; q++)
+      *(uint4 *)(cstart + c0 + 4 * q) = make_uint4(r[4 * q], r[4 * q + 1], r[4 * q + 2], r[4 * q + 3]);
+  } else {
+#pragma unroll
+    for (int u = 0; u < kScanPer; u++)
+      if (c0 + u < m) cstart[c0 + u] = r[u];
+  }
+  if (c0 <= m - 1 && m - 1 < c0 + kScanPer) {
+#pragma unroll
+    for (int u = 0; u < kScanPer; u++)
+      if (c0 + u == m - 1) cstart[m] = r[u + 1];  // total
+  }
 }
 
 // Single-scene scatter: each particle to its cell's range at its arrival
@@ -804,7 +795,8 @@ __global__ void __launch_bounds__(kBlock) k_cellsort(const int *__restrict__ per
                                                      int *__restrict__ tiles, StepArgs a, RecParams rp,
                                                      float4 *__restrict__ rec0, float4 *__restrict__ rec1,
                                                      float4 *__restrict__ rec2, double4_32a *__restrict__ r64a,
-                                                     double4_32a *__restrict__ r64b, const int *__restrict__ orig) {
+                                                     double4_32a *__restrict__ r64b, const int *__restrict__ orig,
+                                                     unsigned int tiles_cap) {
   __shared__ unsigned long long red[kBlock / 32];
   __shared__ unsigned int redn[kBlock / 32];
   const long long k = (long long)blockIdx.x * blockDim.x + threadIdx.x;
@@ -814,8 +806,14 @@ __global__ void __launch_bounds__(kBlock) k_cellsort(const int *__restrict__ per
     const int key = keys_sorted[k];
     const unsigned int s = cstart[key], e = cstart[key + 1];
     const int ts2 = 2 * gp->ts;
-    if (key < gp->ncells && (unsigned)k == __ldg(&cstart[(key >> ts2) << ts2]))
-      tiles[atomicAdd(&ctrl->tl_count, 1u)] = key >> ts2;
+    if (key < gp->ncells && (unsigned)k == __ldg(&cstart[(key >> ts2) << ts2])) {
+      // a tile holding at least one particle per cell is listed from the
+      // front, a sparser one from the back, so that the pair kernel, which
+      // claims them in list order, ends on the cheap ones
+      const unsigned int te = __ldg(&cstart[((key >> ts2) + 1) << ts2]);
+      if (te - (unsigned)k >= (1u << ts2)) tiles[atomicAdd(&ctrl->tl_count, 1u)] = key >> ts2;
+      else tiles[tiles_cap - 1 - atomicAdd(&ctrl->tl_back, 1u)] = key >> ts2;
+    }
     const int v = perm_tmp[k];
     // rank inside the cell by particle index: the caller's index when the
     // run steps on the sorted copy of the state (orig), so that the order,
@@ -864,9 +862,7 @@ void launch_build(const StepArgs &a, const WsPtrs &w, const sph_config_t &cfg, c
   (void)wc;
   const unsigned nb = nblocks(a.n);
   k_keys<<<nb, kBlock, 0, st>>>(a.x, a.y, a.n, w.grid, w.ctrl, w.keys, w.refcell, w.crank, w.counts, w.scan_part);
-  int sb, sper;
-  scan_launch(w.n_parts, sb, sper);
-  k_scan_cells<<<sb, kScanThreads, 0, st>>>(w.counts, w.grid, w.scan_part, w.cstart, sper);
+  k_scan_cells<<<(unsigned)w.n_parts, kScanThreads, 0, st>>>(w.counts, w.grid, w.scan_part, w.cstart);
   k_scatter_rank<<<nb, kBlock, 0, st>>>(w.keys, w.crank, a.n, w.counts, w.cstart, w.perm_tmp, w.keys_sorted,
                                         w.scan_part, w.n_parts);
   RecParams none;
@@ -874,7 +870,7 @@ void launch_build(const StepArgs &a, const WsPtrs &w, const sph_config_t &cfg, c
 #define SPH_CELLSORT(P, ...)                                                                                   \
   k_cellsort<__VA_ARGS__><<<nb, kBlock, 0, st>>>(w.perm_tmp, w.keys_sorted, w.cstart, w.refcell, a.n, w.grid,   \
                                                  w.ctrl, w.perm, w.meta, w.tiles, a, P, w.rec0, w.rec1, w.rec2, \
-                                                 w.rec64a, w.rec64b, w.orig)
+                                                 w.rec64a, w.rec64b, w.orig, (unsigned)(w.max_cells + 1))
   if (!rp) {
     SPH_CELLSORT(none, kRecNone);
   } else if (cfg.precision == SPH_PREC_MIXED) {
@@ -1096,9 +1092,7 @@ void launch_bt_build(const StepArgs &a, const WsPtrs &w, const BatchPtrs &B, cud
   const unsigned nb = nblocks(a.n);
   k_bt_grid<<<1, 256, 0, st>>>(B, w.ctrl);
   k_bt_keys<<<nb, kBlock, 0, st>>>(a.x, a.y, a.n, B, w.ctrl, w.keys, w.refcell, w.crank, w.counts, w.scan_part);
-  int sb, sper;
-  scan_launch(w.n_parts, sb, sper);
-  k_scan_cells<<<sb, kScanThreads, 0, st>>>(w.counts, B.scan, w.scan_part, w.cstart, sper);
+  k_scan_cells<<<(unsigned)w.n_parts, kScanThreads, 0, st>>>(w.counts, B.scan, w.scan_part, w.cstart);
   k_scatter_rank<<<nb, kBlock, 0, st>>>(w.keys, w.crank, a.n, w.counts, w.cstart, w.perm_tmp, w.keys_sorted,
                                         w.scan_part, w.n_parts);
   k_bt_cellsort<<<nb, kBlock, 0, st>>>(w.perm_tmp, w.keys_sorted, w.cstart, w.refcell, a.n, B, w.ctrl, w.perm, w.meta,

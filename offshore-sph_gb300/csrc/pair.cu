@@ -67,7 +67,8 @@ __device__ int exact_count(const StepArgs &a, const int *__restrict__ perm, cons
 // pass gathered, and resets the slots.
 __device__ __forceinline__ void timestep_epilogue(DevCtrl *ctrl, unsigned long long ea, double co, double cfl_c,
                                                   double cfl_f, double *dt_out, double *dt_hist,
-                                                  unsigned int *zero_on_last = nullptr) {
+                                                  unsigned int *zero_on_last = nullptr,
+                                                  unsigned int nblocks = 0 /* 0: every block of the grid */) {
   __shared__ unsigned long long red[kPairBlock / 32];
   __shared__ bool last;
   const unsigned long long wm = warp_max_u64(ea);
@@ -78,7 +79,7 @@ __device__ __forceinline__ void timestep_epilogue(DevCtrl *ctrl, unsigned long l
     for (int w = 0; w < (int)(blockDim.x >> 5); w++) ba = red[w] > ba ? red[w] : ba;
     if (ba != kEncMaxId) atomicMax(&ctrl->pd_a2max, ba);
     __threadfence();
-    last = atomicAdd(&ctrl->done_pair, 1u) == gridDim.x - 1;
+    last = atomicAdd(&ctrl->done_pair, 1u) == (nblocks ? nblocks : gridDim.x) - 1;
   }
   __syncthreads();
   if (last && threadIdx.x == 0) {
@@ -536,6 +537,13 @@ __global__ void __launch_bounds__(kPairBlock, kListBlocks)
                 double *dt_hist) {
   __shared__ unsigned int lists[ListCap<KERNEL>::value][kPairBlock];
   const unsigned int cnt = *(volatile unsigned int *)&P.ctrl->fb_count;
+  // only the blocks that have entries take part (at least block 0, which
+  // finishes the TimeStep when the list is empty); the rest leave at once.
+  // A block that starts after the last participant emptied the list reads
+  // 0 and leaves too: the list is emptied only once every participant,
+  // itself included, has read the count.
+  const unsigned int parts = cnt < gridDim.x ? (cnt > 0u ? cnt : 1u) : gridDim.x;
+  if (blockIdx.x >= parts) return;
   unsigned long long ea = kEncMaxId;
   if (blockIdx.x < cnt) {
     const DevGrid g = *P.grid;
@@ -550,13 +558,13 @@ __global__ void __launch_bounds__(kPairBlock, kListBlocks)
     }
   }
   __syncthreads();
-  // the last block to finish empties the fallback list (with the TimeStep
+  // the last participant empties the fallback list (with the TimeStep
   // epilogue when there is one)
   if (pp.do_dt) {
-    timestep_epilogue(P.ctrl, ea, pp.co, pp.cfl_c, pp.cfl_f, dt_out, dt_hist, &P.ctrl->fb_count);
+    timestep_epilogue(P.ctrl, ea, pp.co, pp.cfl_c, pp.cfl_f, dt_out, dt_hist, &P.ctrl->fb_count, parts);
   } else if (threadIdx.x == 0) {
     __threadfence();
-    if (atomicAdd(&P.ctrl->fb_done, 1u) == gridDim.x - 1) {
+    if (atomicAdd(&P.ctrl->fb_done, 1u) == parts - 1) {
       P.ctrl->fb_count = 0;
       P.ctrl->fb_done = 0;
     }
@@ -757,6 +765,7 @@ template <int KERNEL>
 struct TileBlocks {
   static constexpr int value = ListCap<KERNEL>::value == 32 ? 3 : 2;
 };
+constexpr bool kSplitTail = true;  // the last tiles of a launch as half-tile units
 constexpr int kTileUnrollPairs = SPH_TILE_UNROLL_PAIRS;  // ILP over list entries
 constexpr int kTileUnrollCands = SPH_TILE_UNROLL_CANDS;  // ILP over stencil candidates
 constexpr int kHaloCap = SPH_HALO_CAP;  // particles of one halo in shared memory
@@ -803,7 +812,7 @@ struct TileShared {
   unsigned int hoff[kHaloCellsMax + 1];  // shared-memory offset of each halo cell, then the total
   unsigned int hgs[kHaloCellsMax];       // its first sorted slot
   unsigned short qmap[kHaloCap];         // halo cell of each query of the tile
-  int s_tile[2];                         // this and the next claimed tile (-1: none left)
+  int s_tile[2];                         // this and the next claimed work unit (-1: none left)
   int s_inst[2];                         // their instances (batched form)
   unsigned long long red[kTileThreads / 32];
 };
@@ -820,22 +829,29 @@ struct TileShared {
 // (the own grid's 16x16 tiles with a 5x5 stencil), so that the halo
 // coordinate arithmetic has no integer division; 0 takes them from tg.
 // UH: every fluid particle has the same h (UniformQ).
+// part: 0 the whole tile; 1 and 2 its first and second half of cell rows
+// (the kernel's last tiles are split so that its final round of work is
+// short).
 template <int KERNEL, bool XSPH, bool SUMDENS, bool UH, int TSC, int WC>
 __device__ __forceinline__ unsigned long long tile_process(const StepArgs &a, const PairPtrs &P, const TileGeom &tg,
-                                                           const MixedConsts &mc, int t, TileShared<KERNEL> &sm,
-                                                           DevCtrl *ctrl, int2 *fb, unsigned int fb_cap) {
+                                                           const MixedConsts &mc, int t, int part,
+                                                           TileShared<KERNEL> &sm, DevCtrl *ctrl, int2 *fb,
+                                                           unsigned int fb_cap) {
   constexpr int kListCap = ListCap<KERNEL>::value;
   const int tid = threadIdx.x;
   const int ts = TSC ? TSC : tg.ts;
   const int W = TSC ? WC : tg.W;
-  const int T = 1 << ts, HW = T + 2 * W, HC = HW * HW;
+  const int T = 1 << ts, HW = T + 2 * W;
+  const int rows = part ? T >> 1 : T, row0 = part == 2 ? T >> 1 : 0;
+  const int HWy = rows + 2 * W, HC = HW * HWy;
   const int ntlx = tg.ntlx;
   float4 *h0 = sm.h0, *h1 = sm.h1, *h2 = sm.h2;
   unsigned int *hoff = sm.hoff, *hgs = sm.hgs;
   const unsigned int *cst = P.cstart + tg.cell0;  // this grid's cells
   unsigned long long ea = kEncMaxId;
-  const unsigned int qs = __ldg(&cst[t << (2 * ts)]), qe = __ldg(&cst[(t + 1) << (2 * ts)]);
-  const int ox = (t % ntlx) * T - W, oy = (t / ntlx) * T - W;
+  const unsigned int tb = (unsigned int)t << (2 * ts);  // the tile's first cell (row-major inside)
+  const unsigned int qs = __ldg(&cst[tb + row0 * T]), qe = __ldg(&cst[tb + (row0 + rows) * T]);
+  const int ox = (t % ntlx) * T - W, oy = (t / ntlx) * T + row0 - W;
   // 1. halo table: counts and first slots
   for (int c = tid; c < HC; c += kTileThreads) {
     const int x = ox + c % HW, y = oy + c / HW;
@@ -893,7 +909,7 @@ __device__ __forceinline__ unsigned long long tile_process(const StepArgs &a, co
     const int warp = tid >> 5, lane = tid & 31;
     const int xa = ox > 0 ? ox : 0;
     const int xe = ox + HW < tg.ntx ? ox + HW : tg.ntx;
-    for (int y = warp; y < HW; y += kTileThreads / 32) {
+    for (int y = warp; y < HWy; y += kTileThreads / 32) {
       const int gy = oy + y;
       if (gy < 0 || gy >= tg.nty || xa >= xe) continue;
       const int cb = y * HW - ox;  // halo cell of grid column x: cb + x
@@ -926,7 +942,7 @@ __device__ __forceinline__ unsigned long long tile_process(const StepArgs &a, co
   }
   // query -> halo cell, for the tile's own cells (their sorted slots are the
   // tile's query range, in cell order)
-  for (int c = tid; c < T * T; c += kTileThreads) {
+  for (int c = tid; c < T * rows; c += kTileThreads) {
     const int hc = (W + (c >> ts)) * HW + W + (c & (T - 1));
     const unsigned int cnt = hoff[hc + 1] - hoff[hc], base = hgs[hc] - qs;
     for (unsigned int u = 0; u < cnt; u++) sm.qmap[base + u] = (unsigned short)hc;
@@ -1010,19 +1026,20 @@ __device__ __forceinline__ unsigned long long block_max_u64(unsigned long long v
 // the tile of a single-scene grid with the shape the grid has
 template <int KERNEL, bool XSPH, bool SUMDENS, bool UH>
 __device__ __forceinline__ unsigned long long tile_any(const StepArgs &a, const PairPtrs &P, const TileGeom &tg,
-                                                       const MixedConsts &mc, int t, TileShared<KERNEL> &sm,
-                                                       DevCtrl *ctrl, int2 *fb, unsigned int fb_cap) {
+                                                       const MixedConsts &mc, int t, int part,
+                                                       TileShared<KERNEL> &sm, DevCtrl *ctrl, int2 *fb,
+                                                       unsigned int fb_cap) {
   if (tg.ts == 4 && tg.W == 2)
-    return tile_process<KERNEL, XSPH, SUMDENS, UH, 4, 2>(a, P, tg, mc, t, sm, ctrl, fb, fb_cap);
+    return tile_process<KERNEL, XSPH, SUMDENS, UH, 4, 2>(a, P, tg, mc, t, part, sm, ctrl, fb, fb_cap);
   if (tg.ts == 3 && tg.W == 2)
-    return tile_process<KERNEL, XSPH, SUMDENS, UH, 3, 2>(a, P, tg, mc, t, sm, ctrl, fb, fb_cap);
-  return tile_process<KERNEL, XSPH, SUMDENS, UH, 0, 0>(a, P, tg, mc, t, sm, ctrl, fb, fb_cap);
+    return tile_process<KERNEL, XSPH, SUMDENS, UH, 3, 2>(a, P, tg, mc, t, part, sm, ctrl, fb, fb_cap);
+  return tile_process<KERNEL, XSPH, SUMDENS, UH, 0, 0>(a, P, tg, mc, t, part, sm, ctrl, fb, fb_cap);
 }
 
 template <int KERNEL, bool XSPH, bool SUMDENS, bool UH>
 __global__ void __launch_bounds__(kTileThreads, TileBlocks<KERNEL>::value)
-    k_pair_tiles(StepArgs a, PairPtrs P, PairParams pp, const int *__restrict__ tiles, int2 *__restrict__ fb,
-                 unsigned int fb_cap) {
+    k_pair_tiles(StepArgs a, PairPtrs P, PairParams pp, const int *__restrict__ tiles, unsigned int tiles_cap,
+                 int2 *__restrict__ fb, unsigned int fb_cap) {
   extern __shared__ __align__(128) unsigned char smem_raw[];
   TileShared<KERNEL> &sm = *reinterpret_cast<TileShared<KERNEL> *>(smem_raw);
   const int tid = threadIdx.x;
@@ -1041,24 +1058,34 @@ __global__ void __launch_bounds__(kTileThreads, TileBlocks<KERNEL>::value)
         fb_push(ctrl, fb, fb_cap, (unsigned)(c * kPairBlock), (unsigned)min((long long)kPairBlock, pp.n - c * kPairBlock));
     }
   } else {
-    const unsigned int ntl = ctrl->tl_count;
+    // Work units in claim order: dense tiles (listed from the front) first,
+    // then the sparse ones (listed from the back of the tile list); the last
+    // `split` tiles of that order come as two half-tile units each, so that
+    // the kernel's final round of work is half a tile.  A unit is encoded as
+    // 4 tile + part (part 0: whole tile; 1, 2: halves), -1 when none is left.
+    const unsigned int ntl = ctrl->tl_count, nback = ctrl->tl_back, nall = ntl + nback;
+    const unsigned int split = (kSplitTail && tg.ts >= 1) ? min(nall, gridDim.x) : 0u;
+    auto tile_at = [&](unsigned int p) { return p < ntl ? tiles[p] : tiles[tiles_cap - 1 - (p - ntl)]; };
+    auto claim = [&](unsigned int c) {
+      if (c < nall - split) return 4 * tile_at(c);
+      const unsigned int k = c - (nall - split);
+      return k < 2 * split ? 4 * tile_at(nall - split + (k >> 1)) + 1 + (int)(k & 1u) : -1;
+    };
     if (tid == 0) {
       if (blockIdx.x == 0) {  // the dump cell (reference-OOB particles) is in no tile
         const unsigned int d0 = __ldg(&P.cstart[gp->ncells]), d1 = __ldg(&P.cstart[gp->ncells + 1]);
         for (unsigned int s = d0; s < d1; s += kPairBlock) fb_push(ctrl, fb, fb_cap, s, min((unsigned)kPairBlock, d1 - s));
       }
-      const unsigned int c = atomicAdd(&ctrl->tile_next, 1u);
-      sm.s_tile[0] = c < ntl ? tiles[c] : -1;
+      sm.s_tile[0] = claim(atomicAdd(&ctrl->tile_next, 1u));
     }
     __syncthreads();
     for (int it = 0;; it++) {
-      const int t = sm.s_tile[it & 1];
-      if (t < 0) break;
-      if (tid == 0) {  // claim the next tile while this one runs
-        const unsigned int c = atomicAdd(&ctrl->tile_next, 1u);
-        sm.s_tile[(it + 1) & 1] = c < ntl ? tiles[c] : -1;
-      }
-      const unsigned long long q = tile_any<KERNEL, XSPH, SUMDENS, UH>(a, P, tg, mc, t, sm, ctrl, fb, fb_cap);
+      const int u = sm.s_tile[it & 1];
+      if (u < 0) break;
+      if (tid == 0)  // claim the next unit while this one runs
+        sm.s_tile[(it + 1) & 1] = claim(atomicAdd(&ctrl->tile_next, 1u));
+      const unsigned long long q =
+          tile_any<KERNEL, XSPH, SUMDENS, UH>(a, P, tg, mc, u >> 2, u & 3, sm, ctrl, fb, fb_cap);
       ea = q > ea ? q : ea;
     }
   }
@@ -1127,7 +1154,7 @@ __global__ void __launch_bounds__(kTileThreads, TileBlocks<KERNEL>::value)
       continue;
     }
     const MixedConsts mc = mixed_consts<KERNEL>(pp);
-    const unsigned long long ea = tile_any<KERNEL, XSPH, SUMDENS, true>(a, P, tg, mc, t, sm, ctrl, fb, fb_cap);
+    const unsigned long long ea = tile_any<KERNEL, XSPH, SUMDENS, true>(a, P, tg, mc, t, 0, sm, ctrl, fb, fb_cap);
     const unsigned long long ba = block_max_u64<kTileThreads>(ea, sm.red);
     if (tid == 0 && ba != kEncMaxId) atomicMax(&B.sl[b].pd_a2max, ba);
   }
@@ -1359,7 +1386,8 @@ static void mixed_pair_launch(const StepArgs &a, const WsPtrs &w, const PairPara
   auto tk = k_pair_tiles<KERNEL, XSPH, SUMDENS, UH>;
   static bool done[64] = {false};  // this instantiation's attribute, per device
   const size_t smem = tile_smem(tk, sizeof(TileShared<KERNEL>), done);
-  tk<<<sms * TileBlocks<KERNEL>::value, kTileThreads, smem, st>>>(a, pair_ptrs(w), pp, w.tiles, w.fb,
+  tk<<<sms * TileBlocks<KERNEL>::value, kTileThreads, smem, st>>>(a, pair_ptrs(w), pp, w.tiles,
+                                                                   (unsigned)(w.max_cells + 1), w.fb,
                                                                    (unsigned)w.fb_cap);
   k_pair_list<KERNEL, XSPH, SUMDENS, UH><<<sms * kListBlocks, kPairBlock, 0, st>>>(a, pair_ptrs(w), pp, w.fb,
                                                                                     dt_out, dt_hist);

@@ -152,7 +152,9 @@ struct DevCtrl {
   // kernel; entries and finished blocks of the fallback list
   unsigned int tile_next, tile_done;
   unsigned int fb_count, fb_done;
-  unsigned int tl_count;  // non-empty tiles listed by the build
+  // non-empty tiles listed by the build: tl_count dense ones from the front
+  // of the tile list, tl_back sparse ones from its back (single-scene build)
+  unsigned int tl_count, tl_back;
   unsigned int bounds_done;  // finished blocks of the bounds pass (its last block sets the grid)
   double dt_ring[2][3];  // {dt, dt_c, dt_f} of the step with that parity
 };
