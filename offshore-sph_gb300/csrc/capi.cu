@@ -42,6 +42,8 @@ WsLayout make_layout(long long n_cap, long long max_cells) {
   L.fb_cap = (long long)(n + n / 128 + mc + 2);
   L.fb = take((size_t)L.fb_cap * 8);
   L.tiles = take((mc + 1) * 4);
+  L.tiles_h = take((mc + 1) * 4);
+  L.tflag = take((mc + 1 + 31) / 32 * 4);
   L.total = off;
   L.shadow = take(n * 8 * kStateFields);
   L.shadow_label = take(n);
@@ -73,6 +75,8 @@ WsPtrs ws_ptrs(const sph_workspace_t *ws) {
   p.rec64b = (double4_32a *)(b + L.rec64b);
   p.fb = (int2 *)(b + L.fb);
   p.tiles = (int *)(b + L.tiles);
+  p.tiles_h = (int *)(b + L.tiles_h);
+  p.tflag = (unsigned int *)(b + L.tflag);
   p.fb_cap = L.fb_cap;
   p.n_cap = L.n_cap;
   p.max_cells = L.max_cells;
@@ -98,6 +102,7 @@ __global__ void k_ctrl_init(DevCtrl *c) {
 cudaError_t init_workspace(const WsPtrs &w, cudaStream_t st) {
   cudaError_t e = cudaMemsetAsync(w.counts, 0, (size_t)(w.max_cells + 1) * 4, st);
   if (e == cudaSuccess) e = cudaMemsetAsync(w.scan_part, 0, (size_t)w.n_parts * 4, st);
+  if (e == cudaSuccess) e = cudaMemsetAsync(w.tflag, 0, (size_t)(w.max_cells + 1 + 31) / 32 * 4, st);
   if (e == cudaSuccess) e = cudaMemsetAsync(w.grid, 0, sizeof(DevGrid), st);
   if (e != cudaSuccess) return e;
   k_ctrl_init<<<1, 32, 0, st>>>(w.ctrl);

@@ -452,6 +452,7 @@ __device__ void grid_from_bounds(DevCtrl *ctrl, DevGrid *g, const GridParams &gp
   ctrl->alias_count = 0;
   ctrl->tl_count = 0;
   ctrl->tl_back = 0;
+  ctrl->tl_heavy = 0;
   const unsigned status = grid_setup(xmin, xmax, ymin, ymax, hmin, hmax, gp, g);
   if (status) atomicOr(&ctrl->status, status);
 }
@@ -500,7 +501,8 @@ __global__ void __launch_bounds__(kBlock) k_keys(const double *__restrict__ x, c
                                                  long long n, const DevGrid *__restrict__ gp, DevCtrl *ctrl,
                                                  int *__restrict__ keys, int2 *__restrict__ refcell,
                                                  unsigned int *__restrict__ crank, unsigned int *__restrict__ counts,
-                                                 unsigned int *__restrict__ part) {
+                                                 unsigned int *__restrict__ part, const int8_t *__restrict__ label,
+                                                 unsigned int *__restrict__ tflag) {
   const long long i = (long long)blockIdx.x * blockDim.x + threadIdx.x;
   const int lane = threadIdx.x & 31;
   const bool act = i < n;
@@ -511,6 +513,12 @@ __global__ void __launch_bounds__(kBlock) k_keys(const double *__restrict__ x, c
     key = cell_key(*gp, x[i], y[i], ref, alias, overflow);
     refcell[i] = ref;
     keys[i] = key;
+    // a boundary particle marks its tile, which the pair kernel then claims
+    // before the tiles of fluid alone (its queries next to the wall cost more)
+    if (key < gp->ncells && !is_fluid(label[i])) {
+      const int tl = key >> (2 * gp->ts);
+      atomicOr(&tflag[tl >> 5], 1u << (tl & 31));
+    }
   }
   const unsigned int below = (1u << lane) - 1u;
   const unsigned int peers = __match_any_sync(0xffffffffu, key);
@@ -796,7 +804,8 @@ __global__ void __launch_bounds__(kBlock) k_cellsort(const int *__restrict__ per
                                                      float4 *__restrict__ rec0, float4 *__restrict__ rec1,
                                                      float4 *__restrict__ rec2, double4_32a *__restrict__ r64a,
                                                      double4_32a *__restrict__ r64b, const int *__restrict__ orig,
-                                                     unsigned int tiles_cap) {
+                                                     unsigned int tiles_cap, int *__restrict__ tiles_h,
+                                                     unsigned int *__restrict__ tflag) {
   __shared__ unsigned long long red[kBlock / 32];
   __shared__ unsigned int redn[kBlock / 32];
   const long long k = (long long)blockIdx.x * blockDim.x + threadIdx.x;
@@ -807,12 +816,23 @@ __global__ void __launch_bounds__(kBlock) k_cellsort(const int *__restrict__ per
     const unsigned int s = cstart[key], e = cstart[key + 1];
     const int ts2 = 2 * gp->ts;
     if (key < gp->ncells && (unsigned)k == __ldg(&cstart[(key >> ts2) << ts2])) {
-      // a tile holding at least one particle per cell is listed from the
-      // front, a sparser one from the back, so that the pair kernel, which
-      // claims them in list order, ends on the cheap ones
-      const unsigned int te = __ldg(&cstart[((key >> ts2) + 1) << ts2]);
-      if (te - (unsigned)k >= (1u << ts2)) tiles[atomicAdd(&ctrl->tl_count, 1u)] = key >> ts2;
-      else tiles[tiles_cap - 1 - atomicAdd(&ctrl->tl_back, 1u)] = key >> ts2;
+      // The pair kernel claims the tiles list by list, in list order, so
+      // that it ends on the cheap ones: first the dense tiles (at least one
+      // particle per cell) that hold a boundary particle, whose queries next
+      // to the wall cost about twice the others; then the other dense tiles
+      // (front of the tile list); then the sparse ones (its back).  The
+      // tile's boundary bit (set by k_keys) returns to zero here.
+      const int tl = key >> ts2;
+      const unsigned int tbit = 1u << (tl & 31);
+      const bool wall = (tflag[tl >> 5] & tbit) != 0u;
+      if (wall) atomicAnd(&tflag[tl >> 5], ~tbit);
+      const unsigned int te = __ldg(&cstart[(tl + 1) << ts2]);
+      if (te - (unsigned)k >= (1u << ts2)) {
+        if (wall) tiles_h[atomicAdd(&ctrl->tl_heavy, 1u)] = tl;
+        else tiles[atomicAdd(&ctrl->tl_count, 1u)] = tl;
+      } else {
+        tiles[tiles_cap - 1 - atomicAdd(&ctrl->tl_back, 1u)] = tl;
+      }
     }
     const int v = perm_tmp[k];
     // rank inside the cell by particle index: the caller's index when the
@@ -861,7 +881,8 @@ void launch_build(const StepArgs &a, const WsPtrs &w, const sph_config_t &cfg, c
                   cudaStream_t st, const RecParams *rp) {
   (void)wc;
   const unsigned nb = nblocks(a.n);
-  k_keys<<<nb, kBlock, 0, st>>>(a.x, a.y, a.n, w.grid, w.ctrl, w.keys, w.refcell, w.crank, w.counts, w.scan_part);
+  k_keys<<<nb, kBlock, 0, st>>>(a.x, a.y, a.n, w.grid, w.ctrl, w.keys, w.refcell, w.crank, w.counts, w.scan_part,
+                                a.label, w.tflag);
   k_scan_cells<<<(unsigned)w.n_parts, kScanThreads, 0, st>>>(w.counts, w.grid, w.scan_part, w.cstart);
   k_scatter_rank<<<nb, kBlock, 0, st>>>(w.keys, w.crank, a.n, w.counts, w.cstart, w.perm_tmp, w.keys_sorted,
                                         w.scan_part, w.n_parts);
@@ -870,7 +891,8 @@ void launch_build(const StepArgs &a, const WsPtrs &w, const sph_config_t &cfg, c
 #define SPH_CELLSORT(P, ...)                                                                                   \
   k_cellsort<__VA_ARGS__><<<nb, kBlock, 0, st>>>(w.perm_tmp, w.keys_sorted, w.cstart, w.refcell, a.n, w.grid,   \
                                                  w.ctrl, w.perm, w.meta, w.tiles, a, P, w.rec0, w.rec1, w.rec2, \
-                                                 w.rec64a, w.rec64b, w.orig, (unsigned)(w.max_cells + 1))
+                                                 w.rec64a, w.rec64b, w.orig, (unsigned)(w.max_cells + 1), w.tiles_h, \
+                                                 w.tflag)
   if (!rp) {
     SPH_CELLSORT(none, kRecNone);
   } else if (cfg.precision == SPH_PREC_MIXED) {

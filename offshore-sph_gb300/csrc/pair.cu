@@ -146,16 +146,22 @@ __device__ __forceinline__ MixedConsts mixed_consts(const PairParams &pp) {
   return c;
 }
 
-// Uniform fluid h (the run has a fixed h, Solver(h=...)): every fluid record
-// carries the same FP32 h, so for a fluid query i and a fluid neighbour j,
-// h_ij = 0.5 (h_i + h_j) = h_i exactly, and the averaged h of the viscosity
-// term is h_i as well.  The kernel and viscosity constants are then per
-// query, computed once.
+// Uniform fluid h (the run has a fixed h, Solver(h=...)) and beta = 0 (the
+// reference's WCSPH default): every fluid record carries the same FP32 h, so
+// for a fluid query i and a fluid neighbour j, h_ij = 0.5 (h_i + h_j) = h_i
+// exactly, and the averaged h of the viscosity term is h_i as well.  The
+// kernel, gradient and viscosity constants are then per query, computed once,
+// and with beta = 0 the viscosity
+//   Pi_ij = mu (beta mu - alpha c_ij) / rho_ij,  mu = h v.r / (r^2 + 0.01 h^2)
+// is (-2 alpha c_ij h) v.r / ((r^2 + 0.01 h^2)(rho_i + rho_j)): one
+// reciprocal per pair.
 struct UniformQ {
-  float lim;    // (support h)^2
-  float inv_h;  // 1 / h
-  float al;     // the kernel's normalisation at h
-  float hb2;    // 0.01 h^2 (viscosity denominator)
+  float lim;     // (support h)^2
+  float inv_h;   // 1 / h
+  float al;      // the kernel's normalisation at h
+  float g0, g1, g2;  // kernel-gradient polynomial coefficients with al / h folded in
+  float hb2;     // 0.01 h^2 (viscosity denominator)
+  float pic;     // -2 alpha c_ij h (viscosity numerator)
 };
 
 template <int KERNEL>
@@ -166,12 +172,29 @@ __device__ __forceinline__ UniformQ uniform_q(const MixedConsts &c, float h) {
   const float fac = KERNEL == SPH_KERNEL_CUBIC ? (float)kCubicFac
                                                : (KERNEL == SPH_KERNEL_WENDLAND ? (float)kWendFac : (float)kInvPi);
   u.al = fac * u.inv_h * u.inv_h;
+  const float alh = u.al * u.inv_h;
+  if (KERNEL == SPH_KERNEL_CUBIC) {
+    // dW/dr / r = al/h (-0.75 (2 - q)^2) / r (q > 1), al/h q (2.25 q - 3) / r (q <= 1)
+    u.g0 = -0.75f * alh;
+    u.g1 = 2.25f * alh;
+    u.g2 = -3.0f * alh;
+  } else if (KERNEL == SPH_KERNEL_WENDLAND) {
+    // dW/dr / r = al/h (1 - q/2)^5 q (-14/3 - 35/3 q) / r
+    u.g0 = (-14.0f / 3.0f) * alh;
+    u.g1 = (-35.0f / 3.0f) * alh;
+    u.g2 = 0.f;
+  } else {
+    // dW/dr / r = -2 al / h^2 exp(-q^2)
+    u.g0 = -2.0f * alh * u.inv_h;
+    u.g1 = u.g2 = 0.f;
+  }
   u.hb2 = 0.01f * (h * h);
+  u.pic = -2.0f * c.avc * h;
   return u;
 }
 
-// One FLUID neighbour j of fluid query i under a uniform fluid h (see
-// UniformQ): the same equations as mixed_pair's fluid branch with the
+// One FLUID neighbour j of fluid query i under a uniform fluid h and beta = 0
+// (see UniformQ): the same equations as mixed_pair's fluid branch with the
 // per-pair h arithmetic taken out.
 template <int KERNEL, bool XSPH, bool SUMDENS>
 __device__ __forceinline__ void mixed_fluid_uh(MixedAcc &acc, const MixedConsts &c, const UniformQ &u, float hq,
@@ -187,36 +210,34 @@ __device__ __forceinline__ void mixed_fluid_uh(MixedAcc &acc, const MixedConsts 
   const float q = r * u.inv_h;
   const float vxij = (Vi.x - vj.x) + (Vi.z - vj.z);
   const float vyij = (Vi.y - vj.y) + (Vi.w - vj.w);
-  float w, coef;
+  float w = 0.f, coef;
   if (KERNEL == SPH_KERNEL_CUBIC) {
     const float t2 = fmaxf(2.0f - q, 0.f);
     const bool outer = q > 1.0f;
-    w = XSPH ? (outer ? u.al * 0.25f * (t2 * t2 * t2) : u.al * (1.0f - 1.5f * (q * q) * (1.0f - 0.5f * q))) : 0.f;
-    const float gq = outer ? -0.75f * (t2 * t2) : -3.0f * q * (1.0f - 0.75f * q);
-    coef = r >= 1e-10f ? u.al * gq * u.inv_h * inv_r : 0.f;
+    if (XSPH) w = outer ? u.al * 0.25f * (t2 * t2 * t2) : u.al * (1.0f - 1.5f * (q * q) * (1.0f - 0.5f * q));
+    const float g = outer ? u.g0 * (t2 * t2) : q * fmaf(u.g1, q, u.g2);
+    coef = r >= 1e-10f ? g * inv_r : 0.f;
   } else if (KERNEL == SPH_KERNEL_WENDLAND) {
     const float inner = fmaxf(1.0f - 0.5f * q, 0.f);
     const float i2 = inner * inner, i5 = i2 * i2 * inner;
-    w = XSPH ? u.al * (i5 * inner) * ((35.0f / 12.0f) * q * q + 3.0f * q + 1.0f) : 0.f;
-    const float gq = i5 * (-14.0f / 3.0f) * q * (1.0f + 2.5f * q);
-    coef = r >= 1e-10f ? u.al * gq * u.inv_h * inv_r : 0.f;
+    if (XSPH) w = u.al * (i5 * inner) * ((35.0f / 12.0f) * q * q + 3.0f * q + 1.0f);
+    coef = r >= 1e-10f ? i5 * q * fmaf(u.g1, q, u.g0) * inv_r : 0.f;
   } else {
     const float e = __expf(-q * q);
-    w = u.al * e;
-    coef = r * hq > 1e-12f ? -2.0f * u.al * e * u.inv_h * u.inv_h : 0.f;
+    if (XSPH) w = u.al * e;
+    coef = r * hq > 1e-12f ? u.g0 * e : 0.f;
   }
   const float dwx = coef * dx, dwy = coef * dy;
   const float mj = qj.w;
   if (!SUMDENS) acc.fd = fmaf(mj, vxij * dwx + vyij * dwy, acc.fd);
   const float dot = vxij * dx + vyij * dy;
-  const float ir = __fdividef(2.0f, Ri.z + rj.z);  // 1 / rho_ij
-  const float mu = hq * dot * __fdividef(1.0f, d2 + u.hb2);
-  const float PI = dot < 0.f ? mu * (c.beta * mu - c.avc) * ir : 0.f;
+  const float rs = Ri.z + rj.z;  // 2 rho_ij
+  const float PI = dot < 0.f ? u.pic * dot * __fdividef(1.0f, (d2 + u.hb2) * rs) : 0.f;
   const float fac = mj * (Ri.w + rj.w + PI);
   acc.fax = fmaf(-fac, dwx, acc.fax);
   acc.fay = fmaf(-fac, dwy, acc.fay);
   if (XSPH) {
-    const float fx = -c.eps * mj * w * ir;
+    const float fx = -c.eps * mj * w * __fdividef(2.0f, rs);
     acc.fsx = fmaf(fx, vxij, acc.fsx);
     acc.fsy = fmaf(fx, vyij, acc.fsy);
   }
@@ -293,8 +314,9 @@ __device__ __forceinline__ void mixed_pair(MixedAcc &acc, const MixedConsts &c, 
   }
 }
 
-// One list entry j of query i: with a uniform fluid h (UH), fluid neighbours
-// take the fast path and the rest (boundary particles) the general one.
+// One list entry j of query i: with a uniform fluid h and beta = 0 (UH), fluid
+// neighbours take the fast path and the rest (boundary particles) the general
+// one.
 template <int KERNEL, bool XSPH, bool SUMDENS, bool UH>
 __device__ __forceinline__ void mixed_entry(MixedAcc &acc, const MixedConsts &c, const UniformQ &u, float4 Qi,
                                             float4 Ri, float4 Vi, float4 qj, float4 rj, const float4 *vjp) {
@@ -902,9 +924,10 @@ __device__ __forceinline__ unsigned long long tile_process(const StepArgs &a, co
   // 2b. the halo's records, row by row: warp w copies halo rows w, w + 8,
   // ...; a row's cells are one shared-memory range, and in global memory at
   // most three runs (the cells of one row inside one tile are consecutive
-  // ids).  Each lane copies particles of the row with 16-byte loads and
-  // stores.  (One bulk copy per run and record array would be ~180 small
-  // asynchronous copies per tile, whose per-copy cost dominates.)
+  // ids).  Each lane issues 16-byte asynchronous copies of particles of the
+  // row, so that all copies of the halo are in flight together and the block
+  // waits once.  (One bulk copy per run and record array would be ~180 small
+  // copies per tile, whose per-copy cost dominates.)
   {
     const int warp = tid >> 5, lane = tid & 31;
     const int xa = ox > 0 ? ox : 0;
@@ -921,9 +944,9 @@ __device__ __forceinline__ unsigned long long tile_process(const StepArgs &a, co
         const unsigned int gA = hgs[cb + xa], gB = x1 < xe ? hgs[cb + x1] : 0u, gC = x2 < xe ? hgs[cb + x2] : 0u;
         for (unsigned int k = sA + lane; k < sE; k += 32) {
           const unsigned int src = k < sB ? gA + (k - sA) : (k < sC ? gB + (k - sB) : gC + (k - sC));
-          h0[k] = __ldg(P.rec0 + src);
-          h1[k] = __ldg(P.rec1 + src);
-          h2[k] = __ldg(P.rec2 + src);
+          cp_async16(h0 + k, P.rec0 + src);
+          cp_async16(h1 + k, P.rec1 + src);
+          cp_async16(h2 + k, P.rec2 + src);
         }
       } else {
         // tiles narrower than the stencil: the row's runs one by one
@@ -931,9 +954,9 @@ __device__ __forceinline__ unsigned long long tile_process(const StepArgs &a, co
           const int re = min(((x >> ts) + 1) << ts, xe);
           const unsigned int s0 = hoff[cb + x], e0 = hoff[cb + re], g0 = hgs[cb + x];
           for (unsigned int k = s0 + lane; k < e0; k += 32) {
-            h0[k] = __ldg(P.rec0 + g0 + (k - s0));
-            h1[k] = __ldg(P.rec1 + g0 + (k - s0));
-            h2[k] = __ldg(P.rec2 + g0 + (k - s0));
+            cp_async16(h0 + k, P.rec0 + g0 + (k - s0));
+            cp_async16(h1 + k, P.rec1 + g0 + (k - s0));
+            cp_async16(h2 + k, P.rec2 + g0 + (k - s0));
           }
           x = re;
         }
@@ -947,6 +970,7 @@ __device__ __forceinline__ unsigned long long tile_process(const StepArgs &a, co
     const unsigned int cnt = hoff[hc + 1] - hoff[hc], base = hgs[hc] - qs;
     for (unsigned int u = 0; u < cnt; u++) sm.qmap[base + u] = (unsigned short)hc;
   }
+  cp_async_wait_all();
   __syncthreads();
   // 3. queries.  Candidate radius: the padded reach of the largest pair h
   // (every |h| <= hmaxf), so that one compare per candidate suffices
@@ -980,26 +1004,34 @@ __device__ __forceinline__ unsigned long long tile_process(const StepArgs &a, co
     const float rq = fmaxf(SK * hq, fminf(tg.r0f, 3.0f * hq) * 1.000002f) + tg.pad;
     const float rq2 = rq * rq;
     int nl = 0;
-    for (int r = -W; r <= W; r++) {
+    // the stencil rows' slot ranges, the query's own row as the two ranges
+    // either side of its own slot (the particle itself is no candidate)
+    for (int r = -W, seg = 0; r <= W; seg = 0, r++) {
       const unsigned int *row = hoff + (hy + r) * HW + hx;
       unsigned int j = row[-W];
       const unsigned int e = row[W + 1];
-      while (j < e) {
-        if (nl == kListCap) {
-          physics(nl);
-          nl = 0;
-        }
-        // a chunk that cannot overflow the list: every candidate is written
-        // and kept (counted) when inside the radius; j == sq, the particle
-        // itself, contributes zero
-        const unsigned int ce = min(e, j + (unsigned int)(kListCap - nl));
+      unsigned int se = r == 0 ? sq : e;
+      for (;;) {
+        while (j < se) {
+          if (nl == kListCap) {
+            physics(nl);
+            nl = 0;
+          }
+          // a chunk that cannot overflow the list: every candidate is
+          // written, and kept (counted) when inside the radius
+          const unsigned int ce = min(se, j + (unsigned int)(kListCap - nl));
 #pragma unroll kTileUnrollCands
-        for (; j < ce; j++) {
-          const float2 p = *reinterpret_cast<const float2 *>(h0 + j);
-          const float dx = Qi.x - p.x, dy = Qi.y - p.y;
-          sm.lists[nl][tid] = (unsigned short)j;
-          nl += (fmaf(dx, dx, dy * dy) <= rq2 && j != sq) ? 1 : 0;
+          for (; j < ce; j++) {
+            const float2 p = *reinterpret_cast<const float2 *>(h0 + j);
+            const float dx = Qi.x - p.x, dy = Qi.y - p.y;
+            sm.lists[nl][tid] = (unsigned short)j;
+            nl += fmaf(dx, dx, dy * dy) <= rq2 ? 1 : 0;
+          }
         }
+        if (r != 0 || seg) break;
+        seg = 1;
+        j = sq + 1;
+        se = e;
       }
     }
     physics(nl);
@@ -1038,7 +1070,8 @@ __device__ __forceinline__ unsigned long long tile_any(const StepArgs &a, const 
 
 template <int KERNEL, bool XSPH, bool SUMDENS, bool UH>
 __global__ void __launch_bounds__(kTileThreads, TileBlocks<KERNEL>::value)
-    k_pair_tiles(StepArgs a, PairPtrs P, PairParams pp, const int *__restrict__ tiles, unsigned int tiles_cap,
+    k_pair_tiles(StepArgs a, PairPtrs P, PairParams pp, const int *__restrict__ tiles,
+                 const int *__restrict__ tiles_h, unsigned int tiles_cap,
                  int2 *__restrict__ fb, unsigned int fb_cap) {
   extern __shared__ __align__(128) unsigned char smem_raw[];
   TileShared<KERNEL> &sm = *reinterpret_cast<TileShared<KERNEL> *>(smem_raw);
@@ -1058,14 +1091,17 @@ __global__ void __launch_bounds__(kTileThreads, TileBlocks<KERNEL>::value)
         fb_push(ctrl, fb, fb_cap, (unsigned)(c * kPairBlock), (unsigned)min((long long)kPairBlock, pp.n - c * kPairBlock));
     }
   } else {
-    // Work units in claim order: dense tiles (listed from the front) first,
-    // then the sparse ones (listed from the back of the tile list); the last
-    // `split` tiles of that order come as two half-tile units each, so that
-    // the kernel's final round of work is half a tile.  A unit is encoded as
+    // Work units in claim order: dense tiles with a wall along a side (their
+    // own list), the other dense tiles (listed from the front of the tile
+    // list), then the sparse ones (listed from its back); the last `split`
+    // tiles of that order come as two half-tile units each, so that the
+    // kernel's final round of work is half a tile.  A unit is encoded as
     // 4 tile + part (part 0: whole tile; 1, 2: halves), -1 when none is left.
-    const unsigned int ntl = ctrl->tl_count, nback = ctrl->tl_back, nall = ntl + nback;
+    const unsigned int nh = ctrl->tl_heavy, ntl = nh + ctrl->tl_count, nall = ntl + ctrl->tl_back;
     const unsigned int split = (kSplitTail && tg.ts >= 1) ? min(nall, gridDim.x) : 0u;
-    auto tile_at = [&](unsigned int p) { return p < ntl ? tiles[p] : tiles[tiles_cap - 1 - (p - ntl)]; };
+    auto tile_at = [&](unsigned int p) {
+      return p < nh ? tiles_h[p] : (p < ntl ? tiles[p - nh] : tiles[tiles_cap - 1 - (p - ntl)]);
+    };
     auto claim = [&](unsigned int c) {
       if (c < nall - split) return 4 * tile_at(c);
       const unsigned int k = c - (nall - split);
@@ -1108,7 +1144,8 @@ __global__ void __launch_bounds__(kTileThreads, TileBlocks<KERNEL>::value)
 // Batched form: the tile kernel over the (instance, tile) list of all
 // instances, each tile with its instance's grid and constants, and the
 // fallback list with each entry's instance (see nn_build.cu).  Every instance
-// has a fixed h, so the uniform-h form applies.
+// has a fixed h, so the uniform-h form applies to the instances whose
+// viscosity beta is 0; the others take the general per-pair form.
 // ---------------------------------------------------------------------------
 template <int KERNEL, bool XSPH, bool SUMDENS>
 __global__ void __launch_bounds__(kTileThreads, TileBlocks<KERNEL>::value)
@@ -1154,7 +1191,9 @@ __global__ void __launch_bounds__(kTileThreads, TileBlocks<KERNEL>::value)
       continue;
     }
     const MixedConsts mc = mixed_consts<KERNEL>(pp);
-    const unsigned long long ea = tile_any<KERNEL, XSPH, SUMDENS, true>(a, P, tg, mc, t, 0, sm, ctrl, fb, fb_cap);
+    const unsigned long long ea =
+        pp.beta == 0.0 ? tile_any<KERNEL, XSPH, SUMDENS, true>(a, P, tg, mc, t, 0, sm, ctrl, fb, fb_cap)
+                       : tile_any<KERNEL, XSPH, SUMDENS, false>(a, P, tg, mc, t, 0, sm, ctrl, fb, fb_cap);
     const unsigned long long ba = block_max_u64<kTileThreads>(ea, sm.red);
     if (tid == 0 && ba != kEncMaxId) atomicMax(&B.sl[b].pd_a2max, ba);
   }
@@ -1181,7 +1220,9 @@ __global__ void __launch_bounds__(kPairBlock, kListBlocks)
     const bool filter = g.mode == 1 && (g.need_filter || B.sl[b].alias_count > 0);
     unsigned long long ea = kEncMaxId;
     if ((int)threadIdx.x < r.y)
-      ea = pair_query<KERNEL, XSPH, SUMDENS, true, true>(a, P, pp, g, filter, r.x + threadIdx.x, lists, B.coff[b]);
+      ea = pp.beta == 0.0
+               ? pair_query<KERNEL, XSPH, SUMDENS, true, true>(a, P, pp, g, filter, r.x + threadIdx.x, lists, B.coff[b])
+               : pair_query<KERNEL, XSPH, SUMDENS, true, false>(a, P, pp, g, filter, r.x + threadIdx.x, lists, B.coff[b]);
     const unsigned long long ba = block_max_u64<kPairBlock>(ea, red);
     if (threadIdx.x == 0 && ba != kEncMaxId) atomicMax(&B.sl[b].pd_a2max, ba);
   }
@@ -1386,7 +1427,7 @@ static void mixed_pair_launch(const StepArgs &a, const WsPtrs &w, const PairPara
   auto tk = k_pair_tiles<KERNEL, XSPH, SUMDENS, UH>;
   static bool done[64] = {false};  // this instantiation's attribute, per device
   const size_t smem = tile_smem(tk, sizeof(TileShared<KERNEL>), done);
-  tk<<<sms * TileBlocks<KERNEL>::value, kTileThreads, smem, st>>>(a, pair_ptrs(w), pp, w.tiles,
+  tk<<<sms * TileBlocks<KERNEL>::value, kTileThreads, smem, st>>>(a, pair_ptrs(w), pp, w.tiles, w.tiles_h,
                                                                    (unsigned)(w.max_cells + 1), w.fb,
                                                                    (unsigned)w.fb_cap);
   k_pair_list<KERNEL, XSPH, SUMDENS, UH><<<sms * kListBlocks, kPairBlock, 0, st>>>(a, pair_ptrs(w), pp, w.fb,
@@ -1397,8 +1438,9 @@ template <int KERNEL, bool XSPH, bool SUMDENS>
 static void pair_dispatch(const StepArgs &a, const WsPtrs &w, const sph_config_t &cfg, const PairParams &pp,
                           double *dt_out, double *dt_hist, cudaStream_t st) {
   if (cfg.precision == SPH_PREC_MIXED) {
-    // a fixed h makes every fluid record's h the same (the uniform-h form)
-    if (cfg.h_fixed > 0.0) mixed_pair_launch<KERNEL, XSPH, SUMDENS, true>(a, w, pp, dt_out, dt_hist, st);
+    // a fixed h makes every fluid record's h the same (the uniform-h form,
+    // taken when the viscosity's beta is 0)
+    if (cfg.h_fixed > 0.0 && pp.beta == 0.0) mixed_pair_launch<KERNEL, XSPH, SUMDENS, true>(a, w, pp, dt_out, dt_hist, st);
     else mixed_pair_launch<KERNEL, XSPH, SUMDENS, false>(a, w, pp, dt_out, dt_hist, st);
   } else {
     // one query per thread; below a few blocks per SM, one-warp blocks so

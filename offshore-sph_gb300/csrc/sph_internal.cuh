@@ -152,9 +152,10 @@ struct DevCtrl {
   // kernel; entries and finished blocks of the fallback list
   unsigned int tile_next, tile_done;
   unsigned int fb_count, fb_done;
-  // non-empty tiles listed by the build: tl_count dense ones from the front
-  // of the tile list, tl_back sparse ones from its back (single-scene build)
-  unsigned int tl_count, tl_back;
+  // non-empty tiles listed by the build (single-scene build): tl_heavy dense
+  // tiles holding a boundary particle in their own list, tl_count other dense
+  // ones from the front of the tile list, tl_back sparse ones from its back
+  unsigned int tl_count, tl_back, tl_heavy;
   unsigned int bounds_done;  // finished blocks of the bounds pass (its last block sets the grid)
   double dt_ring[2][3];  // {dt, dt_c, dt_f} of the step with that parity
 };
@@ -198,7 +199,7 @@ struct DevGrid {
 // the state that sph_run steps on when the workspace has room for it.
 struct WsLayout {
   size_t ctrl, grid, keys, refcell, crank, perm_tmp, keys_sorted, perm, meta, counts, cstart, scan_part, rec0,
-      rec1, rec2, rec64a, rec64b, fb, tiles, total;
+      rec1, rec2, rec64a, rec64b, fb, tiles, tiles_h, tflag, total;
   size_t shadow, shadow_label, shadow_orig, total_shadow;
   long long n_cap, max_cells, n_parts, fb_cap;
 };
@@ -319,7 +320,9 @@ struct WsPtrs {
   float4 *rec0, *rec1, *rec2;
   double4_32a *rec64a, *rec64b;
   int2 *fb;  // fallback list of the tile pair kernel: (first slot, count <= 128)
-  int *tiles;  // non-empty tiles of the current build, in no particular order
+  int *tiles;    // non-empty tiles of the current build (dense from the front, sparse from the back)
+  int *tiles_h;  // its dense tiles that hold a boundary particle
+  unsigned int *tflag;  // one bit per tile: it holds a boundary particle (zero between builds)
   long long n_cap, max_cells, n_parts, fb_cap;
   // The sorted copy of the state (when the workspace has room): kStateFields
   // arrays of n_cap doubles, the labels, and each copy index's caller index.
@@ -449,6 +452,16 @@ __device__ __forceinline__ bool mbar_try_wait(unsigned long long *bar, uint32_t 
       : "memory");
   return ok != 0;
 }
+
+// Per-thread asynchronous copies global -> shared (cp.async, 16 bytes each,
+// through L2 only): a thread issues any number of them without holding the
+// data in registers, then waits for all of its own; a block barrier after the
+// wait makes every thread's copies visible to the block.  Addresses 16-byte
+// aligned.
+__device__ __forceinline__ void cp_async16(void *dst, const void *src) {
+  asm volatile("cp.async.cg.shared.global [%0], [%1], 16;" ::"r"(smem_addr(dst)), "l"(src) : "memory");
+}
+__device__ __forceinline__ void cp_async_wait_all() { asm volatile("cp.async.wait_all;" ::: "memory"); }
 
 // Bounded wait for phase `parity` of bar; false when the limit ran out.
 // kMbarWaitLimit polls take milliseconds, far longer than any staging copy of
