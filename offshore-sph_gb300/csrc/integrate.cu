@@ -100,6 +100,7 @@ __device__ __forceinline__ void correct_one(const StepArgs &a, long long i, cons
 }
 
 __global__ void __launch_bounds__(kBlock) k_correct(StepArgs a, IntParams ip) {
+  step_kernel_entry();
   long long i = (long long)blockIdx.x * blockDim.x + threadIdx.x;
   if (i >= a.n || !is_fluid(a.label[i])) return;
   correct_one(a, i, ip);
@@ -125,12 +126,13 @@ void launch_predict(const StepArgs &a, const sph_config_t &cfg, const double *dt
 
 void launch_correct(const StepArgs &a, const sph_config_t &cfg, const double *dt, double dt_fixed,
                     cudaStream_t st) {
-  k_correct<<<nblocks(a.n), kBlock, 0, st>>>(a, int_params(cfg, dt, dt_fixed));
+  launch_pdl(k_correct, dim3(nblocks(a.n)), dim3(kBlock), 0, st, a, int_params(cfg, dt, dt_fixed));
 }
 
 // TimeStep.compute over fluid (src/Equations/TimeStep.py:7-91)
 __global__ void __launch_bounds__(kBlock) k_timestep(StepArgs a, DevCtrl *ctrl, double cfl_c, double cfl_f,
                                                      double *dt3, double *dt_hist) {
+  step_kernel_entry();
   __shared__ unsigned long long red[32];
   __shared__ unsigned int red32[32];
   __shared__ bool last;
@@ -189,7 +191,7 @@ __global__ void __launch_bounds__(kBlock) k_timestep(StepArgs a, DevCtrl *ctrl, 
 
 void launch_timestep(const StepArgs &a, const WsPtrs &w, const sph_config_t &cfg, double *dt3, double *dt_hist,
                      cudaStream_t st) {
-  k_timestep<<<nblocks(a.n), kBlock, 0, st>>>(a, w.ctrl, cfg.cfl_c, cfg.cfl_f, dt3, dt_hist);
+  launch_pdl(k_timestep, dim3(nblocks(a.n)), dim3(kBlock), 0, st, a, w.ctrl, cfg.cfl_c, cfg.cfl_f, dt3, dt_hist);
 }
 
 // WCSPH.initialize (src/Methods/WCSPH.py:82-108 via TaitEOS_height,

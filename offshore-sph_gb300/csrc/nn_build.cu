@@ -210,6 +210,7 @@ constexpr int kBoundsBlocks = SPH_BOUNDS_BLOCKS;  // resident blocks per SM
 template <int INTEG, int STAGE, bool DAMPED, bool XSPH>
 __global__ void __launch_bounds__(kBlock, kBoundsBlocks) k_bounds(StepArgs a, DevCtrl *ctrl, BoundsParams bp,
                                                                   DevGrid *g, GridParams gp) {
+  step_kernel_entry();
   __shared__ unsigned long long red[kBlock / 32][6];
   __shared__ bool last;
   unsigned long long v[6] = {kEncMinId, kEncMinId, kEncMinId, kEncMinId, kEncMinId, kEncMinId};
@@ -317,7 +318,7 @@ void launch_bounds(const StepArgs &a, const WsPtrs &w, const sph_config_t &cfg, 
   const GridParams gp = grid_params(w, cfg, wc);
   const unsigned nb = persist_blocks(a.n, kBoundsBlocks);
   front_dispatch(bp, [&]<int I, int S, bool D, bool X>() {
-    k_bounds<I, S, D, X><<<nb, kBlock, 0, st>>>(a, w.ctrl, bp, w.grid, gp);
+    launch_pdl(k_bounds<I, S, D, X>, dim3(nb), dim3(kBlock), 0, st, a, w.ctrl, bp, w.grid, gp);
   });
 }
 
@@ -503,6 +504,7 @@ __global__ void __launch_bounds__(kBlock) k_keys(const double *__restrict__ x, c
                                                  unsigned int *__restrict__ crank, unsigned int *__restrict__ counts,
                                                  unsigned int *__restrict__ part, const int8_t *__restrict__ label,
                                                  unsigned int *__restrict__ tflag) {
+  step_kernel_entry();
   const long long i = (long long)blockIdx.x * blockDim.x + threadIdx.x;
   const int lane = threadIdx.x & 31;
   const bool act = i < n;
@@ -513,12 +515,16 @@ __global__ void __launch_bounds__(kBlock) k_keys(const double *__restrict__ x, c
     key = cell_key(*gp, x[i], y[i], ref, alias, overflow);
     refcell[i] = ref;
     keys[i] = key;
-    // a boundary particle marks its tile, which the pair kernel then claims
-    // before the tiles of fluid alone (its queries next to the wall cost more)
-    if (key < gp->ncells && !is_fluid(label[i])) {
-      const int tl = key >> (2 * gp->ts);
-      atomicOr(&tflag[tl >> 5], 1u << (tl & 31));
-    }
+  }
+  // A boundary particle marks its tile, which the pair kernel then claims
+  // before the tiles of fluid alone (its queries next to the wall cost more).
+  // One atomic per tile and warp: a wall's particles sit in few tiles, and
+  // one atomic each would queue thousands on the same words.
+  const bool wall = act && key < gp->ncells && !is_fluid(label[i]);
+  if (__ballot_sync(0xffffffffu, wall)) {
+    const int tl = wall ? key >> (2 * gp->ts) : -1;
+    const unsigned int tpeers = __match_any_sync(0xffffffffu, tl);
+    if (wall && lane == __ffs(tpeers) - 1) atomicOr(&tflag[tl >> 5], 1u << (tl & 31));
   }
   const unsigned int below = (1u << lane) - 1u;
   const unsigned int peers = __match_any_sync(0xffffffffu, key);
@@ -556,6 +562,7 @@ __global__ void __launch_bounds__(kScanThreads) k_scan_cells(const unsigned int 
                                                              const DevGrid *__restrict__ g,
                                                              const unsigned int *__restrict__ part,
                                                              unsigned int *__restrict__ cstart) {
+  step_kernel_entry();
   __shared__ unsigned int warp_tot[kScanThreads / 32];
   __shared__ unsigned int warp_pre[kScanThreads / 32];
   const long long m = (long long)g->ncells + 1;
@@ -631,6 +638,7 @@ __global__ void __launch_bounds__(kBlock) k_scatter_rank(const int *__restrict__
                                                          const unsigned int *__restrict__ cstart,
                                                          int *__restrict__ perm_tmp, int *__restrict__ keys_sorted,
                                                          unsigned int *__restrict__ part, long long n_parts) {
+  step_kernel_entry();
   const long long i = (long long)blockIdx.x * blockDim.x + threadIdx.x;
   for (long long t = i; t < n_parts; t += (long long)gridDim.x * blockDim.x) part[t] = 0u;
   if (i >= n) return;
@@ -806,6 +814,7 @@ __global__ void __launch_bounds__(kBlock) k_cellsort(const int *__restrict__ per
                                                      double4_32a *__restrict__ r64b, const int *__restrict__ orig,
                                                      unsigned int tiles_cap, int *__restrict__ tiles_h,
                                                      unsigned int *__restrict__ tflag) {
+  step_kernel_entry();
   __shared__ unsigned long long red[kBlock / 32];
   __shared__ unsigned int redn[kBlock / 32];
   const long long k = (long long)blockIdx.x * blockDim.x + threadIdx.x;
@@ -881,18 +890,18 @@ void launch_build(const StepArgs &a, const WsPtrs &w, const sph_config_t &cfg, c
                   cudaStream_t st, const RecParams *rp) {
   (void)wc;
   const unsigned nb = nblocks(a.n);
-  k_keys<<<nb, kBlock, 0, st>>>(a.x, a.y, a.n, w.grid, w.ctrl, w.keys, w.refcell, w.crank, w.counts, w.scan_part,
-                                a.label, w.tflag);
-  k_scan_cells<<<(unsigned)w.n_parts, kScanThreads, 0, st>>>(w.counts, w.grid, w.scan_part, w.cstart);
-  k_scatter_rank<<<nb, kBlock, 0, st>>>(w.keys, w.crank, a.n, w.counts, w.cstart, w.perm_tmp, w.keys_sorted,
-                                        w.scan_part, w.n_parts);
+  launch_pdl(k_keys, dim3(nb), dim3(kBlock), 0, st, a.x, a.y, a.n, w.grid, w.ctrl, w.keys, w.refcell, w.crank,
+             w.counts, w.scan_part, a.label, w.tflag);
+  launch_pdl(k_scan_cells, dim3((unsigned)w.n_parts), dim3(kScanThreads), 0, st, w.counts, w.grid, w.scan_part,
+             w.cstart);
+  launch_pdl(k_scatter_rank, dim3(nb), dim3(kBlock), 0, st, w.keys, w.crank, a.n, w.counts, w.cstart, w.perm_tmp,
+             w.keys_sorted, w.scan_part, w.n_parts);
   RecParams none;
   memset(&none, 0, sizeof(none));
 #define SPH_CELLSORT(P, ...)                                                                                   \
-  k_cellsort<__VA_ARGS__><<<nb, kBlock, 0, st>>>(w.perm_tmp, w.keys_sorted, w.cstart, w.refcell, a.n, w.grid,   \
-                                                 w.ctrl, w.perm, w.meta, w.tiles, a, P, w.rec0, w.rec1, w.rec2, \
-                                                 w.rec64a, w.rec64b, w.orig, (unsigned)(w.max_cells + 1), w.tiles_h, \
-                                                 w.tflag)
+  launch_pdl(k_cellsort<__VA_ARGS__>, dim3(nb), dim3(kBlock), 0, st, w.perm_tmp, w.keys_sorted, w.cstart,        \
+             w.refcell, a.n, w.grid, w.ctrl, w.perm, w.meta, w.tiles, a, P, w.rec0, w.rec1, w.rec2, w.rec64a,      \
+             w.rec64b, w.orig, (unsigned)(w.max_cells + 1), w.tiles_h, w.tflag)
   if (!rp) {
     SPH_CELLSORT(none, kRecNone);
   } else if (cfg.precision == SPH_PREC_MIXED) {

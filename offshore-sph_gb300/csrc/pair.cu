@@ -557,6 +557,7 @@ template <int KERNEL, bool XSPH, bool SUMDENS, bool UH>
 __global__ void __launch_bounds__(kPairBlock, kListBlocks)
     k_pair_list(StepArgs a, PairPtrs P, PairParams pp, const int2 *__restrict__ fb, double *dt_out,
                 double *dt_hist) {
+  step_kernel_entry();
   __shared__ unsigned int lists[ListCap<KERNEL>::value][kPairBlock];
   const unsigned int cnt = *(volatile unsigned int *)&P.ctrl->fb_count;
   // only the blocks that have entries take part (at least block 0, which
@@ -1073,6 +1074,7 @@ __global__ void __launch_bounds__(kTileThreads, TileBlocks<KERNEL>::value)
     k_pair_tiles(StepArgs a, PairPtrs P, PairParams pp, const int *__restrict__ tiles,
                  const int *__restrict__ tiles_h, unsigned int tiles_cap,
                  int2 *__restrict__ fb, unsigned int fb_cap) {
+  step_kernel_entry();
   extern __shared__ __align__(128) unsigned char smem_raw[];
   TileShared<KERNEL> &sm = *reinterpret_cast<TileShared<KERNEL> *>(smem_raw);
   const int tid = threadIdx.x;
@@ -1427,11 +1429,10 @@ static void mixed_pair_launch(const StepArgs &a, const WsPtrs &w, const PairPara
   auto tk = k_pair_tiles<KERNEL, XSPH, SUMDENS, UH>;
   static bool done[64] = {false};  // this instantiation's attribute, per device
   const size_t smem = tile_smem(tk, sizeof(TileShared<KERNEL>), done);
-  tk<<<sms * TileBlocks<KERNEL>::value, kTileThreads, smem, st>>>(a, pair_ptrs(w), pp, w.tiles, w.tiles_h,
-                                                                   (unsigned)(w.max_cells + 1), w.fb,
-                                                                   (unsigned)w.fb_cap);
-  k_pair_list<KERNEL, XSPH, SUMDENS, UH><<<sms * kListBlocks, kPairBlock, 0, st>>>(a, pair_ptrs(w), pp, w.fb,
-                                                                                    dt_out, dt_hist);
+  launch_pdl(tk, dim3(sms * TileBlocks<KERNEL>::value), dim3(kTileThreads), smem, st, a, pair_ptrs(w), pp, w.tiles,
+             w.tiles_h, (unsigned)(w.max_cells + 1), w.fb, (unsigned)w.fb_cap);
+  launch_pdl(k_pair_list<KERNEL, XSPH, SUMDENS, UH>, dim3(sms * kListBlocks), dim3(kPairBlock), 0, st, a,
+             pair_ptrs(w), pp, w.fb, dt_out, dt_hist);
 }
 
 template <int KERNEL, bool XSPH, bool SUMDENS>

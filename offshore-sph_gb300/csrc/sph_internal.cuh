@@ -353,8 +353,13 @@ __device__ __forceinline__ long long ref_floor_div(double a, double o, double s,
   double d = a - o;
   double t = d * inv_s;
   double f = floor(t);
-  double fr = t - f;
-  if (fr < 1e-9 || fr > 1.0 - 1e-9) f = floor(__ddiv_rn(d, s));
+  // with a power-of-two cell size (the 1.0 of a scene whose smallest h is
+  // 0) the product by the reciprocal is the exact quotient already
+  const bool pow2 = (__double_as_longlong(s) & 0x000fffffffffffffll) == 0;
+  if (!pow2) {
+    double fr = t - f;
+    if (fr < 1e-9 || fr > 1.0 - 1e-9) f = floor(__ddiv_rn(d, s));
+  }
   return (long long)f;
 }
 static __device__ __noinline__ long long ref_floor_div_slow(double a, double o, double s, double inv_s) {
@@ -772,6 +777,34 @@ int sm_count();
 inline unsigned int persist_blocks(long long n, int per_sm = 8, int bs = kBlock) {
   const unsigned int nb = nblocks(n, bs), cap = (unsigned int)(sm_count() * per_sm);
   return nb < cap ? nb : cap;
+}
+
+// Programmatic dependent launch between the kernels of a step.  A kernel
+// launched with launch_pdl has its launch prepared while the stream's
+// previous kernel runs; it begins with step_kernel_entry(), whose wait holds
+// every thread until that kernel has completed and its writes are visible,
+// so no read or write of shared data moves ahead of it.  No kernel triggers
+// its dependent early (griddepcontrol.launch_dependents): the dependent's
+// blocks would then sit waiting on SMs the running grid still uses, which
+// measured slower than the implicit trigger at completion.  Launched without
+// the attribute, the wait returns at once.  Under stream capture the
+// dependency becomes a programmatic graph edge.
+__device__ __forceinline__ void step_kernel_entry() { asm volatile("griddepcontrol.wait;" ::: "memory"); }
+
+template <typename... KArgs, typename... Args>
+inline cudaError_t launch_pdl(void (*kern)(KArgs...), dim3 grid, dim3 block, size_t smem, cudaStream_t st,
+                              Args &&...args) {
+  cudaLaunchConfig_t cfg = {};
+  cfg.gridDim = grid;
+  cfg.blockDim = block;
+  cfg.dynamicSmemBytes = smem;
+  cfg.stream = st;
+  cudaLaunchAttribute attr[1];
+  attr[0].id = cudaLaunchAttributeProgrammaticStreamSerialization;
+  attr[0].val.programmaticStreamSerializationAllowed = 1;
+  cfg.attrs = attr;
+  cfg.numAttrs = 1;
+  return cudaLaunchKernelEx(&cfg, kern, static_cast<KArgs>(args)...);
 }
 
 struct StepArgs {
