@@ -85,8 +85,9 @@ enum {
   /* TimeStep's dt fell below 1e-6 (the reference records it, src/Solver.py:219-224) */
   SPH_STATUS_SMALL_DT = 1u << 5,
   /* a bounded wait on asynchronous shared-memory copies ran out (the pair
-   * kernels stage with plain loads and stores and do not set it; the bit is
-   * kept so that the values of the others stay fixed) */
+   * kernels stage with per-thread cp.async copies, which each thread waits
+   * for with cp.async.wait_all, and do not set it; the bit is kept so that
+   * the values of the others stay fixed) */
   SPH_STATUS_STAGING_TIMEOUT = 1u << 6
 };
 
@@ -165,8 +166,9 @@ const char *sph_status_string(int code);
 /* Human-readable name of a single device status bit (SPH_STATUS_*). */
 const char *sph_status_bit_string(uint32_t bit);
 
-/* Self-test of the pair kernel's staging primitives (bulk asynchronous copy
- * completing on an mbarrier, and the bounded wait): src64 is 64 bytes of
+/* Self-test of the bulk-copy primitives (a bulk asynchronous copy completing
+ * on an mbarrier, and the bounded wait on it that gives up with a status
+ * instead of hanging): src64 is 64 bytes of
  * device memory, 16-byte aligned; result (device, 2 x uint32) receives
  * {1 if the copy landed intact, 2 if a wait on bytes that never arrive gave
  * up after its bound}.  No host synchronisation. */

@@ -109,8 +109,8 @@ cudaError_t init_workspace(const WsPtrs &w, cudaStream_t st) {
   return cudaGetLastError();
 }
 
-// Self-test of the staging primitives of the pair tile kernel: a 64-byte
-// bulk copy completing on an mbarrier, and a wait on bytes that never come,
+// Self-test of the bulk-copy primitives: a 64-byte bulk copy completing on
+// an mbarrier, and a wait on bytes that never come,
 // which must give up after its bound.  result[0] = 1 when the copy landed
 // intact, result[1] = 2 when the second wait ran out (1 if it completed).
 __global__ void k_selftest_staging(const float4 *src, unsigned int *result) {

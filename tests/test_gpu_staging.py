@@ -1,6 +1,6 @@
-"""The pair tile kernel's staging primitives in isolation (sph_selftest_staging):
-a bulk asynchronous copy that completes on an mbarrier, and a bounded wait
-on bytes that never arrive, which must give up and report instead of hanging."""
+"""The bulk-copy primitives in isolation (sph_selftest_staging): a bulk
+asynchronous copy that completes on an mbarrier, and a bounded wait on bytes
+that never arrive, which must give up and report instead of hanging."""
 import ctypes as C
 
 import pytest
