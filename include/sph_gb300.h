@@ -343,11 +343,15 @@ int sph_newmark_acceleration(int64_t n, int32_t kl, int32_t ku, const double *M,
 int sph_run(sph_particles_t *pa, const sph_wcsph_t *w, const sph_config_t *cfg, const sph_workspace_t *ws, int64_t nsteps,
             double *dt_hist, sph_stream_t stream);
 
-/* sph_run with a CUDA-event lap after every stage, for measurement: the
- * time of each stage summed over the steps, in ms, into
- * stage_ms[SPH_NSTAGES] (host memory).  Synchronises after every stage, so
- * it is slower than sph_run and cannot be captured in a graph.  The stages
- * are the parts of Solver.run's step body (src/Solver.py:366-410). */
+/* sph_run with a CUDA event recorded after every stage, for measurement:
+ * the GPU time of each stage summed over the steps, in ms, into
+ * stage_ms[SPH_NSTAGES] (host memory).  The events are recorded without
+ * waiting on them and read after one synchronisation at the end, so a
+ * stage's interval runs from the previous stage's last kernel to its own
+ * last kernel, with no host round trip inside.  Synchronises once on return
+ * and cannot be captured in a graph.  The stages are the parts of
+ * Solver.run's step body (src/Solver.py:366-410); RECORDS is empty unless
+ * summation density adds its pass (the records are written by the build). */
 enum {
   SPH_STAGE_TIMESTEP = 0, /* initial TimeStep.compute */
   SPH_STAGE_PREDICT = 1,  /* the previous step's integrator.correct, this step's

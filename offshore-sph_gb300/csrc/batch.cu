@@ -160,6 +160,8 @@ int sph_batch_setup(const sph_workspace_t *ws, int64_t n_inst, const int64_t *of
     if (gp.max_cells < 1) gp.max_cells = 1;
     gp.ts_ref_max = SPH_TILE_SHIFT_REF;
     gp.ts_own_max = ts_own;
+    gp.n = p.n;
+    gp.ppc = 0.0;
     p.cfl_c = cfg->cfl_c;
     p.cfl_f = cfg->cfl_f;
   }

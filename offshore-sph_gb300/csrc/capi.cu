@@ -1,6 +1,8 @@
 // capi.cu -- extern "C" entry points of libsph_gb300 (see include/sph_gb300.h).
 #include <string.h>
 
+#include <vector>
+
 #include "sph_internal.cuh"
 
 namespace sph {
@@ -592,44 +594,52 @@ int sph_run_profiled(sph_particles_t *pa, const sph_wcsph_t *w, const sph_config
   const StepArgs a = run_state(caller, wp, *cfg, *w, nsteps, st);
   const bool fixed = cfg->dt_fixed > 0.0;
   double *ring = &wp.ctrl->dt_ring[0][0];
-  cudaEvent_t ev[SPH_NSTAGES + 1];
-  for (int k = 0; k <= SPH_NSTAGES; k++)
-    if (cudaEventCreate(&ev[k]) != cudaSuccess) return SPH_ERR_CUDA;
-  int rc = SPH_OK;
-  auto lap = [&](int stage, int from) {
-    float ms = 0.f;
-    cudaEventRecord(ev[stage + 1], st);
-    cudaEventSynchronize(ev[stage + 1]);
-    cudaEventElapsedTime(&ms, ev[from], ev[stage + 1]);
-    stage_ms[stage] += ms;
+  // one event after every stage, read after the run: mark[k] closes the
+  // interval of stage tag[k] that began at mark[k - 1]
+  std::vector<cudaEvent_t> mark;
+  std::vector<int> tag;
+  mark.reserve((size_t)(4 * nsteps + 3));
+  bool ok = true;
+  auto lap = [&](int stage) {
+    cudaEvent_t e = nullptr;
+    if (cudaEventCreate(&e) != cudaSuccess) {
+      ok = false;
+      return;
+    }
+    cudaEventRecord(e, st);
+    mark.push_back(e);
+    tag.push_back(stage);
   };
-  cudaEventRecord(ev[0], st);
+  lap(-1);
   if (!fixed) launch_timestep(a, wp, *cfg, ring, nullptr, st);
-  lap(SPH_STAGE_TIMESTEP, 0);
+  lap(SPH_STAGE_TIMESTEP);
   for (int64_t s = 0; s < nsteps; s++) {
     double *prev = ring + 3 * ((s + 1) & 1);
     double *cur = ring + 3 * (s & 1);
     double *nxt = ring + 3 * ((s + 1) & 1);
-    cudaEventRecord(ev[0], st);
     launch_bounds(a, wp, *cfg, *w, s == 0 ? kStagePredict : kStageCorrectPredict, true, prev, cur, st);
-    lap(SPH_STAGE_PREDICT, 0);
+    lap(SPH_STAGE_PREDICT);
     const RecParams rp = rec_params(*cfg, *w, true, false, !fixed);
     launch_build(a, wp, *cfg, *w, st, &rp);  // the records pass is fused into the build's last kernel
-    lap(SPH_STAGE_BUILD, SPH_STAGE_PREDICT + 1);
+    lap(SPH_STAGE_BUILD);
     if (w->use_summation_density) {
       launch_sumdens(a, wp, *cfg, *w, st);
       launch_records(a, wp, *cfg, *w, false, true, false, st);
     }
-    lap(SPH_STAGE_RECORDS, SPH_STAGE_BUILD + 1);
+    lap(SPH_STAGE_RECORDS);
     launch_pair(a, wp, *cfg, *w, fixed ? nullptr : nxt, nullptr, st);
-    lap(SPH_STAGE_PAIR, SPH_STAGE_RECORDS + 1);
+    lap(SPH_STAGE_PAIR);
   }
-  cudaEventRecord(ev[SPH_STAGE_PAIR + 1], st);
   launch_correct(a, *cfg, ring + 3 * ((nsteps - 1) & 1), cfg->dt_fixed, st);
   run_finish(caller, a, wp, st);  // the copy back counts with the last corrector
-  lap(SPH_STAGE_CORRECT, SPH_STAGE_PAIR + 1);
-  if (check_launch()) rc = SPH_ERR_CUDA;
-  for (int k = 0; k <= SPH_NSTAGES; k++) cudaEventDestroy(ev[k]);
+  lap(SPH_STAGE_CORRECT);
+  int rc = (ok && check_launch() == SPH_OK && cudaEventSynchronize(mark.back()) == cudaSuccess) ? SPH_OK : SPH_ERR_CUDA;
+  for (size_t k = 1; rc == SPH_OK && k < mark.size(); k++) {
+    float ms = 0.f;
+    if (cudaEventElapsedTime(&ms, mark[k - 1], mark[k]) != cudaSuccess) rc = SPH_ERR_CUDA;
+    stage_ms[tag[k]] += ms;
+  }
+  for (cudaEvent_t e : mark) cudaEventDestroy(e);
   return rc;
 }
 

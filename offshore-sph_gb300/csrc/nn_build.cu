@@ -293,6 +293,8 @@ static GridParams grid_params(const WsPtrs &w, const sph_config_t &cfg, const sp
   gp.max_cells = w.max_cells;
   gp.ts_ref_max = SPH_TILE_SHIFT_REF;
   gp.ts_own_max = SPH_TILE_SHIFT_OWN;
+  gp.n = 0;
+  gp.ppc = 0.0;
   return gp;
 }
 
@@ -315,7 +317,8 @@ void launch_bounds(const StepArgs &a, const WsPtrs &w, const sph_config_t &cfg, 
   bp.damped = cfg.damping != 0.0 ? 1 : 0;
   bp.use_xsph = cfg.pec_use_xsph;
   bp.strict = cfg.pec_strict;
-  const GridParams gp = grid_params(w, cfg, wc);
+  GridParams gp = grid_params(w, cfg, wc);
+  gp.n = a.n;
   const unsigned nb = persist_blocks(a.n, kBoundsBlocks);
   front_dispatch(bp, [&]<int I, int S, bool D, bool X>() {
     launch_pdl(k_bounds<I, S, D, X>, dim3(nb), dim3(kBlock), 0, st, a, w.ctrl, bp, w.grid, gp);
@@ -387,8 +390,24 @@ __device__ unsigned grid_setup(double xmin, double xmax, double ymin, double yma
     }
     return false;
   };
+  // Reference cells: the largest tile shift whose halo (the 3 x 3 stencil
+  // adds one cell on each side) holds, at the particles per cell the previous
+  // build saw, at most 85% of the pair kernel's shared-memory halo, so that
+  // tiles hold enough queries for a tile block without spilling to the
+  // global path.  Without a previous build on reference cells, 4 x 4 cells.
+  int ts_ref = gp.ts_ref_max < 2 ? gp.ts_ref_max : 2;
+  if (gp.ppc > 0.0) {
+    ts_ref = 0;
+    for (int t = gp.ts_ref_max; t > 0; t--) {
+      const double side = (double)((1 << t) + 2);
+      if (gp.ppc * side * side <= 0.85 * SPH_HALO_CAP) {
+        ts_ref = t;
+        break;
+      }
+    }
+  }
   int tsA = 0;
-  const bool fitsA = !huge && tile_fit((double)ncx, (double)ncy, gp.ts_ref_max, tsA);
+  const bool fitsA = !huge && tile_fit((double)ncx, (double)ncy, ts_ref, tsA);
   if (!trunc_free && fitsA) {
     g->mode = 0;
     g->ntx = (int)ncx;
@@ -451,10 +470,14 @@ __device__ void grid_from_bounds(DevCtrl *ctrl, DevGrid *g, const GridParams &gp
   ctrl->xmin = kEncMinId; ctrl->xmax = kEncMaxId; ctrl->ymin = kEncMinId; ctrl->ymax = kEncMaxId;
   ctrl->hmin_all = kEncMinId; ctrl->hmax_new = kEncMaxId;
   ctrl->alias_count = 0;
+  // particles per cell of the previous build's listed tiles (reference cells)
+  GridParams q = gp;
+  const unsigned int ntl = ctrl->tl_count + ctrl->tl_back + ctrl->tl_heavy;
+  q.ppc = (g->valid && g->mode == 0 && ntl > 0u) ? (double)gp.n / ((double)ntl * (double)(1 << (2 * g->ts))) : 0.0;
   ctrl->tl_count = 0;
   ctrl->tl_back = 0;
   ctrl->tl_heavy = 0;
-  const unsigned status = grid_setup(xmin, xmax, ymin, ymax, hmin, hmax, gp, g);
+  const unsigned status = grid_setup(xmin, xmax, ymin, ymax, hmin, hmax, q, g);
   if (status) atomicOr(&ctrl->status, status);
 }
 

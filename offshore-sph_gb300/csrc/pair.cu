@@ -773,9 +773,6 @@ __global__ void __launch_bounds__(kPairBlock)
 constexpr int kTileThreads = 256;   // threads of a tile block (8 warps)
 constexpr int kHaloCellsMax = 400;  // (16 + 2 * 2)^2: 16x16 tiles with a 5x5 stencil
 constexpr int kHaloScanPer = (kHaloCellsMax + 31) / 32;
-#ifndef SPH_HALO_CAP
-#define SPH_HALO_CAP 1024
-#endif
 #ifndef SPH_TILE_UNROLL_PAIRS
 #define SPH_TILE_UNROLL_PAIRS 1
 #endif
@@ -1066,6 +1063,8 @@ __device__ __forceinline__ unsigned long long tile_any(const StepArgs &a, const 
     return tile_process<KERNEL, XSPH, SUMDENS, UH, 4, 2>(a, P, tg, mc, t, part, sm, ctrl, fb, fb_cap);
   if (tg.ts == 3 && tg.W == 2)
     return tile_process<KERNEL, XSPH, SUMDENS, UH, 3, 2>(a, P, tg, mc, t, part, sm, ctrl, fb, fb_cap);
+  if (tg.ts == 3 && tg.W == 1)  // reference cells, 8 x 8 tiles
+    return tile_process<KERNEL, XSPH, SUMDENS, UH, 3, 1>(a, P, tg, mc, t, part, sm, ctrl, fb, fb_cap);
   return tile_process<KERNEL, XSPH, SUMDENS, UH, 0, 0>(a, P, tg, mc, t, part, sm, ctrl, fb, fb_cap);
 }
 

@@ -20,12 +20,18 @@ namespace sph {
 constexpr int kBlock = 256;
 constexpr int kScanTile = 4096;  // cells per scan tile (1024 threads x 4, one uint4 each)
 // largest tile shift of the cell numbering: tiles of 2^s x 2^s cells over the
-// reference grid and over the own grid (0 = plain row-major cells)
+// reference grid and over the own grid (0 = plain row-major cells).  The
+// reference grid's shift adapts to the particles per cell (grid_setup).
 #ifndef SPH_TILE_SHIFT_REF
-#define SPH_TILE_SHIFT_REF 2
+#define SPH_TILE_SHIFT_REF 3
 #endif
 #ifndef SPH_TILE_SHIFT_OWN
 #define SPH_TILE_SHIFT_OWN 4
+#endif
+// particles of one tile's halo that the pair tile kernel stages in shared
+// memory (a larger halo takes the global-memory path)
+#ifndef SPH_HALO_CAP
+#define SPH_HALO_CAP 1024
 #endif
 
 // ---------------------------------------------------------------------------
@@ -216,6 +222,10 @@ struct GridParams {
   int kernel;
   long long max_cells;
   int ts_ref_max, ts_own_max;  // largest tile shifts of the cell numbering
+  long long n;                 // particles of the build
+  // particles per cell of the previous build's listed tiles, when that build
+  // used the reference cells (0: unknown); sets the next reference tile shift
+  double ppc;
 };
 
 struct RecParams {
