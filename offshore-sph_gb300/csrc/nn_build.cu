@@ -467,13 +467,16 @@ __device__ void grid_from_bounds(DevCtrl *ctrl, DevGrid *g, const GridParams &gp
   const double xmin = dec_d(__ldcg(&ctrl->xmin)), xmax = dec_d(__ldcg(&ctrl->xmax));
   const double ymin = dec_d(__ldcg(&ctrl->ymin)), ymax = dec_d(__ldcg(&ctrl->ymax));
   const double hmin = dec_d(__ldcg(&ctrl->hmin_all)), hmax = dec_d(__ldcg(&ctrl->hmax_new));
+  // the previous build's listed tiles and grid, loaded with the bounds
+  const unsigned int ntl = __ldcg(&ctrl->tl_count) + __ldcg(&ctrl->tl_back) + __ldcg(&ctrl->tl_heavy);
+  const bool prev_ref = g->valid && g->mode == 0;
+  const int prev_ts = g->ts;
   ctrl->xmin = kEncMinId; ctrl->xmax = kEncMaxId; ctrl->ymin = kEncMinId; ctrl->ymax = kEncMaxId;
   ctrl->hmin_all = kEncMinId; ctrl->hmax_new = kEncMaxId;
   ctrl->alias_count = 0;
   // particles per cell of the previous build's listed tiles (reference cells)
   GridParams q = gp;
-  const unsigned int ntl = ctrl->tl_count + ctrl->tl_back + ctrl->tl_heavy;
-  q.ppc = (g->valid && g->mode == 0 && ntl > 0u) ? (double)gp.n / ((double)ntl * (double)(1 << (2 * g->ts))) : 0.0;
+  q.ppc = (prev_ref && ntl > 0u) ? (double)gp.n / ((double)ntl * (double)(1 << (2 * prev_ts))) : 0.0;
   ctrl->tl_count = 0;
   ctrl->tl_back = 0;
   ctrl->tl_heavy = 0;

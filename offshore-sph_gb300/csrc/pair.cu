@@ -1063,8 +1063,6 @@ __device__ __forceinline__ unsigned long long tile_any(const StepArgs &a, const 
     return tile_process<KERNEL, XSPH, SUMDENS, UH, 4, 2>(a, P, tg, mc, t, part, sm, ctrl, fb, fb_cap);
   if (tg.ts == 3 && tg.W == 2)
     return tile_process<KERNEL, XSPH, SUMDENS, UH, 3, 2>(a, P, tg, mc, t, part, sm, ctrl, fb, fb_cap);
-  if (tg.ts == 3 && tg.W == 1)  // reference cells, 8 x 8 tiles
-    return tile_process<KERNEL, XSPH, SUMDENS, UH, 3, 1>(a, P, tg, mc, t, part, sm, ctrl, fb, fb_cap);
   return tile_process<KERNEL, XSPH, SUMDENS, UH, 0, 0>(a, P, tg, mc, t, part, sm, ctrl, fb, fb_cap);
 }
 

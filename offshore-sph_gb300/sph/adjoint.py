@@ -18,7 +18,9 @@ replays each segment from its checkpoint, keeping a copy of the workspace
 after every replayed step (its neighbour build and FP64 records), and walks
 the segment in reverse with the hand-written adjoint step
 (``sph_adjoint_step``: the vector-Jacobian product of the fused pair
-evaluation and of PEC), which reuses those builds.  ``adjoint_precision``
+evaluation and of PEC), which reuses those builds.  The replay of the
+segment before runs on a second stream while the walk runs, into the other
+of two sets of workspace copies.  ``adjoint_precision``
 "mixed" runs that product's pair arithmetic in FP32 (the mixed form); the
 forward, the checkpoints and the replay stay FP64, so the loss and its
 finite differences are the FP64 ones.
@@ -73,6 +75,8 @@ class WallLoadCase:
         self.half = DeviceParticles(self.n, device)
         self.fr = torch.zeros(self.n, dtype=torch.float64, device=device)
         self._rows = torch.tensor(_STATE_ROWS, dtype=torch.int64, device=device)
+        # the backward's replays run here, beside the adjoint walk
+        self.replay_stream = torch.cuda.Stream(device=device)
 
     def wcsph(self, alpha):
         return core.wcsph_struct(self.height, self.r0, self.rho0, alpha=float(alpha))
@@ -154,24 +158,45 @@ class WallLoadLoss(torch.autograd.Function):
         lib = L.load()
         K = case.checkpoint
         w0 = case.ws.ws
-        for seg in reversed(range(len(ctx.ckpts))):
-            s0 = seg * K
-            m = min(K, case.nsteps - s0)
-            # replay the segment; after each step the workspace holds that
-            # step's neighbour build and FP64 records, which its adjoint reuses
-            dp._buf.copy_(case.base._buf)
-            case.restore(dp, ctx.ckpts[seg])
-            builds = []
-            for s in range(m):
-                # the same step without the wall-load output (the state is identical)
-                core.run(dp, wc, case.cfg, case.ws, 1)
-                builds.append(case.ws.buf.clone())
-            case.ws.check()
-            for s in reversed(range(m)):
-                ws_s = L.Workspace(ptr=builds[s].data_ptr(), bytes=w0.bytes, n_cap=w0.n_cap, max_cells=w0.max_cells)
+        nseg = len(ctx.ckpts)
+        main, side = torch.cuda.current_stream(dev), case.replay_stream
+        side.wait_stream(main)
+        # Two sets of K workspace copies: while the adjoint walks segment seg
+        # on the main stream (reading set seg % 2), the side stream replays
+        # segment seg - 1 into the other set.  walked[seg]: the main stream
+        # has finished reading segment seg's set.
+        sets = [[torch.empty_like(case.ws.buf) for _ in range(K)] for _ in range(min(2, nseg))]
+        walked = [None] * nseg
+
+        def replay(seg):
+            # after each step the workspace holds that step's neighbour build
+            # and FP64 records, which its adjoint reuses; the same step as the
+            # forward's without the wall-load output (the state is identical)
+            bufs = sets[seg % 2]
+            with torch.cuda.stream(side):
+                if seg + 2 < nseg:
+                    side.wait_event(walked[seg + 2])
+                dp._buf.copy_(case.base._buf)
+                case.restore(dp, ctx.ckpts[seg])
+                for s in range(min(K, case.nsteps - seg * K)):
+                    core.run(dp, wc, case.cfg, case.ws, 1)
+                    bufs[s].copy_(case.ws.buf)
+                return side.record_event()
+
+        ready = replay(nseg - 1)
+        for seg in reversed(range(nseg)):
+            main.wait_event(ready)
+            if seg > 0:
+                ready = replay(seg - 1)
+            bufs = sets[seg % 2]
+            for s in reversed(range(min(K, case.nsteps - seg * K))):
+                ws_s = L.Workspace(ptr=bufs[s].data_ptr(), bytes=w0.bytes, n_cap=w0.n_cap, max_cells=w0.max_cells)
                 L.check(lib.sph_adjoint_step(core._P(case.base), core._P(half), C.byref(wc), C.byref(case.cfg_adj),
                                              C.byref(ws_s), C.byref(cs), current_stream()), "sph_adjoint_step")
-            del builds
+            walked[seg] = main.record_event()
+        main.wait_stream(side)
+        case.ws.check()
+        del sets
         f = case.fluid
         galpha = A["alphab"].sum().reshape(())
         gpos = torch.stack((A["xb"][f], A["yb"][f]), 1)
