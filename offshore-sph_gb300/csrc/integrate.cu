@@ -272,6 +272,7 @@ __device__ unsigned dt_from(double min_h, double max_c, double max_a2, unsigned 
 
 // the initial TimeStep's reductions per instance (min h, max c, max a^2 over fluid)
 __global__ void __launch_bounds__(kBlock) k_bt_timestep(StepArgs a, BatchPtrs B) {
+  step_kernel_entry();
   const long long i = (long long)blockIdx.x * blockDim.x + threadIdx.x;
   unsigned long long eh = kEncMinId, ec = kEncMinId, ea = kEncMinId;  // maxima as minima of the complement
   unsigned int nf = 0;
@@ -298,6 +299,7 @@ __global__ void __launch_bounds__(kBlock) k_bt_timestep(StepArgs a, BatchPtrs B)
 // use_c: max c from the reduction (initial TimeStep), else co (the pair
 // pass's epilogue, where compute_speed_of_sound gives co to every particle)
 __global__ void k_bt_dt_finish(BatchPtrs B, DevCtrl *ctrl, int slot, double *dt_hist, int use_c) {
+  step_kernel_entry();
   unsigned st = 0;
   for (int b = threadIdx.x; b < B.n_inst; b += blockDim.x) {
     InstSlots &s = B.sl[b];
@@ -319,6 +321,7 @@ __global__ void k_bt_dt_finish(BatchPtrs B, DevCtrl *ctrl, int slot, double *dt_
 }
 
 __global__ void __launch_bounds__(kBlock) k_bt_correct(StepArgs a, BatchPtrs B, IntParams ip, int slot) {
+  step_kernel_entry();
   const long long i = (long long)blockIdx.x * blockDim.x + threadIdx.x;
   if (i >= a.n || !is_fluid(a.label[i])) return;
   IntParams q = ip;
@@ -328,16 +331,16 @@ __global__ void __launch_bounds__(kBlock) k_bt_correct(StepArgs a, BatchPtrs B, 
 
 void launch_bt_timestep(const StepArgs &a, const WsPtrs &w, const BatchPtrs &B, int slot, double *dt_hist,
                         cudaStream_t st) {
-  k_bt_timestep<<<nblocks(a.n), kBlock, 0, st>>>(a, B);
-  k_bt_dt_finish<<<1, 256, 0, st>>>(B, w.ctrl, slot, dt_hist, 1);
+  launch_pdl(k_bt_timestep, dim3(nblocks(a.n)), dim3(kBlock), 0, st, a, B);
+  launch_pdl(k_bt_dt_finish, dim3(1), dim3(256), 0, st, B, w.ctrl, slot, dt_hist, 1);
 }
 
 void launch_bt_dt_finish(const WsPtrs &w, const BatchPtrs &B, int slot, double *dt_hist, cudaStream_t st) {
-  k_bt_dt_finish<<<1, 256, 0, st>>>(B, w.ctrl, slot, dt_hist, 0);
+  launch_pdl(k_bt_dt_finish, dim3(1), dim3(256), 0, st, B, w.ctrl, slot, dt_hist, 0);
 }
 
 void launch_bt_correct(const StepArgs &a, const BatchPtrs &B, const sph_config_t &cfg, int slot, cudaStream_t st) {
-  k_bt_correct<<<nblocks(a.n), kBlock, 0, st>>>(a, B, int_params(cfg, nullptr, 0.0), slot);
+  launch_pdl(k_bt_correct, dim3(nblocks(a.n)), dim3(kBlock), 0, st, a, B, int_params(cfg, nullptr, 0.0), slot);
 }
 
 }  // namespace sph

@@ -997,6 +997,7 @@ void launch_records(const StepArgs &a, const WsPtrs &w, const sph_config_t &cfg,
 template <int INTEG, int STAGE, bool DAMPED, bool XSPH>
 __global__ void __launch_bounds__(kBlock) k_bt_bounds(StepArgs a, BatchPtrs B, BoundsParams bp, int prev, int cur,
                                                       DevCtrl *ctrl) {
+  step_kernel_entry();
   const long long i = (long long)blockIdx.x * blockDim.x + threadIdx.x;
   unsigned long long v[6] = {kEncMinId, kEncMinId, kEncMinId, kEncMinId, kEncMinId, kEncMinId};
   bool bad = false;
@@ -1023,6 +1024,7 @@ __global__ void __launch_bounds__(kBlock) k_bt_bounds(StepArgs a, BatchPtrs B, B
 
 // every instance's grids (one thread each), then the cell offsets
 __global__ void k_bt_grid(BatchPtrs B, DevCtrl *ctrl) {
+  step_kernel_entry();
   unsigned status = 0;
   for (int b = threadIdx.x; b < B.n_inst; b += blockDim.x) {
     InstSlots &s = B.sl[b];
@@ -1056,6 +1058,7 @@ __global__ void __launch_bounds__(kBlock) k_bt_keys(const double *__restrict__ x
                                                     int2 *__restrict__ refcell, unsigned int *__restrict__ crank,
                                                     unsigned int *__restrict__ counts,
                                                     unsigned int *__restrict__ part) {
+  step_kernel_entry();
   const long long i = (long long)blockIdx.x * blockDim.x + threadIdx.x;
   const int lane = threadIdx.x & 31;
   const bool act = i < n;
@@ -1094,6 +1097,7 @@ __global__ void __launch_bounds__(kBlock) k_bt_cellsort(const int *__restrict__ 
                                                         int2 *__restrict__ meta, StepArgs a,
                                                         float4 *__restrict__ rec0, float4 *__restrict__ rec1,
                                                         float4 *__restrict__ rec2) {
+  step_kernel_entry();
   const long long k = (long long)blockIdx.x * blockDim.x + threadIdx.x;
   unsigned long long eh = kEncMinId;
   unsigned int nf = 0;
@@ -1140,20 +1144,22 @@ void launch_bt_bounds(const StepArgs &a, const WsPtrs &w, const BatchPtrs &B, co
   bp.use_xsph = cfg.pec_use_xsph;
   bp.strict = cfg.pec_strict;
   front_dispatch(bp, [&]<int I, int S, bool D, bool X>() {
-    k_bt_bounds<I, S, D, X><<<nblocks(a.n), kBlock, 0, st>>>(a, B, bp, prev, cur, w.ctrl);
+    launch_pdl(k_bt_bounds<I, S, D, X>, dim3(nblocks(a.n)), dim3(kBlock), 0, st, a, B, bp, prev, cur, w.ctrl);
   });
 }
 
 // the batched build with the records fused into the in-cell sort
 void launch_bt_build(const StepArgs &a, const WsPtrs &w, const BatchPtrs &B, cudaStream_t st) {
   const unsigned nb = nblocks(a.n);
-  k_bt_grid<<<1, 256, 0, st>>>(B, w.ctrl);
-  k_bt_keys<<<nb, kBlock, 0, st>>>(a.x, a.y, a.n, B, w.ctrl, w.keys, w.refcell, w.crank, w.counts, w.scan_part);
-  k_scan_cells<<<(unsigned)w.n_parts, kScanThreads, 0, st>>>(w.counts, B.scan, w.scan_part, w.cstart);
-  k_scatter_rank<<<nb, kBlock, 0, st>>>(w.keys, w.crank, a.n, w.counts, w.cstart, w.perm_tmp, w.keys_sorted,
-                                        w.scan_part, w.n_parts);
-  k_bt_cellsort<<<nb, kBlock, 0, st>>>(w.perm_tmp, w.keys_sorted, w.cstart, w.refcell, a.n, B, w.ctrl, w.perm, w.meta,
-                                       a, w.rec0, w.rec1, w.rec2);
+  launch_pdl(k_bt_grid, dim3(1), dim3(256), 0, st, B, w.ctrl);
+  launch_pdl(k_bt_keys, dim3(nb), dim3(kBlock), 0, st, a.x, a.y, a.n, B, w.ctrl, w.keys, w.refcell, w.crank,
+             w.counts, w.scan_part);
+  launch_pdl(k_scan_cells, dim3((unsigned)w.n_parts), dim3(kScanThreads), 0, st, w.counts, B.scan, w.scan_part,
+             w.cstart);
+  launch_pdl(k_scatter_rank, dim3(nb), dim3(kBlock), 0, st, w.keys, w.crank, a.n, w.counts, w.cstart, w.perm_tmp,
+             w.keys_sorted, w.scan_part, w.n_parts);
+  launch_pdl(k_bt_cellsort, dim3(nb), dim3(kBlock), 0, st, w.perm_tmp, w.keys_sorted, w.cstart, w.refcell, a.n, B,
+             w.ctrl, w.perm, w.meta, a, w.rec0, w.rec1, w.rec2);
 }
 
 }  // namespace sph

@@ -1149,6 +1149,7 @@ __global__ void __launch_bounds__(kTileThreads, TileBlocks<KERNEL>::value)
 template <int KERNEL, bool XSPH, bool SUMDENS>
 __global__ void __launch_bounds__(kTileThreads, TileBlocks<KERNEL>::value)
     k_bt_pair_tiles(StepArgs a, PairPtrs P, BatchPtrs B, int2 *__restrict__ fb, unsigned int fb_cap) {
+  step_kernel_entry();
   extern __shared__ __align__(128) unsigned char smem_raw[];
   TileShared<KERNEL> &sm = *reinterpret_cast<TileShared<KERNEL> *>(smem_raw);
   const int tid = threadIdx.x;
@@ -1208,6 +1209,7 @@ __global__ void __launch_bounds__(kTileThreads, TileBlocks<KERNEL>::value)
 template <int KERNEL, bool XSPH, bool SUMDENS>
 __global__ void __launch_bounds__(kPairBlock, kListBlocks)
     k_bt_pair_list(StepArgs a, PairPtrs P, BatchPtrs B, const int2 *__restrict__ fb) {
+  step_kernel_entry();
   __shared__ unsigned int lists[ListCap<KERNEL>::value][kPairBlock];
   __shared__ unsigned long long red[kPairBlock / 32];
   const unsigned int cnt = *(volatile unsigned int *)&P.ctrl->fb_count;
@@ -1498,8 +1500,9 @@ static void bt_pair_dispatch(const StepArgs &a, const WsPtrs &w, const BatchPtrs
   auto tk = k_bt_pair_tiles<KERNEL, XSPH, SUMDENS>;
   static bool done[64] = {false};  // this instantiation's attribute, per device
   const size_t smem = tile_smem(tk, sizeof(TileShared<KERNEL>), done);
-  tk<<<sms * tile_blocks, kTileThreads, smem, st>>>(a, pair_ptrs(w), B, w.fb, (unsigned)w.fb_cap);
-  k_bt_pair_list<KERNEL, XSPH, SUMDENS><<<sms * kListBlocks, kPairBlock, 0, st>>>(a, pair_ptrs(w), B, w.fb);
+  launch_pdl(tk, dim3(sms * tile_blocks), dim3(kTileThreads), smem, st, a, pair_ptrs(w), B, w.fb, (unsigned)w.fb_cap);
+  launch_pdl(k_bt_pair_list<KERNEL, XSPH, SUMDENS>, dim3(sms * kListBlocks), dim3(kPairBlock), 0, st, a, pair_ptrs(w),
+             B, w.fb);
 }
 
 void launch_bt_pair(const StepArgs &a, const WsPtrs &w, const BatchPtrs &B, int kernel, bool xsph, int tile_blocks,
