@@ -1038,15 +1038,34 @@ __global__ void k_bt_grid(BatchPtrs B, DevCtrl *ctrl) {
   }
   if (status) atomicOr(&ctrl->status, status);
   __syncthreads();
-  if (threadIdx.x == 0) {
-    int run = 0;
-    for (int b = 0; b < B.n_inst; b++) {
-      const int c = B.coff[b];
-      B.coff[b] = run;
-      run += c;
-    }
-    B.coff[B.n_inst] = run;
-    B.scan->ncells = run - 1;  // the scan kernels cover ids 0 .. run - 1
+  // exclusive prefix of the instances' cell counts: each thread a contiguous
+  // run of instances, then a block scan of the run totals
+  __shared__ int wsum[32];
+  const int per = (B.n_inst + (int)blockDim.x - 1) / (int)blockDim.x;
+  const int b0 = (int)threadIdx.x * per, b1 = min(b0 + per, B.n_inst);
+  int loc = 0;
+  for (int b = b0; b < b1; b++) loc += B.coff[b];
+  const int lane = threadIdx.x & 31, wid = threadIdx.x >> 5, nw = ((int)blockDim.x + 31) >> 5;
+  int inc = loc;
+  for (int d = 1; d < 32; d <<= 1) {
+    const int v = __shfl_up_sync(0xffffffffu, inc, d);
+    if (lane >= d) inc += v;
+  }
+  if (lane == 31) wsum[wid] = inc;
+  __syncthreads();
+  int run = inc - loc;
+  for (int w = 0; w < wid; w++) run += wsum[w];
+  __syncthreads();  // every thread has read the counts of its run
+  for (int b = b0; b < b1; b++) {
+    const int c = B.coff[b];
+    B.coff[b] = run;
+    run += c;
+  }
+  if (threadIdx.x == blockDim.x - 1) {
+    int total = 0;
+    for (int w = 0; w < nw; w++) total += wsum[w];
+    B.coff[B.n_inst] = total;
+    B.scan->ncells = total - 1;  // the scan kernels cover ids 0 .. run - 1
     ctrl->tl_count = 0;
   }
 }

@@ -771,6 +771,7 @@ __global__ void __launch_bounds__(kPairBlock)
 // current tile.
 // ---------------------------------------------------------------------------
 constexpr int kTileThreads = 256;   // threads of a tile block (8 warps)
+static_assert(kTileThreads >= 16 * 16, "a sparse unit's slots fit one per thread");
 constexpr int kHaloCellsMax = 400;  // (16 + 2 * 2)^2: 16x16 tiles with a 5x5 stencil
 constexpr int kHaloScanPer = (kHaloCellsMax + 31) / 32;
 #ifndef SPH_TILE_UNROLL_PAIRS
@@ -856,7 +857,7 @@ template <int KERNEL, bool XSPH, bool SUMDENS, bool UH, int TSC, int WC>
 __device__ __forceinline__ unsigned long long tile_process(const StepArgs &a, const PairPtrs &P, const TileGeom &tg,
                                                            const MixedConsts &mc, int t, int part,
                                                            TileShared<KERNEL> &sm, DevCtrl *ctrl, int2 *fb,
-                                                           unsigned int fb_cap) {
+                                                           unsigned int fb_cap, bool skip_dry) {
   constexpr int kListCap = ListCap<KERNEL>::value;
   const int tid = threadIdx.x;
   const int ts = TSC ? TSC : tg.ts;
@@ -872,7 +873,18 @@ __device__ __forceinline__ unsigned long long tile_process(const StepArgs &a, co
   const unsigned int tb = (unsigned int)t << (2 * ts);  // the tile's first cell (row-major inside)
   const unsigned int qs = __ldg(&cst[tb + row0 * T]), qe = __ldg(&cst[tb + (row0 + rows) * T]);
   const int ox = (t % ntlx) * T - W, oy = (t / ntlx) * T + row0 - W;
-  // 1. halo table: counts and first slots
+  // 1. halo table: counts and first slots.  With skip_dry (the batched form,
+  // whose small tanks hold many tiles of wall particles alone), alongside,
+  // for a sparse unit (less than one particle per cell), whether its own
+  // slots hold a fluid particle (the sign bit of a record's h marks the
+  // others): a unit of boundary particles alone has no query and stages
+  // nothing.  A sparse unit has fewer slots than the block has threads: one
+  // load per thread, issued before the table's loads and used only at the
+  // barrier.  (On the single-scene dam break the test cost more than the
+  // few dry tiles it saves.)
+  const bool dense = !skip_dry || qe - qs >= (unsigned int)(T * rows);
+  float hq0 = -1.f;  // sign bit set: no fluid
+  if (!dense && qs + tid < qe) hq0 = __ldg(&P.rec0[qs + tid].z);
   for (int c = tid; c < HC; c += kTileThreads) {
     const int x = ox + c % HW, y = oy + c / HW;
     unsigned int gs = 0, cnt = 0;
@@ -884,7 +896,7 @@ __device__ __forceinline__ unsigned long long tile_process(const StepArgs &a, co
     hgs[c] = gs;
     hoff[c] = cnt;
   }
-  __syncthreads();
+  if (!__syncthreads_or(dense || !signbit(hq0))) return ea;
   if (tid < 32) {  // 2. exclusive scan of the counts, kHaloScanPer cells per lane
     const int c0 = tid * kHaloScanPer;
     unsigned int v[kHaloScanPer], sum = 0;
@@ -1058,12 +1070,12 @@ template <int KERNEL, bool XSPH, bool SUMDENS, bool UH>
 __device__ __forceinline__ unsigned long long tile_any(const StepArgs &a, const PairPtrs &P, const TileGeom &tg,
                                                        const MixedConsts &mc, int t, int part,
                                                        TileShared<KERNEL> &sm, DevCtrl *ctrl, int2 *fb,
-                                                       unsigned int fb_cap) {
+                                                       unsigned int fb_cap, bool skip_dry) {
   if (tg.ts == 4 && tg.W == 2)
-    return tile_process<KERNEL, XSPH, SUMDENS, UH, 4, 2>(a, P, tg, mc, t, part, sm, ctrl, fb, fb_cap);
+    return tile_process<KERNEL, XSPH, SUMDENS, UH, 4, 2>(a, P, tg, mc, t, part, sm, ctrl, fb, fb_cap, skip_dry);
   if (tg.ts == 3 && tg.W == 2)
-    return tile_process<KERNEL, XSPH, SUMDENS, UH, 3, 2>(a, P, tg, mc, t, part, sm, ctrl, fb, fb_cap);
-  return tile_process<KERNEL, XSPH, SUMDENS, UH, 0, 0>(a, P, tg, mc, t, part, sm, ctrl, fb, fb_cap);
+    return tile_process<KERNEL, XSPH, SUMDENS, UH, 3, 2>(a, P, tg, mc, t, part, sm, ctrl, fb, fb_cap, skip_dry);
+  return tile_process<KERNEL, XSPH, SUMDENS, UH, 0, 0>(a, P, tg, mc, t, part, sm, ctrl, fb, fb_cap, skip_dry);
 }
 
 template <int KERNEL, bool XSPH, bool SUMDENS, bool UH>
@@ -1120,7 +1132,7 @@ __global__ void __launch_bounds__(kTileThreads, TileBlocks<KERNEL>::value)
       if (tid == 0)  // claim the next unit while this one runs
         sm.s_tile[(it + 1) & 1] = claim(atomicAdd(&ctrl->tile_next, 1u));
       const unsigned long long q =
-          tile_any<KERNEL, XSPH, SUMDENS, UH>(a, P, tg, mc, u >> 2, u & 3, sm, ctrl, fb, fb_cap);
+          tile_any<KERNEL, XSPH, SUMDENS, UH>(a, P, tg, mc, u >> 2, u & 3, sm, ctrl, fb, fb_cap, false);
       ea = q > ea ? q : ea;
     }
   }
@@ -1192,8 +1204,8 @@ __global__ void __launch_bounds__(kTileThreads, TileBlocks<KERNEL>::value)
     }
     const MixedConsts mc = mixed_consts<KERNEL>(pp);
     const unsigned long long ea =
-        pp.beta == 0.0 ? tile_any<KERNEL, XSPH, SUMDENS, true>(a, P, tg, mc, t, 0, sm, ctrl, fb, fb_cap)
-                       : tile_any<KERNEL, XSPH, SUMDENS, false>(a, P, tg, mc, t, 0, sm, ctrl, fb, fb_cap);
+        pp.beta == 0.0 ? tile_any<KERNEL, XSPH, SUMDENS, true>(a, P, tg, mc, t, 0, sm, ctrl, fb, fb_cap, true)
+                       : tile_any<KERNEL, XSPH, SUMDENS, false>(a, P, tg, mc, t, 0, sm, ctrl, fb, fb_cap, true);
     const unsigned long long ba = block_max_u64<kTileThreads>(ea, sm.red);
     if (tid == 0 && ba != kEncMaxId) atomicMax(&B.sl[b].pd_a2max, ba);
   }
