@@ -388,8 +388,8 @@ def solver_run_bench(wl, precision="mixed", lengths=(20, 120)):
     (k1, t1), (k2, t2) = runs
     return {"value": nf * (k2 - k1) / (t2 - t1), "unit": UNIT, "precision": precision,
             "steps": [k1, k2], "seconds": [t1, t2], "ms_per_step_steady": (t2 - t1) / (k2 - k1) * 1e3,
-            "how": "sph.Solver.run (settled steps in device chunks of 64 with one host synchronisation each), "
-                   "host clock around run(), steady rate from two run lengths"}
+            "how": "sph.Solver.run (no per-step exports: each settled chunk of up to 256 steps is one device "
+                   "run with one host synchronisation), host clock around run(), steady rate from two run lengths"}
 
 
 def replica_value(el, nfluid, steps, world, device):

@@ -70,7 +70,8 @@ class Solver:
                                              "compute", "time_step", "neighbour_hood", "coupling")}
         self._dp = None
         self._ws = None
-        self._chunk_max = 64  # settled steps per host synchronisation
+        self._chunk_max = 64  # settled steps per host synchronisation, with per-step export fields
+        self._chunk_max_bare = 256  # the same without them (one device run per chunk)
 
     # ------------------------------------------------------------------ state
     def addParticles(self, particles):
@@ -158,6 +159,7 @@ class Solver:
         hist = torch.zeros((max(nsteps, 1), 3), dtype=torch.float64, device=self.device)
         start = perf_counter()
         core.run(self._dp, self.method.wcsph_struct(), self._cfg(damping), self._ws, nsteps, hist)
+        self._table_in_own_order(nsteps)
         h = hist.cpu().numpy()
         self.timing_data["compute"] += perf_counter() - start
         self._ws.check()
@@ -236,12 +238,20 @@ class Solver:
         next incremental write-out, and no more than the remaining time
         allows at the last dt (a chunk that still overshoots is rolled
         back)."""
-        k = self._chunk_max
+        k = self._chunk_max if any(key in FLOAT_FIELDS for key in self.exportProperties) else self._chunk_max_bare
         if self.incrementalWriteout:
             k = min(k, self.incrementalFreq - t_step % self.incrementalFreq)
         if self.dt_a and self.dt_a[-1] > 0:
             k = min(k, max(1, int(0.9 * (self.duration - self.t) / self.dt_a[-1])))
         return max(1, k)
+
+    def _table_in_own_order(self, nsteps):
+        """A device run of four or more steps works on a copy of the state
+        sorted by cell and leaves the neighbour table in that copy's order;
+        the probes read the table of the last build in the solver's own
+        order, so rebuild it."""
+        if nsteps >= 4:
+            core.nn_update(self._dp, self._cfg(), self._ws)
 
     def _device_steps(self, t_step):
         """One settling step, or one chunk of settled steps, of run()'s loop
@@ -257,9 +267,14 @@ class Solver:
             exp = torch.empty((taken, len(need), self._dp.n), dtype=torch.float64, device=self.device) \
                 if need else None
             start = perf_counter()
-            for s in range(taken):
-                core.run(self._dp, wc, cfg, self._ws, 1, hist[s])
-                if exp is not None:
+            if exp is None:
+                # no per-step output: the chunk is one device run (its steps
+                # fused, on the sorted copy), with its dt history
+                core.run(self._dp, wc, cfg, self._ws, taken, hist)
+                self._table_in_own_order(taken)
+            else:
+                for s in range(taken):
+                    core.run(self._dp, wc, cfg, self._ws, 1, hist[s])
                     for j, key in enumerate(need):
                         exp[s, j].copy_(self._dp.fields[key])
             h = hist.cpu().numpy()  # the chunk's one synchronisation

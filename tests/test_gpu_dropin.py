@@ -381,12 +381,12 @@ def test_per_block_method_calls_match_reference(sph):
 
 
 
-def _plain_run(sph, chunk):
+def _plain_run(sph, chunk, export=("x", "y", "p")):
     from sph import scenarios as S
     pa, dx = SC.plain_run_case(S)
     solver = sph.Solver(sph.WCSPH(0.4, dx, 1000.0, False, 0.0), sph.PEC(False, True), sph.CubicSpline(),
                         SC.PLAIN_RUN["duration"], incrementalWriteout=False, h=1.3 * dx,
-                        customSettle=SC.settle_after_three, exportProperties=["x", "y", "p"])
+                        customSettle=SC.settle_after_three, exportProperties=list(export))
     solver._chunk_max = chunk
     solver.addParticles(pa.copy())
     solver.setup()
@@ -421,3 +421,24 @@ def test_solver_plain_run_matches_reference(sph):
     assert one.dt_a == solver.dt_a and one.t_step == solver.t_step
     for k in ("x", "y", "vx", "vy", "rho", "p"):
         assert np.array_equal(one.particleArray[k], fin[k]), k
+
+
+def test_solver_run_without_exports_runs_chunks_as_one_device_run(sph):
+    """Without per-step export fields a settled chunk is one device run (its
+    steps fused, on the sorted copy): the same steps, dt history and final
+    state as the step-by-step chunks, within the reference tolerance of the
+    plain-run case, and a neighbour table in the solver's own order after
+    the run (the probes read it)."""
+    from sph import core
+    ref = _plain_run(sph, 64)
+    bare = _plain_run(sph, 64, export=())
+    assert bare.t_step == ref.t_step and len(bare.dt_a) == len(ref.dt_a)
+    np.testing.assert_allclose(bare.dt_a, ref.dt_a, rtol=1e-9)
+    assert bare.t == pytest.approx(ref.t, rel=1e-9)
+    for k in ("x", "y", "vx", "vy", "rho", "p"):
+        assert SC.rel_err(bare.particleArray[k], ref.particleArray[k]) <= 1e-8, k
+    # the table of the last build refers to the solver's own particle order
+    off, idx = core.nn_export(bare._dp, bare._cfg(), bare._ws)
+    core.nn_update(bare._dp, bare._cfg(), bare._ws)
+    off2, idx2 = core.nn_export(bare._dp, bare._cfg(), bare._ws)
+    assert np.array_equal(np.asarray(off), np.asarray(off2)) and np.array_equal(np.asarray(idx), np.asarray(idx2))
