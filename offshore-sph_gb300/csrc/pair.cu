@@ -205,7 +205,10 @@ __device__ __forceinline__ void mixed_fluid_uh(MixedAcc &acc, const MixedConsts 
   const float d2 = dx * dx + dy * dy;
   if (d2 > u.lim) return;
   const float4 vj = *vjp;
-  const float inv_r = d2 > 0.f ? rsqrtf(d2) : 0.f;
+  // 1/r, and 0 below r = 1e-10 (d2 = 1e-20), where the kernel gradient of
+  // the 2h kernels is taken as 0: the guard on the gradient folds into it
+  const bool g2h = KERNEL == SPH_KERNEL_CUBIC || KERNEL == SPH_KERNEL_WENDLAND;
+  const float inv_r = d2 >= (g2h ? 1e-20f : 0.f) && d2 > 0.f ? rsqrtf(d2) : 0.f;
   const float r = d2 * inv_r;
   const float q = r * u.inv_h;
   const float vxij = (Vi.x - vj.x) + (Vi.z - vj.z);
@@ -216,12 +219,12 @@ __device__ __forceinline__ void mixed_fluid_uh(MixedAcc &acc, const MixedConsts 
     const bool outer = q > 1.0f;
     if (XSPH) w = outer ? u.al * 0.25f * (t2 * t2 * t2) : u.al * (1.0f - 1.5f * (q * q) * (1.0f - 0.5f * q));
     const float g = outer ? u.g0 * (t2 * t2) : q * fmaf(u.g1, q, u.g2);
-    coef = r >= 1e-10f ? g * inv_r : 0.f;
+    coef = g * inv_r;
   } else if (KERNEL == SPH_KERNEL_WENDLAND) {
     const float inner = fmaxf(1.0f - 0.5f * q, 0.f);
     const float i2 = inner * inner, i5 = i2 * i2 * inner;
     if (XSPH) w = u.al * (i5 * inner) * ((35.0f / 12.0f) * q * q + 3.0f * q + 1.0f);
-    coef = r >= 1e-10f ? i5 * q * fmaf(u.g1, q, u.g0) * inv_r : 0.f;
+    coef = i5 * q * fmaf(u.g1, q, u.g0) * inv_r;
   } else {
     const float e = __expf(-q * q);
     if (XSPH) w = u.al * e;
