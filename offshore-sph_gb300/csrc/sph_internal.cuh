@@ -319,7 +319,7 @@ struct WsPtrs {
   DevGrid *grid;
   int *keys;          // traversal cell of particle i (caller order)
   int2 *refcell;      // raw reference cell (cx, cy) of particle i
-  unsigned int *crank;  // arrival rank of particle i in its cell (this build)
+  unsigned int *crank;  // arrival rank of particle i in its cell (current neighbour build)
   int *perm_tmp;      // unsorted-within-cell permutation
   int *keys_sorted;   // traversal cell of sorted slot k
   int *perm;          // sorted slot -> particle index

@@ -53,8 +53,8 @@ void resolve_entry_points() {
     g_ctx_get_id = (ctx_get_id_fn)f;
 }
 
-// unique id of the current context (0 when none is current or the driver
-// does not say)
+// unique id of the current context (0 when none is current or the CUDA
+// driver does not say)
 unsigned long long current_context_id() {
   if (!g_ctx_get_current || !g_ctx_get_id) return 0;
   CUcontext ctx = nullptr;
