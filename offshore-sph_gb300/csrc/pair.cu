@@ -853,9 +853,9 @@ struct TileShared {
 // (the own grid's 16x16 tiles with a 5x5 stencil), so that the halo
 // coordinate arithmetic has no integer division; 0 takes them from tg.
 // UH: every fluid particle has the same h (UniformQ).
-// part: 0 the whole tile; 1 and 2 its first and second half of cell rows
-// (the kernel's last tiles are split so that its final round of work is
-// short).
+// part: 0 the whole tile; 1 and 2 its first and second half of cell rows;
+// 3 to 6 its four quarters (the kernel's last tiles are split so that its
+// final round of work is short).
 template <int KERNEL, bool XSPH, bool SUMDENS, bool UH, int TSC, int WC>
 __device__ __forceinline__ unsigned long long tile_process(const StepArgs &a, const PairPtrs &P, const TileGeom &tg,
                                                            const MixedConsts &mc, int t, int part,
@@ -866,7 +866,8 @@ __device__ __forceinline__ unsigned long long tile_process(const StepArgs &a, co
   const int ts = TSC ? TSC : tg.ts;
   const int W = TSC ? WC : tg.W;
   const int T = 1 << ts, HW = T + 2 * W;
-  const int rows = part ? T >> 1 : T, row0 = part == 2 ? T >> 1 : 0;
+  const int rows = part == 0 ? T : (part <= 2 ? T >> 1 : T >> 2);
+  const int row0 = part == 2 ? T >> 1 : (part >= 3 ? (part - 3) * (T >> 2) : 0);
   const int HWy = rows + 2 * W, HC = HW * HWy;
   const int ntlx = tg.ntlx;
   float4 *h0 = sm.h0, *h1 = sm.h1, *h2 = sm.h2;
@@ -1107,19 +1108,24 @@ __global__ void __launch_bounds__(kTileThreads, TileBlocks<KERNEL>::value)
   } else {
     // Work units in claim order: dense tiles with a wall along a side (their
     // own list), the other dense tiles (listed from the front of the tile
-    // list), then the sparse ones (listed from its back); the last `split`
-    // tiles of that order come as two half-tile units each, so that the
-    // kernel's final round of work is half a tile.  A unit is encoded as
-    // 4 tile + part (part 0: whole tile; 1, 2: halves), -1 when none is left.
+    // list), then the sparse ones (listed from its back).  Of that order, the
+    // last `sq` tiles come as four quarter-tile units each and the `sh`
+    // before them as two half-tile units each, so that the kernel's final
+    // rounds of work are short.  A unit is encoded as 8 tile + part (part 0:
+    // whole tile; 1, 2: halves; 3 to 6: quarters), -1 when none is left.
     const unsigned int nh = ctrl->tl_heavy, ntl = nh + ctrl->tl_count, nall = ntl + ctrl->tl_back;
-    const unsigned int split = (kSplitTail && tg.ts >= 1) ? min(nall, gridDim.x) : 0u;
+    const unsigned int sq = (kSplitTail && tg.ts >= 2) ? min(nall, gridDim.x / 4u) : 0u;
+    const unsigned int sh = (kSplitTail && tg.ts >= 1) ? min(nall - sq, gridDim.x) : 0u;
+    const unsigned int nw = nall - sq - sh;  // whole-tile units
     auto tile_at = [&](unsigned int p) {
       return p < nh ? tiles_h[p] : (p < ntl ? tiles[p - nh] : tiles[tiles_cap - 1 - (p - ntl)]);
     };
     auto claim = [&](unsigned int c) {
-      if (c < nall - split) return 4 * tile_at(c);
-      const unsigned int k = c - (nall - split);
-      return k < 2 * split ? 4 * tile_at(nall - split + (k >> 1)) + 1 + (int)(k & 1u) : -1;
+      if (c < nw) return 8 * tile_at(c);
+      c -= nw;
+      if (c < 2 * sh) return 8 * tile_at(nw + (c >> 1)) + 1 + (int)(c & 1u);
+      c -= 2 * sh;
+      return c < 4 * sq ? 8 * tile_at(nw + sh + (c >> 2)) + 3 + (int)(c & 3u) : -1;
     };
     if (tid == 0) {
       if (blockIdx.x == 0) {  // the dump cell (reference-OOB particles) is in no tile
@@ -1135,7 +1141,7 @@ __global__ void __launch_bounds__(kTileThreads, TileBlocks<KERNEL>::value)
       if (tid == 0)  // claim the next unit while this one runs
         sm.s_tile[(it + 1) & 1] = claim(atomicAdd(&ctrl->tile_next, 1u));
       const unsigned long long q =
-          tile_any<KERNEL, XSPH, SUMDENS, UH>(a, P, tg, mc, u >> 2, u & 3, sm, ctrl, fb, fb_cap, false);
+          tile_any<KERNEL, XSPH, SUMDENS, UH>(a, P, tg, mc, u >> 3, u & 7, sm, ctrl, fb, fb_cap, false);
       ea = q > ea ? q : ea;
     }
   }
