@@ -43,10 +43,10 @@ STEP_BYTES = 385    # algorithmic bytes of one PEC step per particle (dt 32 + pr
 # without a profiler, so taken from an ncu capture of the same kernel on the
 # same workload (dram__bytes_read.sum + dram__bytes_write.sum over the
 # particle count), with the capture's date
-TRAFFIC_FROM_PROFILE = {("dambreak1m", "mixed"): (62.9, "2026-12-04, k_pair_tiles, one launch")}
+TRAFFIC_FROM_PROFILE = {("dambreak1m", "mixed"): (62.8, "2026-12-04, k_pair_tiles, one launch")}
 # what bounds the pair kernel instead of HBM, read off the same captures
-LIMITER_FROM_PROFILE = {"mixed": "instruction issue and the shared-memory pipe: 63.3% of active cycles issue, "
-                                 "L1tex 75.8% of peak, DRAM 6.1% of peak (ncu, 2026-12-04)",
+LIMITER_FROM_PROFILE = {"mixed": "instruction issue and the shared-memory pipe: 63.1% of active cycles issue, "
+                                 "L1tex 76.0% of peak, DRAM 6.2% of peak (ncu, 2026-12-04)",
                         "fp64": "FP64 pipe: busy 86.5% of active cycles, DRAM 0.5% of peak (ncu, 2026-12-04)"}
 
 
