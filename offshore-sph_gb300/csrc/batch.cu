@@ -84,6 +84,7 @@ __global__ void k_bt_init_slots(BatchPtrs B) {
     s.xmax = s.ymax = s.hmax_new = s.pd_a2max = s.ts_cmax = kEncMaxId;
     s.pd_nfluid = 0;
     s.alias_count = 0;
+    s.grid_key.set = 0;  // the instance has no grid yet
     for (int p = 0; p < 2; p++)
       for (int q = 0; q < 3; q++) s.dt_ring[p][q] = 0.0;
   }

@@ -328,11 +328,33 @@ void launch_bounds(const StepArgs &a, const WsPtrs &w, const sph_config_t &cfg, 
 
 // ---------------------------------------------------------------------------
 // Grid: the reference grid (NNLinkedList.py:86-127) and the traversal grid.
-// One thread; consumes and resets the bounds slots.
+// One thread; consumes and resets the bounds slots, and sets the grids only
+// when their inputs changed.
 // ---------------------------------------------------------------------------
-// Both grids of one build from its bounds and h range; returns status bits.
+// Tile shift of the reference cells: the largest one whose halo (the 3 x 3
+// stencil adds one cell on each side) holds, at the particles per cell the
+// previous build saw, at most 85% of the pair kernel's shared-memory halo, so
+// that tiles hold enough queries for a tile block without spilling to the
+// global path.  Without a previous build on reference cells, 4 x 4 cells.
+__device__ int ref_tile_shift(const GridParams &gp) {
+  int ts_ref = gp.ts_ref_max < 2 ? gp.ts_ref_max : 2;
+  if (gp.ppc > 0.0) {
+    ts_ref = 0;
+    for (int t = gp.ts_ref_max; t > 0; t--) {
+      const double side = (double)((1 << t) + 2);
+      if (gp.ppc * side * side <= 0.85 * SPH_HALO_CAP) {
+        ts_ref = t;
+        break;
+      }
+    }
+  }
+  return ts_ref;
+}
+
+// Both grids of one build from its bounds and h range, with the reference
+// cells numbered in tiles of at most 2^ts_ref; returns status bits.
 __device__ unsigned grid_setup(double xmin, double xmax, double ymin, double ymax, double hmin, double hmax,
-                               const GridParams &gp, DevGrid *g) {
+                               const GridParams &gp, int ts_ref, DevGrid *g) {
   unsigned status = 0;
   bool fin = isfinite(xmin) && isfinite(xmax) && isfinite(ymin) && isfinite(ymax) && isfinite(hmin) &&
              isfinite(hmax);
@@ -390,22 +412,6 @@ __device__ unsigned grid_setup(double xmin, double xmax, double ymin, double yma
     }
     return false;
   };
-  // Reference cells: the largest tile shift whose halo (the 3 x 3 stencil
-  // adds one cell on each side) holds, at the particles per cell the previous
-  // build saw, at most 85% of the pair kernel's shared-memory halo, so that
-  // tiles hold enough queries for a tile block without spilling to the
-  // global path.  Without a previous build on reference cells, 4 x 4 cells.
-  int ts_ref = gp.ts_ref_max < 2 ? gp.ts_ref_max : 2;
-  if (gp.ppc > 0.0) {
-    ts_ref = 0;
-    for (int t = gp.ts_ref_max; t > 0; t--) {
-      const double side = (double)((1 << t) + 2);
-      if (gp.ppc * side * side <= 0.85 * SPH_HALO_CAP) {
-        ts_ref = t;
-        break;
-      }
-    }
-  }
   int tsA = 0;
   const bool fitsA = !huge && tile_fit((double)ncx, (double)ncy, ts_ref, tsA);
   if (!trunc_free && fitsA) {
@@ -461,6 +467,41 @@ __device__ unsigned grid_setup(double xmin, double xmax, double ymin, double yma
   return status;
 }
 
+// grid_setup, skipped when its inputs equal, bit for bit, those of the grid
+// in use (key): a scene whose walls fix the bounds, at fixed h, keeps its
+// grid from build to build.  Returns the status bits of the setup that made
+// the grid.
+__device__ unsigned grid_setup_keyed(double xmin, double xmax, double ymin, double ymax, double hmin, double hmax,
+                                     const GridParams &gp, DevGrid *g, GridKey *key) {
+  const int ts_ref = ref_tile_shift(gp);
+  const unsigned long long b[6] = {(unsigned long long)__double_as_longlong(xmin),
+                                   (unsigned long long)__double_as_longlong(xmax),
+                                   (unsigned long long)__double_as_longlong(ymin),
+                                   (unsigned long long)__double_as_longlong(ymax),
+                                   (unsigned long long)__double_as_longlong(hmin),
+                                   (unsigned long long)__double_as_longlong(hmax)};
+  const unsigned long long scale = (unsigned long long)__double_as_longlong(gp.scale);
+  const unsigned long long r0 = (unsigned long long)__double_as_longlong(gp.r0);
+  const GridKey k = *key;  // all loads issued before the comparison
+  bool same = (k.set == 1) & (k.ts_ref == ts_ref) & (k.kernel == gp.kernel) & (k.ts_own_max == gp.ts_own_max) &
+              (k.max_cells == gp.max_cells) & (k.scale == scale) & (k.r0 == r0);
+#pragma unroll
+  for (int j = 0; j < 6; j++) same &= (k.b[j] == b[j]);
+  if (same) return k.status;
+  const unsigned status = grid_setup(xmin, xmax, ymin, ymax, hmin, hmax, gp, ts_ref, g);
+#pragma unroll
+  for (int j = 0; j < 6; j++) key->b[j] = b[j];
+  key->scale = scale;
+  key->r0 = r0;
+  key->max_cells = gp.max_cells;
+  key->kernel = gp.kernel;
+  key->ts_ref = ts_ref;
+  key->ts_own_max = gp.ts_own_max;
+  key->status = status;
+  key->set = 1;
+  return status;
+}
+
 // The grid of the next build from the reduced bounds (one thread); the bound
 // slots return to their identities.  Runs in the last block of k_bounds.
 __device__ void grid_from_bounds(DevCtrl *ctrl, DevGrid *g, const GridParams &gp) {
@@ -480,7 +521,7 @@ __device__ void grid_from_bounds(DevCtrl *ctrl, DevGrid *g, const GridParams &gp
   ctrl->tl_count = 0;
   ctrl->tl_back = 0;
   ctrl->tl_heavy = 0;
-  const unsigned status = grid_setup(xmin, xmax, ymin, ymax, hmin, hmax, q, g);
+  const unsigned status = grid_setup_keyed(xmin, xmax, ymin, ymax, hmin, hmax, q, g, &ctrl->grid_key);
   if (status) atomicOr(&ctrl->status, status);
 }
 
@@ -1033,7 +1074,7 @@ __global__ void k_bt_grid(BatchPtrs B, DevCtrl *ctrl) {
     s.xmin = kEncMinId; s.xmax = kEncMaxId; s.ymin = kEncMinId; s.ymax = kEncMaxId;
     s.hmin_all = kEncMinId; s.hmax_new = kEncMaxId;
     s.alias_count = 0;
-    status |= grid_setup(xmin, xmax, ymin, ymax, hmin, hmax, B.ip[b].gp, &B.grids[b]);
+    status |= grid_setup_keyed(xmin, xmax, ymin, ymax, hmin, hmax, B.ip[b].gp, &B.grids[b], &s.grid_key);
     B.coff[b] = B.grids[b].ncells + 1;  // its cells and its dump cell
   }
   if (status) atomicOr(&ctrl->status, status);

@@ -138,6 +138,18 @@ __device__ __forceinline__ int floor_small(float t, float &ft) {
 // Workspace-resident control block: reductions, status, dt ring.  Every
 // reduction slot is returned to its identity by the kernel that consumes it.
 // ---------------------------------------------------------------------------
+// Inputs of the last grid setup on a grid, with the status bits it returned.
+// The setup is a pure function of them, so a build whose inputs match bit for
+// bit keeps the grid as it is.  set = 0 (zeroed workspace): no grid yet.
+struct GridKey {
+  unsigned long long b[6];  // xmin, xmax, ymin, ymax, hmin, hmax (raw bits)
+  unsigned long long scale, r0;  // raw bits
+  long long max_cells;
+  int kernel, ts_ref, ts_own_max;
+  unsigned int status;
+  int set;
+};
+
 struct DevCtrl {
   // bounds of the next neighbour build (all active particles)
   unsigned long long xmin, xmax, ymin, ymax;
@@ -164,6 +176,7 @@ struct DevCtrl {
   unsigned int tl_count, tl_back, tl_heavy;
   unsigned int bounds_done;  // finished blocks of the bounds pass (its last block sets the grid)
   double dt_ring[2][3];  // {dt, dt_c, dt_f} of the step with that parity
+  GridKey grid_key;      // inputs of the grid in use
 };
 
 // the bound slots are consecutive (k_bounds indexes them from xmin)
@@ -264,6 +277,7 @@ struct InstSlots {
   unsigned long long ts_cmax;                                      // initial TimeStep: max c
   unsigned int pd_nfluid, alias_count;
   double dt_ring[2][3];
+  GridKey grid_key;  // inputs of the instance's grid in use
 };
 struct BatchPtrs {
   InstParams *ip;

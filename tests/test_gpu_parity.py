@@ -272,3 +272,31 @@ def test_nn_sets_dam_break_vs_oracle(sph):
     off, idx = core.nn_export(dp, cfg, ws)
     ws.check()
     _assert_same_lists(off, idx, off_r, idx_r)
+
+
+def test_grid_kept_only_while_its_inputs_hold(sph):
+    """One workspace through evaluations whose grid inputs change (the kernel,
+    then the positions) and come back: each is bit-equal to the same
+    evaluation on a fresh workspace, so a grid kept from the previous build
+    is only ever one its inputs would make again."""
+    from sph import _lib
+    core, state = sph
+    meta, init, ev, steps, dts = SC.load_case("solver_tank_cubic")
+    dp, wc, cfg, ws = _setup(meta, init, "fp64")
+    moved = dict(init)
+    moved["x"] = np.asarray(init["x"]) + 0.37
+    moved["y"] = np.asarray(init["y"]) * 1.5
+    seq = [(init, _lib.KERNEL_CUBIC), (init, _lib.KERNEL_CUBIC), (init, _lib.KERNEL_GAUSSIAN),
+           (init, _lib.KERNEL_CUBIC), (moved, _lib.KERNEL_CUBIC), (init, _lib.KERNEL_CUBIC)]
+    for k, (st, kern) in enumerate(seq):
+        cfg.kernel = kern
+        dp.upload_soa(st)
+        core.compute(dp, wc, cfg, ws)
+        ws.check()
+        got = dp.soa(("rho", "drho", "ax", "ay"))
+        dp_f, _, _, ws_f = _setup(meta, st, "fp64")
+        core.compute(dp_f, wc, cfg, ws_f)
+        ws_f.check()
+        ref = dp_f.soa(("rho", "drho", "ax", "ay"))
+        for f in ("rho", "drho", "ax", "ay"):
+            assert np.array_equal(got[f], ref[f]), (k, kern, f)
