@@ -863,6 +863,34 @@ __device__ __forceinline__ void reduce_h_block(unsigned long long eh, unsigned i
   }
 }
 
+// Rank of a slot's particle among the members of its cell, by particle
+// index (ov; all lanes call it, inactive lanes with a key that matches no
+// other lane), for the batched build.  A cell's members sit in consecutive
+// slots, so most cells lie inside one warp: its lanes compare the indices
+// they already hold.  outside_cell_rank adds the members of a cell [s, e)
+// that lie outside the warp's slots [k0, k0 + 32), loaded again.
+__device__ __forceinline__ unsigned int warp_cell_rank(int key, int ov) {
+  const unsigned int peers = __match_any_sync(0xffffffffu, key);
+  const int first = __ffs(peers) - 1, cnt = __popc(peers);
+  const int span = (int)__reduce_max_sync(0xffffffffu, (unsigned)cnt);
+  unsigned int rank = 0;
+  for (int d = 0; d < span; d++) {
+    const int o = __shfl_sync(0xffffffffu, ov, min(first + d, 31));
+    rank += (unsigned)(d < cnt && o < ov);
+  }
+  return rank;
+}
+
+__device__ __forceinline__ unsigned int outside_cell_rank(unsigned int s, unsigned int e, unsigned int k0, int ov,
+                                                          const int *__restrict__ perm_tmp) {
+  unsigned int rank = 0;
+  if (s < k0 || e > k0 + 32u) {
+    for (unsigned int t = s; t < k0; t++) rank += (unsigned)(perm_tmp[t] < ov);
+    for (unsigned int t = k0 + 32u; t < e; t++) rank += (unsigned)(perm_tmp[t] < ov);
+  }
+  return rank;
+}
+
 // In-cell order by particle index (deterministic); the first particle of each
 // non-empty tile also lists its tile for the tile pair kernel.  With REC the
 // same thread then writes the pair records of its final slot (the records
@@ -913,7 +941,9 @@ __global__ void __launch_bounds__(kBlock) k_cellsort(const int *__restrict__ per
     const int v = perm_tmp[k];
     // rank inside the cell by particle index: the caller's index when the
     // run steps on the sorted copy of the state (orig), so that the order,
-    // and with it every sum, is the same as on the caller's arrays
+    // and with it every sum, is the same as on the caller's arrays.  (The
+    // batched form's warp-shuffle rank measured slower here: build stage
+    // 70.6 against 69.2 us on the 1M-fluid dam break.)
     unsigned int rank = 0;
     if (orig) {
       const int ov = orig[v];
@@ -1162,12 +1192,14 @@ __global__ void __launch_bounds__(kBlock) k_bt_cellsort(const int *__restrict__ 
   unsigned long long eh = kEncMinId;
   unsigned int nf = 0;
   int b = -1;
-  if (k < n) {
-    const int key = keys_sorted[k];
+  const int lane = threadIdx.x & 31;
+  const bool act = k < n;
+  const int key = act ? keys_sorted[k] : -1 - lane;  // inactive lanes match no other lane
+  const int v = act ? perm_tmp[k] : 0;
+  unsigned int rank = warp_cell_rank(key, v);
+  if (act) {
     const unsigned int s = cstart[key], e = cstart[key + 1];
-    const int v = perm_tmp[k];
-    unsigned int rank = 0;
-    for (unsigned int t = s; t < e; t++) rank += (unsigned)(perm_tmp[t] < v);
+    rank += outside_cell_rank(s, e, (unsigned int)(k - lane), v, perm_tmp);
     const unsigned int slot = s + rank;
     perm[slot] = v;
     meta[slot] = refcell[v];

@@ -71,24 +71,46 @@ __device__ __forceinline__ void timestep_epilogue(DevCtrl *ctrl, unsigned long l
                                                   unsigned int nblocks = 0 /* 0: every block of the grid */) {
   __shared__ unsigned long long red[kPairBlock / 32];
   __shared__ bool last;
+  const unsigned int nb = nblocks ? nblocks : gridDim.x;
   const unsigned long long wm = warp_max_u64(ea);
   if ((threadIdx.x & 31) == 0) red[threadIdx.x >> 5] = wm;
   __syncthreads();
+  unsigned long long ba = kEncMaxId;
   if (threadIdx.x == 0) {
-    unsigned long long ba = kEncMaxId;
     for (int w = 0; w < (int)(blockDim.x >> 5); w++) ba = red[w] > ba ? red[w] : ba;
-    if (ba != kEncMaxId) atomicMax(&ctrl->pd_a2max, ba);
-    __threadfence();
-    last = atomicAdd(&ctrl->done_pair, 1u) == (nblocks ? nblocks : gridDim.x) - 1;
+    if (nb == 1) {
+      last = true;
+    } else {
+      if (ba != kEncMaxId) atomicMax(&ctrl->pd_a2max, ba);
+      __threadfence();
+      last = atomicAdd(&ctrl->done_pair, 1u) == nb - 1;
+    }
   }
   __syncthreads();
   if (last && threadIdx.x == 0) {
-    __threadfence();
-    const double min_h = dec_d(atomicExch(&ctrl->pd_hmin, kEncMinId));
-    const double max_a2 = dec_d(atomicExch(&ctrl->pd_a2max, kEncMaxId));
-    const unsigned int cnt = atomicExch(&ctrl->pd_nfluid, 0u);
-    atomicExch(&ctrl->done_pair, 0u);
+    unsigned long long eh, ea2;
+    unsigned int cnt;
+    if (nb == 1) {
+      // the only block: the other contributions came from kernels that
+      // completed before this one started, so plain loads see them (one
+      // round trip instead of a fence and a chain of returning atomics)
+      eh = __ldcg(&ctrl->pd_hmin);
+      ea2 = __ldcg(&ctrl->pd_a2max);
+      cnt = __ldcg(&ctrl->pd_nfluid);
+      ea2 = ba > ea2 ? ba : ea2;
+      ctrl->pd_hmin = kEncMinId;
+      ctrl->pd_a2max = kEncMaxId;
+      ctrl->pd_nfluid = 0u;
+    } else {
+      __threadfence();
+      eh = atomicExch(&ctrl->pd_hmin, kEncMinId);
+      ea2 = atomicExch(&ctrl->pd_a2max, kEncMaxId);
+      cnt = atomicExch(&ctrl->pd_nfluid, 0u);
+      atomicExch(&ctrl->done_pair, 0u);
+    }
     if (zero_on_last) *zero_on_last = 0u;
+    const double min_h = dec_d(eh);
+    const double max_a2 = dec_d(ea2);
     const double max_c = co;  // compute_speed_of_sound gives co to every particle (WCSPH.py:110-129)
     double dc = __ddiv_rn(__dmul_rn(cfl_c, min_h), max_c);
     double df = max_a2 < 1e-12 ? 1e10 : __dmul_rn(cfl_f, __dsqrt_rn(__ddiv_rn(min_h, max_a2)));
