@@ -240,6 +240,9 @@ struct GridParams {
   // used the reference cells (0: unknown); sets the next reference tile shift
   double ppc;
 };
+// grid_setup_keyed skips the setup when the GridKey of the grid in use holds
+// the same inputs: a field added here that grid_setup reads must join the key
+static_assert(sizeof(GridParams) == 56, "a new GridParams field must be compared by grid_setup_keyed");
 
 struct RecParams {
   double h_fixed, gamma, B, inv_rho0, Pb, co;
