@@ -425,9 +425,10 @@ int sph_probe_density(const sph_particles_t *pa, const sph_wcsph_t *w, int kerne
 }
 
 static void compute_body(const StepArgs &a, const WsPtrs &w, const sph_wcsph_t &wc, const sph_config_t &cfg,
-                         double *dt_out, double *dt_hist, cudaStream_t st, const WallLoad *wall = nullptr) {
+                         double *dt_out, double *dt_hist, cudaStream_t st, const WallLoad *wall = nullptr,
+                         bool write_state = true) {
   const bool do_dt = dt_out != nullptr || dt_hist != nullptr;
-  const RecParams rp = rec_params(cfg, wc, true, false, do_dt);
+  const RecParams rp = rec_params(cfg, wc, write_state, false, do_dt);
   launch_build(a, w, cfg, wc, st, &rp);
   if (wc.use_summation_density) {
     launch_sumdens(a, w, cfg, wc, st);
@@ -497,6 +498,18 @@ static void run_finish(const StepArgs &a, const StepArgs &b, const WsPtrs &wp, c
   k_shadow_scatter<<<nblocks(a.n), kBlock, 0, st>>>(b, a, wp.orig);
 }
 
+// Whether step s of a run of nsteps writes p, c and the fluid h back to the
+// state.  The first step does: the next bounds pass reads h.  The last does:
+// the caller sees the state.  In between, with a fixed h and no summation
+// density, no kernel of the run reads p or c (the pair records hold p from
+// the EOS, the TimeStep takes c = co), and the values c = co and fluid
+// h = h_fixed repeat what the first step wrote, so those steps skip the
+// stores; the state after the run is the same.
+static bool step_writes_state(const sph_wcsph_t &wc, const sph_config_t &cfg, int64_t s, int64_t nsteps) {
+  const bool repeat = cfg.h_fixed > 0.0 && !wc.use_summation_density;
+  return !repeat || s == 0 || s + 1 == nsteps;
+}
+
 int sph_run(sph_particles_t *pa, const sph_wcsph_t *w, const sph_config_t *cfg, const sph_workspace_t *ws,
             int64_t nsteps, double *dt_hist, sph_stream_t stream) {
   if (!particles_ok(pa) || !w || !config_ok(cfg) || nsteps < 0) return SPH_ERR_INVALID_ARGUMENT;
@@ -522,7 +535,8 @@ int sph_run(sph_particles_t *pa, const sph_wcsph_t *w, const sph_config_t *cfg, 
     double *nxt = ring + 3 * ((s + 1) & 1);
     launch_bounds(a, wp, *cfg, *w, s == 0 ? kStagePredict : kStageCorrectPredict, true, prev, cur, st);
     double *hist_next = (dt_hist && !fixed && s + 1 < nsteps) ? dt_hist + 3 * (s + 1) : nullptr;
-    compute_body(a, wp, *w, *cfg, fixed ? nullptr : nxt, hist_next, st);
+    compute_body(a, wp, *w, *cfg, fixed ? nullptr : nxt, hist_next, st, nullptr,
+                 step_writes_state(*w, *cfg, s, nsteps));
   }
   launch_correct(a, *cfg, ring + 3 * ((nsteps - 1) & 1), cfg->dt_fixed, st);
   run_finish(caller, a, wp, st);
@@ -619,7 +633,7 @@ int sph_run_profiled(sph_particles_t *pa, const sph_wcsph_t *w, const sph_config
     double *nxt = ring + 3 * ((s + 1) & 1);
     launch_bounds(a, wp, *cfg, *w, s == 0 ? kStagePredict : kStageCorrectPredict, true, prev, cur, st);
     lap(SPH_STAGE_PREDICT);
-    const RecParams rp = rec_params(*cfg, *w, true, false, !fixed);
+    const RecParams rp = rec_params(*cfg, *w, step_writes_state(*w, *cfg, s, nsteps), false, !fixed);
     launch_build(a, wp, *cfg, *w, st, &rp);  // the records pass is fused into the build's last kernel
     lap(SPH_STAGE_BUILD);
     if (w->use_summation_density) {

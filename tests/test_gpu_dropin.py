@@ -437,6 +437,10 @@ def test_solver_run_without_exports_runs_chunks_as_one_device_run(sph):
     assert bare.t == pytest.approx(ref.t, rel=1e-9)
     for k in ("x", "y", "vx", "vy", "rho", "p"):
         assert SC.rel_err(bare.particleArray[k], ref.particleArray[k]) <= 1e-8, k
+    # c and the fixed h as the step-by-step chunks left them (the fused run
+    # writes them back on its first and last steps only)
+    for k in ("c", "h"):
+        assert np.array_equal(bare.particleArray[k], ref.particleArray[k]), k
     # the table of the last build refers to the solver's own particle order
     off, idx = core.nn_export(bare._dp, bare._cfg(), bare._ws)
     core.nn_update(bare._dp, bare._cfg(), bare._ws)
