@@ -339,7 +339,10 @@ int sph_newmark_acceleration(int64_t n, int32_t kl, int32_t ku, const double *M,
  * sorted order of a first neighbour build and scattered back at the end;
  * the results are the same, bit for bit.  The workspace's neighbour table
  * then refers to that copy: call sph_nn_update before sph_nn_count,
- * sph_nn_export or the probes. */
+ * sph_nn_export or the probes.  p, c and h are those of the last step, as
+ * after nsteps single-step runs; with a fixed h and no summation density
+ * the steps between the first and the last do not store them (no kernel of
+ * the run reads them). */
 int sph_run(sph_particles_t *pa, const sph_wcsph_t *w, const sph_config_t *cfg, const sph_workspace_t *ws, int64_t nsteps,
             double *dt_hist, sph_stream_t stream);
 
