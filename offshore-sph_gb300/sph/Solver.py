@@ -385,30 +385,33 @@ class Solver:
 
     def save(self, location: str, printLocation: bool = True, extraProperties: dict = None):
         """Solver.save (Solver.py:497-531): the HDF5 layout of the reference
-        (particleArray, dt_a, dt_c, dt_f, settleTime, one dataset per export
-        key); written with h5py, or as an .npz of the same datasets when h5py
-        is not installed."""
+        (particleArray, dt_a, dt_c, dt_f and one dataset per export key,
+        gzip-compressed with the shuffle filter; settleTime and the extra
+        properties plain); written with h5py, or as an .npz of the same
+        datasets when h5py is not installed."""
         if self._dp is not None:
             self._download()
-        data = {"particleArray": self.particleArray, "dt_a": np.asarray(self.dt_a), "dt_c": np.asarray(self.dt_c),
-                "dt_f": np.asarray(self.dt_f), "settleTime": np.asarray(self.settleTime)}
+        packed = {"particleArray": self.particleArray, "dt_a": np.asarray(self.dt_a), "dt_c": np.asarray(self.dt_c),
+                  "dt_f": np.asarray(self.dt_f)}
         for key in self.exportProperties:
             if self.export.get(key):
-                data[key] = np.stack(self.export[key])
+                packed[key] = np.stack(self.export[key])
+        plain = {"settleTime": np.asarray(self.settleTime)}
         if extraProperties:
-            data.update(extraProperties)
+            plain.update(extraProperties)
         try:
             import h5py
         except ImportError:
             h5py = None
         if h5py is not None:
             with h5py.File(location, "w") as h5f:
-                for k, v in data.items():
-                    if np.ndim(v) == 0:
-                        h5f.create_dataset(k, data=v)
-                    else:
-                        h5f.create_dataset(k, data=v, shuffle=True, compression="gzip")
+                for k, v in packed.items():
+                    h5f.create_dataset(k, data=v, shuffle=True, compression="gzip")
+                for k, v in plain.items():
+                    h5f.create_dataset(k, data=v)
         else:
+            data = dict(packed)
+            data.update(plain)
             np.savez_compressed(location if location.endswith(".npz") else location + ".npz", **data)
         if printLocation:
             print('\nExported arrays to: "{0}".'.format(location))

@@ -60,3 +60,68 @@ def test_save_load_without_hdf5(tmp_path, monkeypatch):
     t.load(path + ".npz")
     np.testing.assert_array_equal(t.particleArray, s.particleArray)
     assert t.dt_a == s.dt_a
+
+
+class _StandInDataset:
+    def __init__(self, data, options):
+        self.data = np.asarray(data)
+        self.options = options
+
+    def __getitem__(self, idx):
+        return self.data[idx]
+
+
+class _StandInFile:
+    """The part of h5py.File that Solver.save / Solver.load use: datasets
+    kept in memory per path, with the options they were created with."""
+    files = {}
+
+    def __init__(self, path, mode):
+        if mode == "w":
+            _StandInFile.files[path] = {}
+        self.sets = _StandInFile.files[path]
+
+    def __enter__(self):
+        return self
+
+    def __exit__(self, *exc):
+        return False
+
+    def create_dataset(self, name, data=None, **options):
+        assert name not in self.sets, name
+        self.sets[name] = _StandInDataset(data, options)
+
+    def __getitem__(self, name):
+        return self.sets[name]
+
+
+def test_hdf5_branch_writes_the_reference_layout(tmp_path, monkeypatch):
+    """The h5py branch, run against a stand-in h5py module (neither machine
+    has h5py): the datasets and filter options of src/Solver.py:518-527 --
+    particleArray, dt_a, dt_c, dt_f and the export keys with shuffle + gzip,
+    settleTime and the extra properties plain -- and load reading them back."""
+    import sys
+    import types
+    import sph
+    monkeypatch.setitem(sys.modules, "h5py", types.SimpleNamespace(File=_StandInFile))
+    s = _solver()
+    path = str(tmp_path / "run.hdf5")
+    extra = {"tank_width": np.float64(0.8), "probe_x": np.linspace(0.0, 0.8, 5)}
+    s.save(path, printLocation=False, extraProperties=extra)
+    sets = _StandInFile.files[path]
+    packed = {"particleArray", "dt_a", "dt_c", "dt_f", "x", "y", "p"}
+    assert set(sets) == packed | {"settleTime", "tank_width", "probe_x"}
+    for k in packed:
+        assert sets[k].options == {"shuffle": True, "compression": "gzip"}, k
+    for k in ("settleTime", "tank_width", "probe_x"):
+        assert sets[k].options == {}, k
+    assert sets["particleArray"].data.dtype.itemsize == 154
+    np.testing.assert_array_equal(sets["particleArray"].data, s.particleArray)
+    np.testing.assert_array_equal(sets["x"].data, np.stack(s.export["x"]))
+    np.testing.assert_array_equal(sets["dt_c"].data, s.dt_c)
+    assert float(sets["settleTime"].data) == s.settleTime
+    np.testing.assert_array_equal(sets["probe_x"].data, extra["probe_x"])
+    t = sph.Solver(sph.WCSPH(0.4, 0.025, 1000.0, False, 0.0), sph.PEC(False, True), sph.CubicSpline())
+    t.load(path)
+    np.testing.assert_array_equal(t.particleArray, s.particleArray)
+    assert t.dt_a == s.dt_a and t.dt_c == s.dt_c and t.dt_f == s.dt_f
